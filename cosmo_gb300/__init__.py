@@ -1,0 +1,350 @@
+"""cosmo_gb300: GB300 (sm_103a) configuration-interaction hot path of CoSMo.
+
+Python view of the C ABI in ``include/cosmo_gb300.h`` (ctypes over the in-tree
+``libcosmo_gb300.so``).  The names follow the reference's objects:
+
+* :class:`Problem`          system XML + s.p. states + ESP/VSPX operator terms
+                            (``SM::Make``, ``xReadSPInt``)
+* :class:`ManyBodyStates`   the M-scheme basis (``SM::Many_Body_States``,
+                            ``MakeMBS2``/``Xsysmbs``, ``SM::locate``)
+* :class:`Hamiltonian`      the stored H + lambda J-J+ (``PPMatrix2CSBBlk`` /
+                            ``SparseMatrixCSB``, ``TimesMatrix``, ``ReadDiagonal``)
+* :func:`davidson_diagonalization`  ``DavidsonDiagonalization``
+
+Every failure raises :class:`CosmoError` carrying the C status code.  There is
+no CPU fallback: without the built library or a CUDA device the calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcosmo_gb300.so")
+
+CG_OK = 0
+CG_PREC_FP64, CG_PREC_FP32, CG_PREC_REFINE = 0, 1, 2
+STATUS_NAMES = {0: "CG_OK", -1: "CG_ERR_ARG", -2: "CG_ERR_IO", -3: "CG_ERR_PARSE", -4: "CG_ERR_CUDA",
+                -5: "CG_ERR_NOMEM", -6: "CG_ERR_UNSUPPORTED", -7: "CG_ERR_NOT_CONVERGED",
+                -8: "CG_ERR_TIMEOUT", -9: "CG_ERR_NO_DEVICE", -10: "CG_ERR_INTERNAL"}
+
+
+class CosmoError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class ProblemInfo(C.Structure):
+    _fields_ = [("n_sps", C.c_int32), ("n_neutron_sps", C.c_int32), ("nv", C.c_int32), ("zv", C.c_int32),
+                ("twom", C.c_int32), ("parity", C.c_int32), ("has_jj", C.c_int32), ("jj", C.c_double),
+                ("n_one_body", C.c_int64), ("n_two_body", C.c_int64)]
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("n_sps", C.c_int32), ("n_neutron_sps", C.c_int32), ("sps", C.c_void_p), ("nv", C.c_int32),
+                ("zv", C.c_int32), ("twom", C.c_int32), ("parity", C.c_int32), ("n_one_body", C.c_int64),
+                ("one_keys", C.c_void_p), ("one_vals", C.c_void_p), ("n_two_body", C.c_int64),
+                ("two_keys", C.c_void_p), ("two_vals", C.c_void_p)]
+
+
+class HamiltonianInfo(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("nnz_full", C.c_uint64), ("nnz_upper", C.c_uint64), ("precision", C.c_int32),
+                ("max_row", C.c_int32), ("device_bytes", C.c_uint64), ("build_seconds", C.c_double)]
+
+
+class DavidsonParams(C.Structure):
+    _fields_ = [("nstates", C.c_int32), ("block", C.c_int32), ("lim", C.c_int32), ("maxiter", C.c_int32),
+                ("crite", C.c_double), ("critc", C.c_double), ("critr", C.c_double), ("ortho", C.c_double),
+                ("tol_resid", C.c_double), ("switch_resid", C.c_double), ("precision", C.c_int32),
+                ("verbose", C.c_int32), ("ortho_block", C.c_int32)]
+
+
+class DavidsonStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refine_iterations", C.c_int32), ("matvecs", C.c_int64),
+                ("restarts", C.c_int32), ("converged", C.c_int32), ("ierr", C.c_int32), ("seconds", C.c_double),
+                ("spmm_seconds", C.c_double)]
+
+
+# every symbol the header declares, with its ctypes signature
+_P = C.c_void_p
+_SIGS = {
+    "cg_last_error": (C.c_char_p, []),
+    "cg_version": (C.c_int32, []),
+    "cg_device_count": (C.c_int32, []),
+    "cg_problem_load_xml": (C.c_int32, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
+    "cg_problem_create": (C.c_int32, [C.POINTER(ProblemDesc), C.POINTER(_P)]),
+    "cg_problem_destroy": (None, [_P]),
+    "cg_problem_get_info": (C.c_int32, [_P, C.POINTER(ProblemInfo)]),
+    "cg_problem_sps": (C.c_int32, [_P, _P]),
+    "cg_problem_one_body": (C.c_int32, [_P, _P, _P]),
+    "cg_problem_two_body": (C.c_int32, [_P, _P, _P]),
+    "cg_basis_build": (C.c_int32, [_P, C.POINTER(_P)]),
+    "cg_basis_destroy": (None, [_P]),
+    "cg_basis_dims": (C.c_int32, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]),
+    "cg_basis_states": (C.c_int32, [_P, C.c_uint64, C.c_uint64, _P]),
+    "cg_basis_locate": (C.c_int32, [_P, _P, C.c_uint64, _P]),
+    "cg_basis_write_mbs": (C.c_int32, [_P, C.c_char_p]),
+    "cg_hamiltonian_build": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(_P)]),
+    "cg_hamiltonian_destroy": (None, [_P]),
+    "cg_hamiltonian_get_info": (C.c_int32, [_P, C.POINTER(HamiltonianInfo)]),
+    "cg_hamiltonian_diagonal": (C.c_int32, [_P, _P]),
+    "cg_hamiltonian_upper_rows": (C.c_int32, [_P, C.c_uint64, C.c_uint64, _P, _P, _P]),
+    "cg_hamiltonian_write_hh": (C.c_int32, [_P, C.c_char_p]),
+    "cg_hamiltonian_stream": (_P, [_P]),
+    "cg_spmm": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32]),
+    "cg_spmm_device": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32]),
+    "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
+    "cg_davidson": (C.c_int32, [_P, C.POINTER(DavidsonParams), _P, C.c_int32, _P, _P, _P, _P,
+                                C.POINTER(DavidsonStats)]),
+    "cg_write_ee": (C.c_int32, [C.c_char_p, C.c_int32, C.c_uint64, _P, _P, _P, _P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree library (fails loudly when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise CosmoError(-10, f"{LIB_PATH} is missing: run `python -m cosmo_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != CG_OK:
+        raise CosmoError(status, lib().cg_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def device_count() -> int:
+    return int(lib().cg_device_count())
+
+
+class Problem:
+    """System XML -> s.p. table and forward-ordered m-scheme operator terms."""
+
+    def __init__(self, xml_path: str | None = None, system: str | None = None, _handle=None):
+        if _handle is None:
+            h = _P()
+            _check(lib().cg_problem_load_xml(xml_path.encode(), system.encode() if system else None, C.byref(h)))
+        else:
+            h = _handle
+        self._h = h
+        inf = ProblemInfo()
+        _check(lib().cg_problem_get_info(h, C.byref(inf)))
+        self.info = inf
+
+    @classmethod
+    def from_terms(cls, sps: np.ndarray, n_neutron_sps: int, nv: int, zv: int, twom: int, parity: int,
+                   one_keys, one_vals, two_keys, two_vals) -> "Problem":
+        """Problem from an explicit s.p. table and forward-ordered operator terms."""
+        keep = [np.ascontiguousarray(sps, dtype=np.int32), np.ascontiguousarray(one_keys, dtype=np.int32),
+                np.ascontiguousarray(one_vals, dtype=np.float64), np.ascontiguousarray(two_keys, dtype=np.int32),
+                np.ascontiguousarray(two_vals, dtype=np.float64)]
+        d = ProblemDesc(len(keep[0]), n_neutron_sps, _ptr(keep[0]), nv, zv, twom, parity, len(keep[2]),
+                        _ptr(keep[1]), _ptr(keep[2]), len(keep[4]), _ptr(keep[3]), _ptr(keep[4]))
+        h = _P()
+        _check(lib().cg_problem_create(C.byref(d), C.byref(h)))
+        return cls(_handle=h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().cg_problem_destroy(self._h)
+            self._h = None
+
+    def sps(self) -> np.ndarray:
+        t = np.zeros((self.info.n_sps, 8), dtype=np.int32)
+        _check(lib().cg_problem_sps(self._h, _ptr(t)))
+        return t
+
+    def one_body(self) -> tuple[np.ndarray, np.ndarray]:
+        k = np.zeros((self.info.n_one_body, 2), dtype=np.int32)
+        v = np.zeros(self.info.n_one_body)
+        _check(lib().cg_problem_one_body(self._h, _ptr(k), _ptr(v)))
+        return k, v
+
+    def two_body(self) -> tuple[np.ndarray, np.ndarray]:
+        k = np.zeros((self.info.n_two_body, 4), dtype=np.int32)
+        v = np.zeros(self.info.n_two_body)
+        _check(lib().cg_problem_two_body(self._h, _ptr(k), _ptr(v)))
+        return k, v
+
+
+class ManyBodyStates:
+    """GPU-resident M-scheme basis in the reference's lexicographic order."""
+
+    def __init__(self, problem: Problem):
+        h = _P()
+        _check(lib().cg_basis_build(problem._h, C.byref(h)))
+        self._h = h
+        n = C.c_uint64()
+        N = C.c_int32()
+        _check(lib().cg_basis_dims(h, C.byref(n), C.byref(N)))
+        self.n = int(n.value)
+        self.N = int(N.value)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().cg_basis_destroy(self._h)
+            self._h = None
+
+    def states(self, first: int = 0, count: int | None = None) -> np.ndarray:
+        count = self.n - first if count is None else count
+        z = np.zeros((count, self.N), dtype=np.uint16)
+        _check(lib().cg_basis_states(self._h, first, count, _ptr(z)))
+        return z
+
+    def locate(self, tuples: np.ndarray) -> np.ndarray:
+        t = np.ascontiguousarray(tuples, dtype=np.uint16).reshape(-1, self.N)
+        out = np.zeros(len(t), dtype=np.uint64)
+        _check(lib().cg_basis_locate(self._h, _ptr(t), len(t), _ptr(out)))
+        return out
+
+    def write_mbs(self, path: str) -> None:
+        _check(lib().cg_basis_write_mbs(self._h, path.encode()))
+
+
+class Hamiltonian:
+    """Stored H + lambda J-J+ on the GPU (both triangles, row-sliced)."""
+
+    def __init__(self, problem: Problem, basis: ManyBodyStates, precision: int = CG_PREC_FP64):
+        h = _P()
+        _check(lib().cg_hamiltonian_build(problem._h, basis._h, precision, C.byref(h)))
+        self._h = h
+        self.refresh_info()
+
+    def refresh_info(self):
+        inf = HamiltonianInfo()
+        _check(lib().cg_hamiltonian_get_info(self._h, C.byref(inf)))
+        self.info = inf
+        self.n = int(inf.n)
+        self.precision = int(inf.precision)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().cg_hamiltonian_destroy(self._h)
+            self._h = None
+
+    @property
+    def stream(self) -> int:
+        return int(lib().cg_hamiltonian_stream(self._h) or 0)
+
+    def diagonal(self) -> np.ndarray:
+        d = np.zeros(self.n)
+        _check(lib().cg_hamiltonian_diagonal(self._h, _ptr(d)))
+        return d
+
+    def upper_rows(self, row0: int = 0, nrows: int | None = None):
+        nrows = self.n - row0 if nrows is None else nrows
+        rp = np.zeros(nrows + 1, dtype=np.uint64)
+        _check(lib().cg_hamiltonian_upper_rows(self._h, row0, nrows, _ptr(rp), None, None))
+        cols = np.zeros(int(rp[-1]), dtype=np.uint32)
+        vals = np.zeros(int(rp[-1]))
+        _check(lib().cg_hamiltonian_upper_rows(self._h, row0, nrows, _ptr(rp), _ptr(cols), _ptr(vals)))
+        return rp, cols, vals
+
+    def write_hh(self, path: str) -> None:
+        _check(lib().cg_hamiltonian_write_hh(self._h, path.encode()))
+
+    def times_matrix(self, x: np.ndarray, precision: int | None = None) -> np.ndarray:
+        """y = H x for the columns of x (n x m), like SparseMatrixCSB::TimesMatrix."""
+        x = np.asarray(x, dtype=np.float64)
+        x2 = x.reshape(self.n, -1)
+        m = x2.shape[1]
+        xc = np.ascontiguousarray(x2.T)  # vector k at k*n
+        yc = np.zeros_like(xc)
+        prec = self.precision if precision is None else precision
+        _check(lib().cg_spmm(self._h, _ptr(xc), _ptr(yc), m, prec))
+        return yc.T.reshape(x.shape)
+
+    def spmm_device(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, m: int, precision: int) -> None:
+        _check(lib().cg_spmm_device(self._h, x_ptr, ldx, y_ptr, ldy, m, precision))
+
+
+@dataclass
+class DavidsonResult:
+    eig: np.ndarray
+    de: np.ndarray
+    resid: np.ndarray
+    vecs: np.ndarray | None
+    stats: DavidsonStats
+
+
+def davidson_params(nstates: int, **kw) -> DavidsonParams:
+    p = DavidsonParams()
+    lib().cg_davidson_defaults(C.byref(p), nstates)
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise TypeError(f"unknown Davidson parameter {k}")
+        setattr(p, k, v)
+    return p
+
+
+def davidson_diagonalization(h: Hamiltonian, nstates: int = 10, want_vectors: bool = True,
+                             init: np.ndarray | None = None, **kw) -> DavidsonResult:
+    """Lowest eigenpairs of h (DavidsonDiagonalization, include/kdav/davidson.cxx:168).
+
+    Keyword arguments set :class:`DavidsonParams` fields (block, lim, maxiter,
+    crite, critc, critr, ortho, tol_resid, switch_resid, precision, verbose,
+    ortho_block).  precision defaults to the matrix precision."""
+    kw.setdefault("precision", h.precision)
+    p = davidson_params(nstates, **kw)
+    eig = np.zeros(nstates)
+    de = np.zeros(nstates)
+    res = np.zeros(nstates)
+    vecs = np.zeros((nstates, h.n)) if want_vectors else None
+    st = DavidsonStats()
+    ninit = 0
+    ip = None
+    if init is not None:
+        init = np.ascontiguousarray(np.asarray(init, dtype=np.float64).reshape(-1, h.n))
+        ninit = init.shape[0]
+        ip = _ptr(init)
+    _check(lib().cg_davidson(h._h, C.byref(p), ip, ninit, _ptr(eig), _ptr(de), _ptr(res),
+                             _ptr(vecs) if vecs is not None else None, C.byref(st)))
+    return DavidsonResult(eig, de, res, vecs, st)
+
+
+def write_ee(path: str, eig, de, resid, vecs) -> None:
+    """Write a .EE eigenpair file (Davidson::Save, include/kdav/cdavidson.cpp:327-368)."""
+    eig = np.ascontiguousarray(eig, dtype=np.float64)
+    de = np.ascontiguousarray(de, dtype=np.float64)
+    resid = np.ascontiguousarray(resid, dtype=np.float64)
+    vecs = np.ascontiguousarray(vecs, dtype=np.float64)
+    _check(lib().cg_write_ee(path.encode(), len(eig), vecs.shape[1], _ptr(eig), _ptr(de), _ptr(resid), _ptr(vecs)))
+
+
+def read_ee(path: str):
+    """Read a .EE file: returns (E, dE, resid, vectors)."""
+    with open(path, "rb") as f:
+        cnt = int(np.frombuffer(f.read(4), dtype=np.uint32)[0])
+        E, dE, R, V = [], [], [], []
+        for _ in range(cnt):
+            e, d, r = np.frombuffer(f.read(24), dtype=np.float64)
+            n = int(np.frombuffer(f.read(8), dtype=np.uint64)[0])
+            V.append(np.frombuffer(f.read(8 * n), dtype=np.float64).copy())
+            E.append(e); dE.append(d); R.append(r)
+    return np.array(E), np.array(dE), np.array(R), np.array(V)
+
+
+def read_mbs(path: str) -> np.ndarray:
+    """Read a .mbs basis file (Many_Body_States::Read, include/sm/ManyBodyStates.cxx:209)."""
+    with open(path, "rb") as f:
+        N = int(np.frombuffer(f.read(4), dtype=np.int32)[0])
+        n = int(np.frombuffer(f.read(8), dtype=np.uint64)[0])
+        z = np.frombuffer(f.read(2 * N * n), dtype=np.uint16).reshape(n, N)
+    return z

@@ -1,0 +1,484 @@
+// extern "C" entry points of libcosmo_gb300: status codes in, exceptions never
+// out.  Each call maps to one reference interface (see include/cosmo_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+
+#include "cosmo_gb300.h"
+#include "davidson.h"
+#include "device.h"
+#include "model.h"
+
+struct cg_problem {
+  cg::System sys;
+  cg::Operator op;
+};
+struct cg_basis {
+  cg::Basis b;
+  cg::System sys;
+};
+struct cg_hamiltonian {
+  cg::Hamiltonian h;
+};
+
+namespace {
+thread_local std::string g_err;
+
+template <class F>
+cg_status guard(F&& f) {
+  try {
+    g_err.clear();
+    f();
+    return CG_OK;
+  } catch (const cg::Error& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return CG_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return CG_ERR_INTERNAL;
+  } catch (...) {
+    g_err = "unknown error";
+    return CG_ERR_INTERNAL;
+  }
+}
+
+void require_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    throw cg::Error(CG_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+}
+
+void same_device(int dev) {
+  int cur = -1;
+  CG_CUDA(cudaGetDevice(&cur));
+  if (cur != dev) throw cg::Error(CG_ERR_ARG, "handle belongs to another CUDA device; make it current first");
+}
+
+#define CG_NOT_NULL(p) \
+  if (!(p)) throw cg::Error(CG_ERR_ARG, #p " is NULL")
+}  // namespace
+
+extern "C" {
+
+const char* cg_last_error(void) { return g_err.c_str(); }
+int32_t cg_version(void) { return 100; }
+int32_t cg_device_count(void) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    g_err = cudaGetErrorString(e);
+    return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? 0 : CG_ERR_CUDA;
+  }
+  return n;
+}
+
+// ------------------------------------------------------------- problem
+cg_status cg_problem_load_xml(const char* xml_path, const char* system_name, cg_problem** out) {
+  return guard([&] {
+    CG_NOT_NULL(xml_path);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    auto p = std::make_unique<cg_problem>();
+    p->sys = cg::load_system(xml_path, system_name ? system_name : "");
+    p->op = cg::build_operator(p->sys);
+    *out = p.release();
+  });
+}
+cg_status cg_problem_create(const cg_problem_desc* d, cg_problem** out) {
+  return guard([&] {
+    CG_NOT_NULL(d);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    if (d->n_sps < 1 || d->n_sps > 64 || d->n_neutron_sps < 0 || d->n_neutron_sps > d->n_sps)
+      throw cg::Error(CG_ERR_ARG, "bad s.p. table size");
+    CG_NOT_NULL(d->sps);
+    if (d->nv < 0 || d->zv < 0) throw cg::Error(CG_ERR_ARG, "negative particle number");
+    auto p = std::make_unique<cg_problem>();
+    cg::System& s = p->sys;
+    s.name = "terms";
+    s.nv = d->nv;
+    s.zv = d->zv;
+    s.twom = d->twom;
+    s.parity = d->parity & 1;
+    s.n_neutron_states = d->n_neutron_sps;
+    for (int i = 0; i < d->n_sps; ++i) {
+      const int32_t* r = d->sps + 8 * i;
+      cg::SPState x{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]};
+      bool neutron = i < d->n_neutron_sps;
+      if ((neutron && x.tz2 != 1) || (!neutron && x.tz2 != -1))
+        throw cg::Error(CG_ERR_ARG, "s.p. table must list neutrons (2tz=+1) before protons (2tz=-1)");
+      s.sps.push_back(x);
+    }
+    auto key_ok = [&](int k) { return k >= 0 && k < d->n_sps; };
+    if (d->n_one_body) { CG_NOT_NULL(d->one_keys); CG_NOT_NULL(d->one_vals); }
+    if (d->n_two_body) { CG_NOT_NULL(d->two_keys); CG_NOT_NULL(d->two_vals); }
+    for (int64_t k = 0; k < d->n_one_body; ++k) {
+      int a = d->one_keys[2 * k], b = d->one_keys[2 * k + 1];
+      if (!key_ok(a) || !key_ok(b) || b < a) throw cg::Error(CG_ERR_ARG, "one-body key out of range or not forward");
+      p->op.one[{a, b}] += d->one_vals[k];
+    }
+    for (int64_t k = 0; k < d->n_two_body; ++k) {
+      const int32_t* q = d->two_keys + 4 * k;
+      for (int j = 0; j < 4; ++j)
+        if (!key_ok(q[j])) throw cg::Error(CG_ERR_ARG, "two-body key out of range");
+      bool fwd = q[0] <= q[1] && q[2] <= q[3] && (q[0] < q[2] || (q[0] == q[2] && q[1] <= q[3]));
+      if (!fwd) throw cg::Error(CG_ERR_ARG, "two-body key is not forward ordered");
+      p->op.two[{q[0], q[1], q[2], q[3]}] += d->two_vals[k];
+    }
+    *out = p.release();
+  });
+}
+
+void cg_problem_destroy(cg_problem* p) { delete p; }
+
+cg_status cg_problem_get_info(const cg_problem* p, cg_problem_info* info) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(info);
+    info->n_sps = int32_t(p->sys.sps.size());
+    info->n_neutron_sps = p->sys.n_neutron_states;
+    info->nv = p->sys.nv;
+    info->zv = p->sys.zv;
+    info->twom = p->sys.twom;
+    info->parity = p->sys.parity;
+    info->has_jj = p->sys.has_jj;
+    info->jj = p->sys.jj;
+    info->n_one_body = int64_t(p->op.one.size());
+    info->n_two_body = int64_t(p->op.two.size());
+  });
+}
+
+cg_status cg_problem_sps(const cg_problem* p, int32_t* t) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(t);
+    for (size_t i = 0; i < p->sys.sps.size(); ++i) {
+      const auto& s = p->sys.sps[i];
+      int32_t* r = t + 8 * i;
+      r[0] = s.level; r[1] = s.n; r[2] = s.l; r[3] = s.j2; r[4] = s.m2; r[5] = s.t2; r[6] = s.tz2; r[7] = s.parity;
+    }
+  });
+}
+
+cg_status cg_problem_one_body(const cg_problem* p, int32_t* keys, double* vals) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(keys);
+    CG_NOT_NULL(vals);
+    size_t k = 0;
+    for (auto& kv : p->op.one) {
+      keys[2 * k] = kv.first[0];
+      keys[2 * k + 1] = kv.first[1];
+      vals[k++] = kv.second;
+    }
+  });
+}
+
+cg_status cg_problem_two_body(const cg_problem* p, int32_t* keys, double* vals) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(keys);
+    CG_NOT_NULL(vals);
+    size_t k = 0;
+    for (auto& kv : p->op.two) {
+      for (int j = 0; j < 4; ++j) keys[4 * k + j] = kv.first[j];
+      vals[k++] = kv.second;
+    }
+  });
+}
+
+// ---------------------------------------------------------------- basis
+cg_status cg_basis_build(const cg_problem* p, cg_basis** out) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    require_device();
+    auto b = std::make_unique<cg_basis>();
+    b->sys = p->sys;
+    cg::basis_build(p->sys, b->b);
+    *out = b.release();
+  });
+}
+void cg_basis_destroy(cg_basis* b) { delete b; }
+
+cg_status cg_basis_dims(const cg_basis* b, uint64_t* n, int32_t* np) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    if (n) *n = b->b.n;
+    if (np) *np = b->b.kn + b->b.kp;
+  });
+}
+
+cg_status cg_basis_states(const cg_basis* b, uint64_t first, uint64_t count, uint16_t* tuples) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(tuples);
+    same_device(b->b.device);
+    cg::basis_tuples(b->b, first, count, tuples);
+  });
+}
+
+cg_status cg_basis_locate(const cg_basis* b, const uint16_t* tuples, uint64_t count, uint64_t* out) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(tuples);
+    CG_NOT_NULL(out);
+    int N = b->b.kn + b->b.kp;
+    for (uint64_t k = 0; k < count; ++k) out[k] = cg::basis_locate_host(b->b, tuples + k * N);
+  });
+}
+
+cg_status cg_basis_write_mbs(const cg_basis* b, const char* path) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(path);
+    same_device(b->b.device);
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("cannot write ") + path);
+    int32_t N = b->b.kn + b->b.kp;
+    uint64_t n = b->b.n;
+    f.write(reinterpret_cast<const char*>(&N), 4);
+    f.write(reinterpret_cast<const char*>(&n), 8);
+    const uint64_t chunk = 1ull << 22;
+    std::vector<uint16_t> buf;
+    for (uint64_t s = 0; s < n; s += chunk) {
+      uint64_t c = std::min(chunk, n - s);
+      buf.resize(c * N);
+      cg::basis_tuples(b->b, s, c, buf.data());
+      f.write(reinterpret_cast<const char*>(buf.data()), c * N * 2);
+    }
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("write failed: ") + path);
+  });
+}
+
+// ---------------------------------------------------------- Hamiltonian
+cg_status cg_hamiltonian_build(const cg_problem* p, const cg_basis* b, int32_t precision, cg_hamiltonian** out) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    same_device(b->b.device);
+    if (p->sys.sps.size() != b->sys.sps.size() || p->sys.nv != b->sys.nv || p->sys.zv != b->sys.zv)
+      throw cg::Error(CG_ERR_ARG, "basis was built for another problem");
+    auto h = std::make_unique<cg_hamiltonian>();
+    cg::hamiltonian_build(p->sys, p->op, b->b, precision, h->h);
+    *out = h.release();
+  });
+}
+void cg_hamiltonian_destroy(cg_hamiltonian* h) { delete h; }
+
+cg_status cg_hamiltonian_get_info(const cg_hamiltonian* h, cg_hamiltonian_info* info) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(info);
+    info->n = h->h.n;
+    info->nnz_full = h->h.nnz;
+    info->nnz_upper = h->h.nnz_upper;
+    info->precision = h->h.precision;
+    info->max_row = h->h.max_row;
+    info->device_bytes = h->h.device_bytes();
+    info->build_seconds = h->h.build_seconds;
+  });
+}
+
+cg_status cg_hamiltonian_diagonal(const cg_hamiltonian* h, double* d) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(d);
+    same_device(h->h.device);
+    CG_CUDA(cudaMemcpy(d, h->h.diag.p, h->h.n * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
+cg_status cg_hamiltonian_upper_rows(const cg_hamiltonian* h, uint64_t row0, uint64_t nrows, uint64_t* rowptr,
+                                    uint32_t* cols, double* vals) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(rowptr);
+    same_device(h->h.device);
+    cg::hamiltonian_upper_rows(h->h, row0, nrows, rowptr, cols, vals);
+  });
+}
+
+cg_status cg_hamiltonian_write_hh(const cg_hamiltonian* h, const char* path) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(path);
+    same_device(h->h.device);
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("cannot write ") + path);
+    uint64_t n = h->h.n;
+    f.write(reinterpret_cast<const char*>(&n), 8);
+    const uint64_t chunk = 1 << 16;
+    for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
+      uint64_t nr = std::min(chunk, n - r0);
+      std::vector<uint64_t> rp(nr + 1);
+      cg::hamiltonian_upper_rows(h->h, r0, nr, rp.data(), nullptr, nullptr);
+      std::vector<uint32_t> c(rp[nr]);
+      std::vector<double> v(rp[nr]);
+      cg::hamiltonian_upper_rows(h->h, r0, nr, rp.data(), c.data(), v.data());
+      for (uint64_t r = 0; r < nr; ++r) {
+        uint32_t nz = uint32_t(rp[r + 1] - rp[r]);
+        f.write(reinterpret_cast<const char*>(&nz), 4);
+        for (uint64_t k = rp[r]; k < rp[r + 1]; ++k) {
+          uint64_t ind = c[k];
+          f.write(reinterpret_cast<const char*>(&ind), 8);
+        }
+        f.write(reinterpret_cast<const char*>(v.data() + rp[r]), 8 * nz);
+      }
+    }
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("write failed: ") + path);
+  });
+}
+
+void* cg_hamiltonian_stream(const cg_hamiltonian* h) { return h ? static_cast<void*>(h->h.stream) : nullptr; }
+
+// ------------------------------------------------------------------ SpMM
+cg_status cg_spmm(const cg_hamiltonian* h, const double* x, double* y, int32_t m, int32_t precision) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(x);
+    CG_NOT_NULL(y);
+    same_device(h->h.device);
+    cg::spmm_host(h->h, precision, x, y, m);
+  });
+}
+
+cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, void* y, int32_t ldy, int32_t m,
+                         int32_t precision) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(x);
+    CG_NOT_NULL(y);
+    same_device(h->h.device);
+    cg::spmm_launch(h->h, precision, x, ldx, y, ldy, m, h->h.stream);
+  });
+}
+
+// -------------------------------------------------------------- Davidson
+void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
+  if (!prm) return;
+  std::memset(prm, 0, sizeof(*prm));
+  prm->nstates = nstates;
+  prm->block = nstates;
+  prm->lim = nstates + 20;
+  prm->maxiter = 0;
+  prm->crite = 1e-15;
+  prm->critc = 1e-12;
+  prm->critr = 1e-8;
+  prm->ortho = 1e-9;
+  prm->tol_resid = 0.0;
+  prm->switch_resid = 1e-3;
+  prm->precision = CG_PREC_FP64;
+  prm->verbose = 0;
+  prm->ortho_block = 0;
+}
+
+cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
+                      double* eig, double* de, double* resid, double* vecs, cg_davidson_stats* stats) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(prm);
+    CG_NOT_NULL(eig);
+    same_device(h->h.device);
+    int nume = prm->nstates;
+    if (nume < 1 || nume > 16) throw cg::Error(CG_ERR_ARG, "nstates must be in 1..16");
+    if (uint64_t(nume) > h->h.n) throw cg::Error(CG_ERR_ARG, "nstates exceeds the dimension");
+    if (prm->block < 1 || prm->block > nume) throw cg::Error(CG_ERR_ARG, "block must be in 1..nstates");
+    if (prm->lim <= nume || prm->lim > 64) throw cg::Error(CG_ERR_ARG, "lim must be in nstates+1..64");
+    if (n_init < 0 || (n_init > 0 && !init)) throw cg::Error(CG_ERR_ARG, "bad initial vectors");
+    if (prm->precision != CG_PREC_FP64 && prm->precision != CG_PREC_FP32)
+      throw cg::Error(CG_ERR_ARG, "precision must be CG_PREC_FP64 or CG_PREC_FP32");
+    if (prm->precision != h->h.precision)
+      throw cg::Error(CG_ERR_ARG, "Davidson precision must match the stored Hamiltonian precision");
+    const double final_tol = prm->tol_resid > 0 ? prm->tol_resid : prm->critr;
+    cg::DavConfig c;
+    c.nume = nume;
+    c.block = prm->block;
+    c.lim = std::min<int64_t>(prm->lim, int64_t(h->h.n));
+    if (c.lim <= nume) c.lim = nume;
+    c.maxiter = prm->maxiter > 0 ? prm->maxiter : std::max(40 * nume, 200);
+    c.crite = prm->crite;
+    c.critc = prm->critc;
+    c.critr = final_tol;
+    c.ortho = prm->ortho;
+    c.verbose = prm->verbose;
+    c.seq_ortho = !prm->ortho_block;
+    cg::DavidsonRequest rq;
+    rq.nume = nume;
+    rq.init = init;
+    rq.ninit = n_init;
+    rq.vecs_out = vecs;
+    if (prm->precision == CG_PREC_FP64) {
+      c.spmm_prec = CG_PREC_FP64;
+      rq.phase1 = c;
+    } else {
+      cg::DavConfig c1 = c;
+      c1.spmm_prec = CG_PREC_FP32;
+      c1.critr = std::max(prm->switch_resid, final_tol);
+      c1.seq_ortho = false;  // FP32 vectors cannot reach the FP64 overlap threshold one vector at a time
+      rq.phase1 = c1;
+      cg::DavConfig c2 = c;
+      c2.spmm_prec = CG_PREC_REFINE;
+      rq.phase2 = c2;
+      rq.refine = true;
+    }
+    cg::DavResult r = cg::davidson_solve(h->h, rq);
+    const cg::DavOutcome& f = r.final_;
+    for (int i = 0; i < nume; ++i) {
+      eig[i] = f.eig[i];
+      if (de) de[i] = f.de[i];
+      if (resid) resid[i] = f.resid[i];
+    }
+    if (stats) {
+      stats->iterations = r.phase1.iterations + (r.refined ? r.phase2.iterations : 0);
+      stats->refine_iterations = r.refined ? r.phase2.iterations : 0;
+      stats->matvecs = r.phase1.matvecs + (r.refined ? r.phase2.matvecs : 0);
+      stats->restarts = r.phase1.restarts + (r.refined ? r.phase2.restarts : 0);
+      int conv = 0;
+      for (int i = 0; i < nume; ++i) conv += f.resid[i] <= final_tol;
+      stats->converged = conv;
+      stats->ierr = f.ierr;
+      stats->seconds = r.seconds;
+      stats->spmm_seconds = r.phase1.spmm_seconds + (r.refined ? r.phase2.spmm_seconds : 0);
+    }
+  });
+}
+
+// ------------------------------------------------------------- file I/O
+cg_status cg_write_ee(const char* path, int32_t nstates, uint64_t n, const double* eig, const double* de,
+                      const double* resid, const double* vecs) {
+  return guard([&] {
+    CG_NOT_NULL(path);
+    CG_NOT_NULL(eig);
+    CG_NOT_NULL(de);
+    CG_NOT_NULL(resid);
+    CG_NOT_NULL(vecs);
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("cannot write ") + path);
+    uint32_t cnt = uint32_t(nstates);
+    f.write(reinterpret_cast<const char*>(&cnt), 4);
+    for (int i = 0; i < nstates; ++i) {
+      f.write(reinterpret_cast<const char*>(eig + i), 8);
+      f.write(reinterpret_cast<const char*>(de + i), 8);
+      f.write(reinterpret_cast<const char*>(resid + i), 8);
+      f.write(reinterpret_cast<const char*>(&n), 8);
+      f.write(reinterpret_cast<const char*>(vecs + uint64_t(i) * n), 8 * n);
+    }
+    if (!f) throw cg::Error(CG_ERR_IO, std::string("write failed: ") + path);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// Device-side objects shared by the kernels: the resident basis, the stored
+// Hamiltonian and the interaction tables, plus CUDA error plumbing.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "cosmo_gb300.h"
+#include "model.h"
+
+namespace cg {
+
+#define CG_CUDA(call)                                                                            \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      throw ::cg::Error(e_ == cudaErrorMemoryAllocation ? CG_ERR_NOMEM : CG_ERR_CUDA,            \
+                        std::string(#call) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" + \
+                            std::to_string(__LINE__) + ")");                                     \
+  } while (0)
+
+// Owning device buffer.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count) CG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s = 0) {
+    if (count) CG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s = 0) {
+    if (n < h.size()) alloc(h.size());
+    upload(h.data(), h.size(), s);
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Binomial table in constant memory, C(a, b) for a, b < 65.
+constexpr int kBinom = 65;
+
+// ------------------------------------------------------------------ basis
+// Per-species bitstring description: a species has `norb` m-scheme states
+// (bits 0..norb-1 of its mask) and `k` particles.  A configuration's colex rank
+// (sum over set bits c_i, ascending, of C(c_i, i+1)) indexes the small lookup
+// tables; the basis order itself is the reference's lexicographic order.
+struct SpeciesTables {
+  int norb = 0, k = 0;
+  uint64_t nconf = 0;              // C(norb, k)
+  std::vector<uint32_t> lex_mask;  // configurations in lexicographic order
+  std::vector<int> lex_m2, lex_par;
+};
+
+struct Basis {
+  int device = 0;
+  int ns = 0, nn = 0, np = 0;  // s.p. states: total, neutron, proton
+  int kn = 0, kp = 0;          // particles per species
+  int twom = 0, parity = 0;
+  uint64_t n = 0;
+  SpeciesTables neut, prot;
+  std::vector<int> sp_m2, sp_par;  // per global s.p. index
+  // device tables
+  DBuf<uint64_t> state;            // per basis state: combined mask (neutron bits low, proton bits << nn)
+  DBuf<uint64_t> noff;             // by neutron colex rank: first index of that neutron block, ~0 if none
+  DBuf<uint32_t> pcrank;           // by proton colex rank: rank inside its (2m, parity) class
+  DBuf<uint64_t> binom;            // kBinom x kBinom
+  // host copies used for locate and .mbs output
+  std::vector<uint64_t> h_noff;
+  std::vector<uint32_t> h_pcrank;
+  std::vector<uint64_t> h_binom;
+  cudaStream_t stream = nullptr;
+  ~Basis();
+};
+
+void basis_build(const System& sys, Basis& b);
+void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);
+uint64_t basis_locate_host(const Basis& b, const uint16_t* tuple);
+
+// ----------------------------------------------------------- interaction
+struct DevOperator {
+  int ns = 0, npairs = 0;
+  DBuf<double> e1;      // ns x ns, forward one-body terms (i <= f)
+  DBuf<double> v2;      // npairs x npairs, forward two-body terms
+  DBuf<int32_t> pidx;   // ns x ns pair index for a < b
+  DBuf<uint64_t> mmask; // per species (2) x per 2m value (kMOff*2+1): mask of s.p. states
+};
+constexpr int kMOff = 64;  // 2m in [-64, 64]
+
+void upload_operator(const System& sys, const Operator& op, DevOperator& d, cudaStream_t s);
+
+// ----------------------------------------------------------- Hamiltonian
+struct Hamiltonian {
+  int device = 0;
+  int precision = CG_PREC_FP64;
+  uint64_t n = 0, nnz = 0, nnz_upper = 0;
+  int max_row = 0;
+  double build_seconds = 0;
+  DBuf<uint64_t> rowptr;  // n + 1
+  DBuf<uint32_t> col;     // nnz
+  DBuf<double> val64;     // nnz (CG_PREC_FP64)
+  DBuf<float> hi, lo;     // nnz (CG_PREC_FP32)
+  DBuf<double> diag;      // n
+  cudaStream_t stream = nullptr;
+  ~Hamiltonian();
+  uint64_t device_bytes() const {
+    return rowptr.bytes() + col.bytes() + val64.bytes() + hi.bytes() + lo.bytes() + diag.bytes();
+  }
+};
+
+void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h);
+void hamiltonian_upper_rows(const Hamiltonian& h, uint64_t row0, uint64_t nrows, uint64_t* rowptr, uint32_t* cols,
+                            double* vals);
+
+// ------------------------------------------------------------------ SpMM
+// Row-interleaved operands: element (i, k) at x[i*ldx + k].
+void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, void* y, int ldy, int m,
+                 cudaStream_t s);
+// Host column-major doubles in and out (vector k at k*n), any m >= 1.
+void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, int m);
+
+}  // namespace cg

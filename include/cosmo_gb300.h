@@ -1,0 +1,224 @@
+/*
+ * cosmo_gb300 — C ABI of the GB300 (sm_103a) configuration-interaction hot path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, every call returns a
+ * status (0 = CG_OK, negative = error; the message is in cg_last_error()).
+ * Nothing throws across this boundary.  Handles are bound to the CUDA device
+ * that was current when they were created; calls on one handle are not
+ * thread-safe.  All large objects (basis, Hamiltonian, Davidson vectors) stay
+ * resident in HBM; host buffers are only touched by the calls that take them.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the reference project, alvolya/cosmo).
+ */
+#ifndef COSMO_GB300_H
+#define COSMO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef int32_t cg_status;
+#define CG_OK 0
+#define CG_ERR_ARG (-1)
+#define CG_ERR_IO (-2)
+#define CG_ERR_PARSE (-3)
+#define CG_ERR_CUDA (-4)
+#define CG_ERR_NOMEM (-5)
+#define CG_ERR_UNSUPPORTED (-6)
+#define CG_ERR_NOT_CONVERGED (-7)
+#define CG_ERR_TIMEOUT (-8)
+#define CG_ERR_NO_DEVICE (-9)
+#define CG_ERR_INTERNAL (-10)
+
+/* precision of a stored Hamiltonian / of an SpMM call */
+#define CG_PREC_FP64 0   /* FP64 values, FP64 vectors                        */
+#define CG_PREC_FP32 1   /* FP32 values and vectors, FP32 in-row, FP64 across */
+#define CG_PREC_REFINE 2 /* FP32 hi + FP32 lo values (~FP64), FP64 vectors    */
+
+/* Last error message of the calling thread ("" if none). */
+const char* cg_last_error(void);
+/* ABI version (major * 100 + minor). */
+int32_t cg_version(void);
+/* Number of CUDA devices visible, or a negative status. */
+int32_t cg_device_count(void);
+
+/* --------------------------------------------------------------- problem */
+/* Host-side CI problem: valence space, s.p. states, system quantum numbers and
+ * the forward-ordered m-scheme operator terms ESP (one-body) and VSPX
+ * (two-body, including lambda * J-J+).
+ * Replaces SM::Make(sps, XMLNode) (include/xsm/xSingleParticleStates.cxx:26)
+ * and xReadSPInt(ESP, VSPX, ...) (include/xsm/xReadSPInt.cxx:24). */
+typedef struct cg_problem cg_problem;
+
+typedef struct {
+  int32_t n_sps;          /* m-scheme s.p. states                          */
+  int32_t n_neutron_sps;  /* sps [0, n_neutron_sps) are neutrons           */
+  int32_t nv, zv;         /* valence neutrons, protons                     */
+  int32_t twom;           /* 2 * Jz                                        */
+  int32_t parity;         /* 0 '+', 1 '-'                                  */
+  int32_t has_jj;         /* matrix JJ attribute present                   */
+  double jj;              /* lambda                                        */
+  int64_t n_one_body;     /* ESP terms                                     */
+  int64_t n_two_body;     /* VSPX terms                                    */
+} cg_problem_info;
+
+/* system_name may be NULL when the XML holds one <system>. */
+cg_status cg_problem_load_xml(const char* xml_path, const char* system_name, cg_problem** out);
+
+/* A problem from explicit operator terms, as SM::PPMatrix is assembled from
+ * any set of MBOperator components (include/sm/PPMatrix.cxx:42-60, pushed in
+ * include/xsm/DEXHVcsb.cxx:47-49).  sps: n_sps rows of 8 int32 in the layout of
+ * cg_problem_sps (neutron states first); keys are forward ordered as in
+ * cg_problem_one_body / cg_problem_two_body. */
+typedef struct {
+  int32_t n_sps, n_neutron_sps;
+  const int32_t* sps;
+  int32_t nv, zv, twom, parity;
+  int64_t n_one_body;
+  const int32_t* one_keys;
+  const double* one_vals;
+  int64_t n_two_body;
+  const int32_t* two_keys;
+  const double* two_vals;
+} cg_problem_desc;
+cg_status cg_problem_create(const cg_problem_desc* desc, cg_problem** out);
+void cg_problem_destroy(cg_problem* p);
+cg_status cg_problem_get_info(const cg_problem* p, cg_problem_info* info);
+/* n_sps rows of 8 int32: level n l 2j 2m 2t 2tz parity (SPS, include/sm/SingleParticleStates.cxx:36). */
+cg_status cg_problem_sps(const cg_problem* p, int32_t* table);
+/* Operator terms in key order: keys[2*k], vals[k] (ESP) / keys[4*k], vals[k] (VSPX). */
+cg_status cg_problem_one_body(const cg_problem* p, int32_t* keys, double* vals);
+cg_status cg_problem_two_body(const cg_problem* p, int32_t* keys, double* vals);
+
+/* ----------------------------------------------------------------- basis */
+/* M-scheme Slater-determinant basis, enumerated on the GPU from per-species
+ * bitstrings; index order is the reference's lexicographic order of sorted
+ * s.p. tuples.  Replaces SM::MakeMBS2 (include/sm/MakeMBS.cxx:186) and the
+ * Xsysmbs/XsysmbsOMP tools (xmlshell/xmbs/XsysmbsOMP.cpp:323). */
+typedef struct cg_basis cg_basis;
+
+cg_status cg_basis_build(const cg_problem* p, cg_basis** out);
+void cg_basis_destroy(cg_basis* b);
+/* dimension n and particle number N */
+cg_status cg_basis_dims(const cg_basis* b, uint64_t* n, int32_t* nparticles);
+/* count states from `first` as sorted uint16 tuples (count * N values), host buffer.
+ * Same content as Many_Body_States::z (include/sm/ManyBodyStates.cxx:43-49). */
+cg_status cg_basis_states(const cg_basis* b, uint64_t first, uint64_t count, uint16_t* tuples);
+/* state -> index, the reference's SM::locate (include/sm/ManyBodyStates.cxx:92);
+ * out[k] = n + 1 when tuple k is not in the basis (same sentinel). */
+cg_status cg_basis_locate(const cg_basis* b, const uint16_t* tuples, uint64_t count, uint64_t* out);
+/* write the .mbs file: int32 N, uint64 n, n*N uint16
+ * (Many_Body_States::Write, include/sm/ManyBodyStates.cxx:199-206) */
+cg_status cg_basis_write_mbs(const cg_basis* b, const char* path);
+
+/* ----------------------------------------------------------- Hamiltonian */
+/* H + lambda * J-J+ built on the GPU (count -> scan -> fill -> per-row sort):
+ * every pair of determinants differing by at most two particle-hole moves,
+ * fermionic phases by popcount, |H_ij| < 1e-14 dropped like PPMatrix2CSBBlk
+ * (include/sm/PPMatrix.cxx:571-656, drop at :621).  Both triangles are stored
+ * (row-sliced CSR with 32-bit columns); each element is computed once from the
+ * lower-index determinant with the forward operator, so H is exactly symmetric
+ * and its upper triangle is the reference's CSB content.
+ * precision: CG_PREC_FP64 stores FP64 values; CG_PREC_FP32 stores FP32 hi and
+ * FP32 lo = fl(h - hi) so the same matrix serves CG_PREC_FP32 and
+ * CG_PREC_REFINE products. */
+typedef struct cg_hamiltonian cg_hamiltonian;
+
+typedef struct {
+  uint64_t n;
+  uint64_t nnz_full;     /* stored entries, both triangles              */
+  uint64_t nnz_upper;    /* entries with col >= row (reference CSB nnz) */
+  int32_t precision;     /* CG_PREC_FP64 or CG_PREC_FP32                 */
+  int32_t max_row;       /* longest row                                 */
+  uint64_t device_bytes; /* HBM held by the matrix                      */
+  double build_seconds;  /* device time of the build                    */
+} cg_hamiltonian_info;
+
+cg_status cg_hamiltonian_build(const cg_problem* p, const cg_basis* b, int32_t precision, cg_hamiltonian** out);
+void cg_hamiltonian_destroy(cg_hamiltonian* h);
+cg_status cg_hamiltonian_get_info(const cg_hamiltonian* h, cg_hamiltonian_info* info);
+/* FP64 diagonal, host buffer of n (SparseMatrixCSB::ReadDiagonal, include/tav/csbmatrix.cxx:393). */
+cg_status cg_hamiltonian_diagonal(const cg_hamiltonian* h, double* diag);
+/* Upper triangle (col >= row) of rows [row0, row0 + nrows), columns ascending.
+ * rowptr has nrows + 1 entries (relative to the first exported row); when cols
+ * is NULL only rowptr is filled.  Values are the stored values widened to FP64
+ * (hi + lo for CG_PREC_FP32 matrices). */
+cg_status cg_hamiltonian_upper_rows(const cg_hamiltonian* h, uint64_t row0, uint64_t nrows, uint64_t* rowptr,
+                                    uint32_t* cols, double* vals);
+/* .HH row-sparse file: uint64 n, then per row uint32 nz, uint64 ind[nz], double
+ * elem[nz] (upper triangle incl. diagonal), PPMatrix::Write (include/sm/PPMatrix.cxx:413-465). */
+cg_status cg_hamiltonian_write_hh(const cg_hamiltonian* h, const char* path);
+/* Stream used by this handle's kernels (cudaStream_t), for event timing. */
+void* cg_hamiltonian_stream(const cg_hamiltonian* h);
+
+/* ------------------------------------------------------------------ SpMM */
+/* y = H x for m vectors on host buffers, both n x m column-major (vector k at
+ * offset k*n) as SparseMatrixCSB::TimesMatrix(ftyp* y, ftyp* x, m)
+ * (include/tav/csbmatrix.cxx:680) and MatB::MatrixBase::TimesMatrix
+ * (include/kdav/matrixbase.h:17).  precision selects the product:
+ * CG_PREC_FP64 (FP64 matrix), CG_PREC_FP32 or CG_PREC_REFINE (FP32 matrix). */
+cg_status cg_spmm(const cg_hamiltonian* h, const double* x, double* y, int32_t m, int32_t precision);
+/* Device-resident product on the handle's stream: x and y are row-interleaved
+ * n x ld arrays (element (i, k) at i*ld + k) of float (CG_PREC_FP32) or double
+ * (CG_PREC_FP64, CG_PREC_REFINE); columns [0, m) are used.  Asynchronous. */
+cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, void* y, int32_t ldy, int32_t m,
+                         int32_t precision);
+
+/* -------------------------------------------------------------- Davidson */
+/* Block Davidson for the lowest eigenpairs (Davidson-Liu with diagonal
+ * preconditioning, classical Gram-Schmidt with re-orthogonalisation, restart by
+ * collapse), the algorithm of dvdrvr2 (include/kdav/fsdavidson.cxx:615-775)
+ * driven by DavidsonDiagonalization (include/kdav/davidson.cxx:168-225).
+ * All vectors, the projection and the small eigensolve stay on the GPU.
+ * precision CG_PREC_FP64: FP64 matrix and vectors throughout.
+ * precision CG_PREC_FP32: FP32 matrix and vectors, FP64 projections, then FP64
+ *   refinement sweeps (CG_PREC_REFINE products) until resid <= tol_resid. */
+typedef struct {
+  int32_t nstates;   /* eigenpairs wanted (nume)                          */
+  int32_t block;     /* vectors added per iteration (mblock)              */
+  int32_t lim;       /* maximum basis size before collapse (limmax)       */
+  int32_t maxiter;   /* iteration cap (0: max(40*nstates, 200) as the reference) */
+  double crite;      /* eigenvalue-change threshold (reference 1e-15)     */
+  double critc;      /* Ritz-coefficient threshold (reference 1e-12)      */
+  double critr;      /* residual-norm threshold (reference 1e-8)          */
+  double ortho;      /* re-orthogonalisation threshold (reference 1e-9)   */
+  double tol_resid;  /* stop when every wanted residual norm <= tol_resid (0: use critr only) */
+  double switch_resid; /* FP32 phase hands over to FP64 refinement below this residual */
+  int32_t precision; /* CG_PREC_FP64 or CG_PREC_FP32 (must match the matrix) */
+  int32_t verbose;   /* 0 silent, 1 per-iteration line on stderr          */
+  int32_t ortho_block; /* FP64 only: 0 = one vector at a time as the reference,
+                          1 = block Gram-Schmidt (the FP32 phase always uses blocks) */
+} cg_davidson_params;
+
+typedef struct {
+  int32_t iterations;        /* outer iterations (all phases)                */
+  int32_t refine_iterations; /* of which FP64 refinement                     */
+  int64_t matvecs;           /* vectors multiplied by H                      */
+  int32_t restarts;          /* collapses                                    */
+  int32_t converged;         /* wanted pairs with resid <= tolerance         */
+  int32_t ierr;              /* reference-style error code (1024 ortho, 2048 maxiter) */
+  double seconds;            /* wall time of the solve                       */
+  double spmm_seconds;       /* device time in SpMM                          */
+} cg_davidson_stats;
+
+void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates);
+/* eig, de (|last change|), resid: nstates doubles; vecs: NULL or nstates*n
+ * doubles (vector k at k*n); init: NULL or n_init*n doubles used as starting
+ * vectors (Davidson::InitVectors, include/kdav/cdavidson.cpp:386). */
+cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
+                      double* eig, double* de, double* resid, double* vecs, cg_davidson_stats* stats);
+
+/* ------------------------------------------------------------ file I/O */
+/* .EE eigenpair file: uint32 count, then per state double E, dE, resid,
+ * uint64 n, double v[n] (Davidson::Save, include/kdav/cdavidson.cpp:327-368). */
+cg_status cg_write_ee(const char* path, int32_t nstates, uint64_t n, const double* eig, const double* de,
+                      const double* resid, const double* vecs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COSMO_GB300_H */

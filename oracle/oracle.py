@@ -1,0 +1,160 @@
+"""CPU ORACLE — test infrastructure only.
+
+ctypes wrapper over oracle/_build/liboracle.so (cosmo_oracle.c,
+oracle_davidson.c): a plain-C restatement of the reference algorithms used as
+the checker in tests/ and smoke(), and as the timed CPU reference in bench.py.
+It is never imported by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRCS = ["cosmo_oracle.c", "oracle_davidson.c"]
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, s) for s in SRCS]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp"
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-o", tmp] + srcs + ["-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference(ref_root: str = "/root/reference") -> bool:
+    """Compile the reference tools from the reference sources into oracle/_ref
+    (only where the reference tree exists; the GPU host uses prebuilt files)."""
+    if not os.path.isdir(os.path.join(ref_root, "include")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    return True
+
+
+_lib = None
+_P = C.c_void_p
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.oracle_basis.restype = C.c_uint64
+        L.oracle_basis.argtypes = [C.c_int, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, C.c_uint64]
+        L.oracle_build_upper.restype = C.c_int64
+        L.oracle_build_upper.argtypes = [C.c_int, C.c_int64, _P, _P, C.c_int64, _P, _P, C.c_uint64, C.c_int, _P,
+                                         _P, _P, _P, C.c_int]
+        L.oracle_csb_from_upper.restype = _P
+        L.oracle_csb_from_upper.argtypes = [C.c_uint64, _P, _P, _P]
+        L.oracle_csb_free.argtypes = [_P]
+        L.oracle_csb_times_matrix.argtypes = [_P, _P, _P, C.c_int, C.c_int]
+        L.oracle_diagonal.argtypes = [C.c_uint64, _P, _P, _P, _P]
+        L.oracle_davidson.restype = C.c_int
+        L.oracle_davidson.argtypes = [_P, _P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                      C.c_double, C.c_double, C.c_double, _P, _P, _P, _P, _P, _P, C.c_int,
+                                      C.c_double, _P, _P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def basis(sps: np.ndarray, N: int, twom: int, tz2: int, parity: int, cap: int | None = None) -> np.ndarray:
+    """sps: rows (level n l 2j 2m 2t 2tz parity) as cosmo_gb300.Problem.sps()."""
+    m2 = np.ascontiguousarray(sps[:, 4], dtype=np.int32)
+    tz = np.ascontiguousarray(sps[:, 6], dtype=np.int32)
+    pa = np.ascontiguousarray(sps[:, 7], dtype=np.int32)
+    n = lib().oracle_basis(len(sps), _p(m2), _p(tz), _p(pa), N, twom, tz2, parity, None, 0)
+    if cap is not None and n > cap:
+        raise ValueError(f"basis of {n} states exceeds cap {cap}")
+    z = np.zeros((n, N), dtype=np.uint16)
+    lib().oracle_basis(len(sps), _p(m2), _p(tz), _p(pa), N, twom, tz2, parity, _p(z), n)
+    return z
+
+
+def build_upper(ns: int, k1, v1, k2, v2, z: np.ndarray, nthreads: int = 0):
+    """Upper-triangle rows (CSR) of H from forward-ordered operator terms."""
+    k1 = np.ascontiguousarray(k1, dtype=np.int32)
+    v1 = np.ascontiguousarray(v1, dtype=np.float64)
+    k2 = np.ascontiguousarray(k2, dtype=np.int32)
+    v2 = np.ascontiguousarray(v2, dtype=np.float64)
+    z = np.ascontiguousarray(z, dtype=np.uint16)
+    n, N = z.shape
+    rp = np.zeros(n + 1, dtype=np.uint64)
+    r = lib().oracle_build_upper(ns, len(v1), _p(k1), _p(v1), len(v2), _p(k2), _p(v2), n, N, _p(z), _p(rp), None,
+                                 None, nthreads)
+    if r < 0:
+        raise RuntimeError("oracle row buffer overflow")
+    cols = np.zeros(int(rp[-1]), dtype=np.uint32)
+    vals = np.zeros(int(rp[-1]))
+    lib().oracle_build_upper(ns, len(v1), _p(k1), _p(v1), len(v2), _p(k2), _p(v2), n, N, _p(z), _p(rp), _p(cols),
+                             _p(vals), nthreads)
+    return rp, cols, vals
+
+
+class CSB:
+    """Reference-layout upper CSB (square blocks of floor(sqrt(n)) + 1)."""
+
+    def __init__(self, rp, cols, vals):
+        self.rp = np.ascontiguousarray(rp, dtype=np.uint64)
+        self.cols = np.ascontiguousarray(cols, dtype=np.uint32)
+        self.vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.n = len(self.rp) - 1
+        self._h = lib().oracle_csb_from_upper(self.n, _p(self.rp), _p(self.cols), _p(self.vals))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_csb_free(self._h)
+            self._h = None
+
+    def times_matrix(self, x: np.ndarray, nthreads: int = 0) -> np.ndarray:
+        x2 = np.asarray(x, dtype=np.float64).reshape(self.n, -1)
+        m = x2.shape[1]
+        xc = np.ascontiguousarray(x2.T)
+        yc = np.zeros_like(xc)
+        lib().oracle_csb_times_matrix(self._h, _p(xc), _p(yc), m, nthreads)
+        return yc.T.reshape(np.shape(x))
+
+    def diagonal(self) -> np.ndarray:
+        d = np.zeros(self.n)
+        lib().oracle_diagonal(self.n, _p(self.rp), _p(self.cols), _p(self.vals), _p(d))
+        return d
+
+    def davidson(self, nume: int = 10, block: int | None = None, lim: int | None = None, maxiter: int = 0,
+                 crite=1e-15, critc=1e-12, critr=1e-8, ortho=1e-9, nthreads: int = 0, time_budget: float = 0.0,
+                 want_vectors: bool = False):
+        block = block or nume
+        lim = lim or nume + 20
+        maxiter = maxiter or max(40 * nume, 200)
+        d = self.diagonal()
+        eig = np.zeros(nume); de = np.zeros(nume); res = np.zeros(nume)
+        vecs = np.zeros((nume, self.n)) if want_vectors else None
+        it = C.c_int(0); nmv = C.c_int64(0); per = C.c_double(0); t0 = C.c_double(0)
+        ierr = lib().oracle_davidson(self._h, _p(d), self.n, nume, block, lim, maxiter, crite, critc, critr, ortho,
+                                     _p(eig), _p(de), _p(res), _p(vecs), C.byref(it), C.byref(nmv), nthreads,
+                                     time_budget, C.byref(per), C.byref(t0))
+        return dict(eig=eig, de=de, resid=res, vecs=vecs, iterations=it.value, matvecs=nmv.value, ierr=ierr,
+                    seconds_per_iteration=per.value)
+
+
+def full_from_upper(rp, cols, vals):
+    """scipy CSR of the full symmetric matrix from upper rows."""
+    import scipy.sparse as sp
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp).astype(np.int64))
+    U = sp.csr_matrix((vals, (rows, cols.astype(np.int64))), shape=(n, n))
+    D = sp.diags(U.diagonal())
+    return (U + U.T - D).tocsr()

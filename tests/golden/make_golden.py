@@ -1,0 +1,200 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference CoSMo code compiled from the reference sources by
+oracle/Makefile (oracle/_ref/ref_dump = the DEXHVJTcsb CSB path without the
+Eigen fallback, oracle/_ref/XsysmbsOMP = the basis tool) on seeded synthetic
+inputs (cosmo_gb300.synthetic) and on the 24Mg/usdb example, and stores what
+the GPU build must reproduce:
+
+* s.p. table, ESP and VSPX operator terms (full, small)
+* the .mbs basis: full tuples for small cases, sha256 of the file otherwise
+* the upper-triangle Hamiltonian rows: full for small cases; otherwise the
+  sha256 of (rowptr u64 | cols u32) plus every 97th row with values
+* y = H x from the reference SpMM for small cases
+* eigenvalues, eigenvalue changes and residual norms of the reference Davidson
+
+usage (needs the reference tree; the fixtures are committed):
+    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from cosmo_gb300.synthetic import SD_ORBITS, SyntheticSystem, make_system, write_xml  # noqa: E402
+
+# name: (system, full dumps, Davidson nstates, Davidson iterations)
+CASES = {
+    "sd22m0s1": (SyntheticSystem("sd", 2, 2, 0, "+", 0.5, 1), True, 10, 0),
+    "sd32m1s2": (SyntheticSystem("sd", 3, 2, 1, "+", 0.5, 2), True, 5, 0),
+    "fp22m0s3": (SyntheticSystem("fp", 2, 2, 0, "+", 0.5, 3), False, 10, 0),
+    "fp21m3s6": (SyntheticSystem("fp", 2, 1, 3, "-", 0.5, 6), True, 5, 0),
+    "sd44m0s4": (SyntheticSystem("sd", 4, 4, 0, "+", 0.5, 4), False, 10, 0),
+    "sd66m0s5": (SyntheticSystem("sd", 6, 6, 0, "+", 0.5, 5), False, 10, 0),
+}
+# basis-only cases (XsysmbsOMP)
+BASIS_CASES = {
+    "fp44m0s7": SyntheticSystem("fp", 4, 4, 0, "+", 0.5, 7),
+    "fp55m0s8": SyntheticSystem("fp", 5, 5, 0, "+", 0.5, 8),
+}
+# 24Mg with usdb (EXAMPLE-24Mg-usdb.md); usdb orbit order 1=d3/2 2=d5/2 3=s1/2
+USDB_ORBITS = [("0d3", 0, 2, 3), ("0d5", 0, 2, 5), ("1s1", 1, 0, 1)]
+
+
+def sha(path_or_bytes) -> str:
+    h = hashlib.sha256()
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        h.update(path_or_bytes)
+    else:
+        with open(path_or_bytes, "rb") as f:
+            for blk in iter(lambda: f.read(1 << 24), b""):
+                h.update(blk)
+    return h.hexdigest()
+
+
+def conn_hash(rowptr: np.ndarray, cols: np.ndarray) -> str:
+    """sha256 over rowptr (u64 LE) then cols (u32 LE) of the upper rows."""
+    return sha(np.ascontiguousarray(rowptr, dtype="<u8").tobytes() + np.ascontiguousarray(cols, dtype="<u4").tobytes())
+
+
+def read_rows(path: str, n: int):
+    raw = open(path, "rb").read()
+    nnz = int(np.frombuffer(raw[:8], np.uint64)[0])
+    r = np.frombuffer(raw[8:8 + 4 * nnz], np.uint32)
+    c = np.frombuffer(raw[8 + 4 * nnz:8 + 8 * nnz], np.uint32)
+    v = np.frombuffer(raw[8 + 8 * nnz:], np.float64)
+    rp = np.zeros(n + 1, dtype=np.uint64)
+    np.add.at(rp, r.astype(np.int64) + 1, 1)
+    return np.cumsum(rp).astype(np.uint64), c.copy(), v.copy()
+
+
+def read_ee(path: str):
+    with open(path, "rb") as f:
+        cnt = int(np.frombuffer(f.read(4), np.uint32)[0])
+        E, D, R = [], [], []
+        for _ in range(cnt):
+            e, d, r = np.frombuffer(f.read(24), np.float64)
+            n = int(np.frombuffer(f.read(8), np.uint64)[0])
+            f.seek(8 * n, 1)
+            E.append(e); D.append(d); R.append(r)
+    return np.array(E), np.array(D), np.array(R)
+
+
+def run_ref(ref_bin: str, xml: str, prefix: str, cwd: str, nstates: int, iters: int) -> None:
+    cmd = [os.path.join(ROOT, "oracle", "_ref", ref_bin), xml]
+    if ref_bin == "ref_dump":
+        cmd.append(prefix)
+    if nstates:
+        cmd += [str(nstates), str(iters)]
+    with open(os.path.join(cwd, prefix + ".log"), "w") as log:
+        subprocess.run(cmd, cwd=cwd, stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+
+
+def dump_case(name: str, work: str, xml: str, full: bool, nstates: int, iters: int, manifest: dict,
+              keep_terms: bool = False) -> None:
+    run_ref("ref_dump", xml, name, work, nstates, iters)
+    sysname = name
+    mbs = os.path.join(work, sysname + ".mbs")
+    raw = open(mbs, "rb").read(12)
+    N = int(np.frombuffer(raw[:4], np.int32)[0])
+    n = int(np.frombuffer(raw[4:12], np.uint64)[0])
+    sps = np.loadtxt(os.path.join(work, name + ".sps.txt"), dtype=np.int64, ndmin=2)
+    esp = np.loadtxt(os.path.join(work, name + ".esp.txt"), ndmin=2)
+    vspx = np.loadtxt(os.path.join(work, name + ".vspx.txt"), ndmin=2)
+    rp, cols, vals = read_rows(os.path.join(work, name + ".rows.bin"), n)
+    entry = dict(n=n, N=N, mbs_sha256=sha(mbs), nnz_upper=int(rp[-1]), conn_sha256=conn_hash(rp, cols))
+    arrays = dict(sps=sps[:, 1:].astype(np.int32),
+                  esp_keys=esp[:, :2].astype(np.int32), esp_vals=esp[:, 2],
+                  vspx_keys=vspx[:, :4].astype(np.int32), vspx_vals=vspx[:, 4])
+    if full:
+        z = np.frombuffer(open(mbs, "rb").read()[12:], np.uint16).reshape(n, N)
+        arrays.update(mbs=z, rowptr=rp, cols=cols, vals=vals)
+        sp = open(os.path.join(work, name + ".spmm.bin"), "rb").read()
+        nn = int(np.frombuffer(sp[:8], np.uint64)[0]); m = int(np.frombuffer(sp[8:12], np.uint32)[0])
+        arrays["spmm_x"] = np.frombuffer(sp[12:12 + 8 * m * nn], np.float64).reshape(m, nn)
+        arrays["spmm_y"] = np.frombuffer(sp[12 + 8 * m * nn:], np.float64).reshape(m, nn)
+    else:
+        sample = np.arange(0, n, 97, dtype=np.int64)
+        srp = [0]
+        sc, sv = [], []
+        for r in sample:
+            a, b = int(rp[r]), int(rp[r + 1])
+            sc.append(cols[a:b]); sv.append(vals[a:b]); srp.append(srp[-1] + b - a)
+        arrays.update(sample_rows=sample, sample_rowptr=np.array(srp, dtype=np.uint64),
+                      sample_cols=np.concatenate(sc), sample_vals=np.concatenate(sv))
+    if not keep_terms and not full:
+        # the operator terms of synthetic cases are regenerated from the .int by the tests
+        for k in ("esp_keys", "esp_vals", "vspx_keys", "vspx_vals"):
+            arrays.pop(k)
+    if nstates:
+        E, D, R = read_ee(os.path.join(work, name + ".EE"))
+        arrays.update(ref_eig=E, ref_de=D, ref_resid=R)
+        entry.update(ref_eig=[float(x) for x in E], ref_resid=[float(x) for x in R])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    manifest[name] = entry
+    print(name, json.dumps({k: v for k, v in entry.items() if k not in ("ref_eig", "ref_resid")}))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
+    mpath = os.path.join(HERE, "manifest.json")
+    manifest = json.load(open(mpath)) if os.path.exists(mpath) else {}
+    work = tempfile.mkdtemp(prefix="cg_golden_")
+    try:
+        for name, (sysd, full, nst, it) in CASES.items():
+            if a.only and a.only != name:
+                continue
+            sysd.name = name
+            _, xml = make_system(work, sysd)
+            dump_case(name, work, xml, full, nst, it, manifest)
+            manifest[name]["system"] = dict(space=sysd.space, nv=sysd.nv, zv=sysd.zv, twom=sysd.twom,
+                                            parity=sysd.parity, jj=sysd.jj, seed=sysd.seed)
+        for name, sysd in BASIS_CASES.items():
+            if a.only and a.only != name:
+                continue
+            sysd.name = name
+            _, xml = make_system(work, sysd)
+            run_ref("XsysmbsOMP", xml, name, work, 0, 0)
+            mbs = os.path.join(work, name + ".mbs")
+            raw = open(mbs, "rb").read(12)
+            manifest[name] = dict(n=int(np.frombuffer(raw[4:12], np.uint64)[0]),
+                                  N=int(np.frombuffer(raw[:4], np.int32)[0]), mbs_sha256=sha(mbs),
+                                  system=dict(space=sysd.space, nv=sysd.nv, zv=sysd.zv, twom=sysd.twom,
+                                              parity=sysd.parity, jj=sysd.jj, seed=sysd.seed))
+            print(name, manifest[name])
+        if not a.only or a.only == "mg24usdb":
+            sysd = SyntheticSystem("sd", 4, 4, 0, "+", 0.0, 0, name="mg24usdb")
+            xml = os.path.join(work, "mg24usdb.xml")
+            write_xml(xml, sysd, os.path.join(a.ref, "interactions", "sd", "usdb.int"), USDB_ORBITS, hname="usdb")
+            # no JJ shift in the example (EXAMPLE-24Mg-usdb.md:10)
+            txt = open(xml).read().replace('<matrix JJ="0.0"/>', "")
+            open(xml, "w").write(txt)
+            dump_case("mg24usdb", work, xml, False, 10, 0, manifest, keep_terms=True)
+            manifest["mg24usdb"]["system"] = dict(space="sd-usdb", nv=4, zv=4, twom=0, parity="+", jj=None)
+            # known answers printed in EXAMPLE-24Mg-usdb.md:29-38 (E, 4 decimals)
+            manifest["mg24usdb"]["example_E"] = [-87.1044, -85.6021, -82.9883, -82.732, -82.0294, -81.2219,
+                                                 -79.7662, -79.6227, -79.3076, -79.2863]
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    with open(mpath, "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+"""GPU parity tests: basis, Hamiltonian connectivity/phases/values, SpMM and
+Davidson through the C ABI against the oracle and the reference's golden
+outputs.  Tolerances: integer work (basis, columns, signs) bit-exact; H values
+1e-12 absolute (FP64 TBME sums); FP64 SpMM 1e-11 relative; FP32 SpMM 1e-5
+relative; eigenvalues 1e-4 MeV with residual <= 1e-5 (the parity bar)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import cosmo_gb300 as cg
+from conftest import conn_hash, golden, manifest, mbs_sha, problem_for
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SMALL = ["sd22m0s1", "sd32m1s2", "fp21m3s6"]
+MEDIUM = ["fp22m0s3", "sd44m0s4", "mg24usdb", "sd66m0s5"]
+
+
+def _gpu(name, tmp, prec=cg.CG_PREC_FP64):
+    p = problem_for(name, tmp)
+    b = cg.ManyBodyStates(p)
+    h = cg.Hamiltonian(p, b, prec)
+    return p, b, h
+
+
+@pytest.mark.parametrize("name", SMALL + MEDIUM)
+def test_basis_matches_reference(gpu_available, name, tmp_path):
+    m = manifest()[name]
+    p = problem_for(name, str(tmp_path))
+    b = cg.ManyBodyStates(p)
+    assert (b.n, b.N) == (m["n"], m["N"])
+    z = b.states()
+    assert mbs_sha(z) == m["mbs_sha256"]
+    g = golden(name)
+    if "mbs" in g:
+        assert np.array_equal(z, g["mbs"])
+    # .mbs writer is byte-identical
+    f = tmp_path / "x.mbs"
+    b.write_mbs(str(f))
+    assert hashlib.sha256(f.read_bytes()).hexdigest() == m["mbs_sha256"]
+
+
+@pytest.mark.parametrize("name", ["fp44m0s7", "fp55m0s8"])
+def test_large_basis_matches_reference(gpu_available, name, tmp_path):
+    m = manifest()[name]
+    p = problem_for(name, str(tmp_path))
+    b = cg.ManyBodyStates(p)
+    assert (b.n, b.N) == (m["n"], m["N"])
+    h = hashlib.sha256()
+    h.update(np.int32(b.N).tobytes())
+    h.update(np.uint64(b.n).tobytes())
+    step = 1 << 22
+    for s in range(0, b.n, step):
+        h.update(b.states(s, min(step, b.n - s)).astype("<u2").tobytes())
+    assert h.hexdigest() == m["mbs_sha256"]
+
+
+def test_locate(gpu_available, tmp_path):
+    p = problem_for("sd32m1s2", str(tmp_path))
+    b = cg.ManyBodyStates(p)
+    z = b.states()
+    idx = np.array([0, 1, 7, b.n // 2, b.n - 1])
+    assert np.array_equal(b.locate(z[idx]), idx.astype(np.uint64))
+    bad = z[:1].copy()
+    bad[0, -1] = bad[0, -2]  # repeated orbital: not a determinant of the basis
+    assert b.locate(bad)[0] == b.n + 1
+
+
+@pytest.mark.parametrize("name", SMALL + MEDIUM)
+def test_hamiltonian_connectivity_and_values(gpu_available, name, tmp_path):
+    m = manifest()[name]
+    g = golden(name)
+    p, b, h = _gpu(name, str(tmp_path))
+    assert h.info.nnz_upper == m["nnz_upper"]
+    rp, c, v = h.upper_rows()
+    assert conn_hash(rp, c) == m["conn_sha256"]
+    if "rowptr" in g:
+        np.testing.assert_allclose(v, g["vals"], rtol=0, atol=1e-12)
+        assert np.array_equal(np.signbit(v), np.signbit(g["vals"]))
+    else:
+        for k, r in enumerate(g["sample_rows"]):
+            a, e = int(rp[r]), int(rp[r + 1])
+            sa, sb = int(g["sample_rowptr"][k]), int(g["sample_rowptr"][k + 1])
+            np.testing.assert_allclose(v[a:e], g["sample_vals"][sa:sb], rtol=0, atol=1e-12)
+            assert np.array_equal(np.signbit(v[a:e]), np.signbit(g["sample_vals"][sa:sb]))
+    d = h.diagonal()
+    diag_ref = np.zeros(h.n)
+    rows = np.repeat(np.arange(h.n), np.diff(rp).astype(np.int64))
+    on = c == rows
+    diag_ref[rows[on]] = v[on]
+    assert np.array_equal(d, diag_ref)
+    # both triangles: H is exactly symmetric
+    x = np.random.default_rng(0).standard_normal((h.n, 2))
+    y = h.times_matrix(x)
+    assert abs(x[:, 0] @ y[:, 1] - x[:, 1] @ y[:, 0]) <= 1e-10 * np.abs(y).sum()
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_spmm_matches_reference(gpu_available, name, tmp_path):
+    g = golden(name)
+    x = g["spmm_x"].T.copy()
+    yref = g["spmm_y"].T
+    _, _, h64 = _gpu(name, str(tmp_path), cg.CG_PREC_FP64)
+    y = h64.times_matrix(x)
+    np.testing.assert_allclose(y, yref, rtol=0, atol=1e-11 * np.abs(yref).max())
+    _, _, h32 = _gpu(name, str(tmp_path), cg.CG_PREC_FP32)
+    y32 = h32.times_matrix(x, cg.CG_PREC_FP32)
+    np.testing.assert_allclose(y32, yref, rtol=0, atol=1e-5 * np.abs(yref).max())
+    yr = h32.times_matrix(x, cg.CG_PREC_REFINE)
+    np.testing.assert_allclose(yr, yref, rtol=0, atol=1e-11 * np.abs(yref).max())
+
+
+@pytest.mark.parametrize("m", [1, 3, 4, 8, 10, 16, 19])
+def test_spmm_block_widths(gpu_available, m, tmp_path):
+    """Every vector count against the oracle's pull-form CSB product (sd 6+6)."""
+    name = "sd66m0s5"
+    p, b, h = _gpu(name, str(tmp_path))
+    rp, c, v = h.upper_rows()
+    x = np.random.default_rng(m).standard_normal((h.n, m))
+    yref = O.CSB(rp, c, v).times_matrix(x)
+    y = h.times_matrix(x)
+    np.testing.assert_allclose(y, yref, rtol=0, atol=1e-10 * np.abs(yref).max())
+
+
+def _exact(name, tmp, k=10):
+    import scipy.sparse.linalg as sla
+    p = problem_for(name, tmp)
+    inf = p.info
+    z = O.basis(p.sps(), inf.nv + inf.zv, inf.twom, inf.nv - inf.zv, inf.parity)
+    k1, v1 = p.one_body()
+    k2, v2 = p.two_body()
+    rp, c, v = O.build_upper(inf.n_sps, k1, v1, k2, v2, z)
+    H = O.full_from_upper(rp, c, v)
+    return np.sort(sla.eigsh(H, k=k, which="SA", tol=1e-13)[0])
+
+
+@pytest.mark.parametrize("name", SMALL + ["mg24usdb"])
+def test_davidson_fp64_reference_algorithm(gpu_available, name, tmp_path):
+    """The reference algorithm (block = nstates, lim = nstates + 20, one-vector
+    Gram-Schmidt) in FP64 on the GPU reproduces the reference's converged states."""
+    g = golden(name)
+    nst = len(g["ref_eig"])
+    _, _, h = _gpu(name, str(tmp_path))
+    r = cg.davidson_diagonalization(h, nst, want_vectors=True)
+    ok = g["ref_resid"] < 1e-5
+    np.testing.assert_allclose(r.eig[ok], g["ref_eig"][ok], rtol=0, atol=1e-6)
+    # eigenvectors: |H v - E v| small and orthonormal
+    V = r.vecs.T
+    HV = h.times_matrix(V)
+    res = np.linalg.norm(HV - V * r.eig, axis=0)
+    np.testing.assert_allclose(res, r.resid, rtol=1e-3, atol=1e-9)
+    np.testing.assert_allclose(V.T @ V, np.eye(nst), atol=1e-8)
+
+
+@pytest.mark.parametrize("name", ["sd32m1s2", "fp22m0s3", "sd44m0s4", "mg24usdb", "sd66m0s5"])
+def test_davidson_mixed_vs_exact(gpu_available, name, tmp_path):
+    """Mixed precision (FP32 H and vectors, FP64 projection, FP64 refinement):
+    lowest eigenvalues within 1e-4 MeV of an exact solve, residuals <= 1e-5."""
+    nst = 5 if name == "sd32m1s2" else 10
+    exact = _exact(name, str(tmp_path), nst)
+    _, _, h = _gpu(name, str(tmp_path), cg.CG_PREC_FP32)
+    r = cg.davidson_diagonalization(h, nst, want_vectors=True, precision=cg.CG_PREC_FP32, tol_resid=1e-5,
+                                    block=nst, lim=min(48, nst * 4))
+    assert r.stats.converged == nst, (r.resid, r.stats.ierr)
+    assert np.all(r.resid <= 1e-5)
+    np.testing.assert_allclose(r.eig, exact, rtol=0, atol=1e-4)
+
+
+def test_ee_roundtrip(gpu_available, tmp_path):
+    _, _, h = _gpu("sd22m0s1", str(tmp_path))
+    r = cg.davidson_diagonalization(h, 4, want_vectors=True)
+    f = str(tmp_path / "x.EE")
+    cg.write_ee(f, r.eig, r.de, r.resid, r.vecs)
+    E, D, R, V = cg.read_ee(f)
+    assert np.array_equal(E, r.eig) and np.array_equal(R, r.resid) and np.array_equal(V, r.vecs)
+
+
+def test_hh_writer_layout(gpu_available, tmp_path):
+    """.HH: u64 n, per row u32 nz, u64 ind[nz], f64 elem[nz] (PPMatrix::Write)."""
+    g = golden("sd22m0s1")
+    _, _, h = _gpu("sd22m0s1", str(tmp_path))
+    f = tmp_path / "x.HH"
+    h.write_hh(str(f))
+    raw = f.read_bytes()
+    n = int(np.frombuffer(raw[:8], np.uint64)[0])
+    off = 8
+    cols, vals = [], []
+    for _ in range(n):
+        nz = int(np.frombuffer(raw[off:off + 4], np.uint32)[0]); off += 4
+        cols.append(np.frombuffer(raw[off:off + 8 * nz], np.uint64)); off += 8 * nz
+        vals.append(np.frombuffer(raw[off:off + 8 * nz], np.float64)); off += 8 * nz
+    assert off == len(raw)
+    assert np.array_equal(np.concatenate(cols), g["cols"].astype(np.uint64))
+    np.testing.assert_allclose(np.concatenate(vals), g["vals"], rtol=0, atol=1e-12)
