@@ -42,7 +42,7 @@ WORKLOAD = dict(workload="fp-shell 4p+4n M=0, lowest 10 eigenpairs, |dE|<=1e-4 M
                 space="fp", protons=4, neutrons=4, twoM=0, dimension=1963461, lam=0.5, seed=7,
                 l2="inputs larger than L2 (stored H ~15 GB, vectors ~300 MB)")
 # Davidson settings of the mixed solve (block vectors per SpMM, basis limit)
-MIXED = dict(block=10, lim=40, switch_resid=2e-4)
+MIXED = dict(block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5)
 # iterations of the reference algorithm to reach resid <= 1e-5 on this problem,
 # measured with the same algorithm in FP64 (used to scale the CPU sample)
 REF_ITERS_DEFAULT = None
@@ -116,33 +116,69 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def make_inputs(tmp: str):
+CONFIGS = {"fp44": ("fp", 4, 4, 0, "+", 0.5, 7, "fp44m0s7"), "sd66": ("sd", 6, 6, 0, "+", 0.5, 5, "sd66m0s5")}
+
+
+def make_inputs(tmp: str, config: str = "fp44"):
     from cosmo_gb300.synthetic import SyntheticSystem, make_system
-    return make_system(tmp, SyntheticSystem("fp", 4, 4, 0, "+", 0.5, 7, name="fp44m0s7"))[1]
+    sp, nv, zv, tm, par, lam, seed, name = CONFIGS[config]
+    return make_system(tmp, SyntheticSystem(sp, nv, zv, tm, par, lam, seed, name=name))[1]
 
 
-def spmm_roofline(cg, h, b: int, reps: int = 20):
-    """Average device time of the FP32 SpMM (b vectors) with CUDA events on the
-    library's stream, and its algorithmic bytes per launch."""
+def run_spmm_only(args):
+    """SpMM kernel alone (for profiling): build H, time --steps launches."""
+    import torch
+    import cosmo_gb300 as cg
+    torch.cuda.set_device(0)
+    tmp = tempfile.mkdtemp(prefix="cg_spmm_")
+    prob = cg.Problem(make_inputs(tmp, args.config))
+    basis = cg.ManyBodyStates(prob)
+    prec = cg.CG_PREC_FP64 if args.precision == "fp64" else cg.CG_PREC_FP32
+    H = cg.Hamiltonian(prob, basis, prec)
+    tune = None
+    if prec == cg.CG_PREC_FP32:
+        if args.tuning:
+            w, c = (int(v) for v in args.tuning.split("x"))
+            cg._check(cg.lib().cg_spmm_set_tuning(H._h, w, c))
+            tune = {"warps": w, "ctas_per_sm": c, "fixed": True}
+        else:
+            tune = H.autotune(args.nvec)
+        spmm_s, alg = spmm_roofline(cg, H, args.nvec, reps=args.steps, warm=args.warmup)
+    else:
+        spmm_s, alg = spmm_roofline(cg, H, args.nvec, reps=args.steps, warm=args.warmup, fp64=True)
+    peak, kind = measured_peaks()
+    print(json.dumps({"mode": "spmm", "config": args.config, "precision": args.precision, "nvec": args.nvec,
+                      "n": H.n, "nnz_full": int(H.info.nnz_full), "launch_ms": spmm_s * 1e3, "alg_bytes": alg,
+                      "achieved_gbs": alg / spmm_s / 1e9, "peak_gbs": peak, "frac": alg / spmm_s / 1e9 / peak,
+                      "tuning": tune}))
+
+
+def spmm_roofline(cg, h, b: int, reps: int = 20, warm: int = 3, fp64: bool = False):
+    """Average device time of one SpMM launch (b vectors) from CUDA events on the
+    library's stream, and its algorithmic bytes per launch: stored entries x
+    (value + 4-byte column) + row pointers + the input and output vectors."""
     import torch
     n = h.n
-    ld = (b + 3) // 4 * 4
-    x = torch.randn(n, ld, device="cuda", dtype=torch.float32)
-    y = torch.empty(n, ld, device="cuda", dtype=torch.float32)
+    esz = 8 if fp64 else 4
+    ld = (8 if b <= 8 else 16) if not fp64 else (b + 3) // 4 * 4
+    dt = torch.float64 if fp64 else torch.float32
+    prec = cg.CG_PREC_FP64 if fp64 else cg.CG_PREC_FP32
+    x = torch.randn(n, ld, device="cuda", dtype=dt)
+    y = torch.empty(n, ld, device="cuda", dtype=dt)
     torch.cuda.synchronize()
     st = torch.cuda.ExternalStream(h.stream)
-    for _ in range(3):
-        h.spmm_device(x.data_ptr(), ld, y.data_ptr(), ld, b, cg.CG_PREC_FP32)
+    for _ in range(warm):
+        h.spmm_device(x.data_ptr(), ld, y.data_ptr(), ld, b, prec)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(st)
     for _ in range(reps):
-        h.spmm_device(x.data_ptr(), ld, y.data_ptr(), ld, b, cg.CG_PREC_FP32)
+        h.spmm_device(x.data_ptr(), ld, y.data_ptr(), ld, b, prec)
     e1.record(st)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
     nnz = int(h.info.nnz_full)
-    alg = nnz * (4 + 4) + (n + 1) * 8 + n * b * 4 * 2
+    alg = nnz * (esz + 4) + (n + 1) * 8 + n * b * esz * 2
     del x, y
     return ms * 1e-3, alg
 
@@ -161,6 +197,7 @@ def run_ours(args):
     prob = cg.Problem(xml)
     basis = cg.ManyBodyStates(prob)
     H = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP32)
+    tuning = H.autotune(MIXED["block"])
     kw = dict(precision=cg.CG_PREC_FP32, tol_resid=TOL, **MIXED)
 
     for _ in range(args.warmup):
@@ -170,12 +207,14 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    l0 = cg.launch_count()
     t0 = time.perf_counter()
     results = []
     for _ in range(args.steps):
         results.append(cg.davidson_diagonalization(H, NSTATES, want_vectors=False, **kw))
     torch.cuda.synchronize()
     t1 = time.perf_counter()
+    launches = cg.launch_count() - l0
     clocks.stop()
     elapsed = t1 - t0
     if dist:
@@ -204,6 +243,7 @@ def run_ours(args):
 
     # SpMM roofline (FP32 mixed kernel, block of 10 vectors)
     spmm_s, alg_bytes = spmm_roofline(cg, H, MIXED["block"])
+    kernel_name = f"k_spmm_f32w<{8 if MIXED['block'] <= 8 else 16}>"
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / spmm_s / 1e9
 
@@ -237,11 +277,12 @@ def run_ours(args):
         "scaling": "replicas", "vs_baseline": None, "dtype": "fp32 storage / fp64 projection",
         "data": "synthetic (seeded Gaussian TBMEs)", "config": WORKLOAD,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": None,
+        "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "k_spmm<10, FP32>",
+                     "frac": achieved / peak, "traffic": None, "kernel": kernel_name,
                      "peak_source": peak_kind, "launch_ms": spmm_s * 1e3, "alg_bytes": alg_bytes},
         "clocks": clocks.summary(),
+        "spmm_tuning": {k: v for k, v in tuning.items() if k != "candidates"},
         "solve": {"iterations": int(last.stats.iterations), "refine_iterations": int(last.stats.refine_iterations),
                   "matvecs": int(last.stats.matvecs), "converged": int(last.stats.converged),
                   "max_resid": float(last.resid.max()), "spmm_seconds": last.stats.spmm_seconds,
@@ -321,8 +362,15 @@ def main():
     ap.add_argument("--fp64-maxiter", type=int, default=400)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-iters", type=int, default=200)
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmm"])
+    ap.add_argument("--config", default="fp44", choices=sorted(CONFIGS))
+    ap.add_argument("--nvec", type=int, default=10)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--tuning", default=None, help="fixed launch shape WARPSxCTAS for --mode spmm")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.mode == "spmm":
+        run_spmm_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -60,7 +60,8 @@ class DavidsonParams(C.Structure):
     _fields_ = [("nstates", C.c_int32), ("block", C.c_int32), ("lim", C.c_int32), ("maxiter", C.c_int32),
                 ("crite", C.c_double), ("critc", C.c_double), ("critr", C.c_double), ("ortho", C.c_double),
                 ("tol_resid", C.c_double), ("switch_resid", C.c_double), ("precision", C.c_int32),
-                ("verbose", C.c_int32), ("ortho_block", C.c_int32)]
+                ("verbose", C.c_int32), ("ortho_block", C.c_int32), ("algorithm", C.c_int32),
+                ("keep", C.c_int32), ("precond", C.c_int32)]
 
 
 class DavidsonStats(C.Structure):
@@ -75,6 +76,7 @@ _SIGS = {
     "cg_last_error": (C.c_char_p, []),
     "cg_version": (C.c_int32, []),
     "cg_device_count": (C.c_int32, []),
+    "cg_launch_count": (C.c_uint64, []),
     "cg_problem_load_xml": (C.c_int32, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
     "cg_problem_create": (C.c_int32, [C.POINTER(ProblemDesc), C.POINTER(_P)]),
     "cg_problem_destroy": (None, [_P]),
@@ -97,6 +99,9 @@ _SIGS = {
     "cg_hamiltonian_stream": (_P, [_P]),
     "cg_spmm": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32]),
     "cg_spmm_device": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32]),
+    "cg_spmm_autotune": (C.c_int32, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _P, _P, _P]),
+    "cg_spmm_set_tuning": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
     "cg_davidson": (C.c_int32, [_P, C.POINTER(DavidsonParams), _P, C.c_int32, _P, _P, _P, _P,
                                 C.POINTER(DavidsonStats)]),
@@ -132,6 +137,21 @@ def _ptr(a: np.ndarray) -> int:
 
 def device_count() -> int:
     return int(lib().cg_device_count())
+
+
+def launch_count() -> int:
+    """Kernel launches issued by the library so far in this process."""
+    return int(lib().cg_launch_count())
+
+
+def _device_name() -> str:
+    try:
+        import subprocess
+        out = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                             capture_output=True, text=True, timeout=10).stdout.strip()
+        return out or "cuda"
+    except Exception:
+        return "cuda"
 
 
 class Problem:
@@ -274,6 +294,43 @@ class Hamiltonian:
     def spmm_device(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, m: int, precision: int) -> None:
         _check(lib().cg_spmm_device(self._h, x_ptr, ldx, y_ptr, ldy, m, precision))
 
+    def autotune(self, nvec: int = 8, reps: int = 3, cache: str | None = None) -> dict:
+        """Choose the FP32 product's launch shape for this matrix (timed on the
+        device).  With `cache` (a JSON file) a previous choice for the same
+        matrix size, vector count and device is reused instead of re-timing."""
+        import json
+        key = f"n={self.n},nnz={int(self.info.nnz_full)},nvec={nvec},dev={_device_name()}"
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                db = json.load(f)
+            if key in db:
+                w, c = db[key]["warps"], db[key]["ctas_per_sm"]
+                _check(lib().cg_spmm_set_tuning(self._h, w, c))
+                return {"warps": w, "ctas_per_sm": c, "cached": True}
+        cap = C.c_int32(64)
+        w = np.zeros(64, dtype=np.int32)
+        c = np.zeros(64, dtype=np.int32)
+        ms = np.zeros(64, dtype=np.float32)
+        _check(lib().cg_spmm_autotune(self._h, nvec, reps, C.byref(cap), _ptr(w), _ptr(c), _ptr(ms)))
+        k = int(cap.value)
+        bw, bc, _ = self.tuning()
+        res = {"warps": bw, "ctas_per_sm": bc, "cached": False,
+               "candidates": [(int(w[i]), int(c[i]), float(ms[i])) for i in range(k)]}
+        if cache:
+            db = {}
+            if os.path.exists(cache):
+                with open(cache) as f:
+                    db = json.load(f)
+            db[key] = {"warps": bw, "ctas_per_sm": bc, "ms": float(min(ms[:k]))}
+            with open(cache, "w") as f:
+                json.dump(db, f, indent=1, sort_keys=True)
+        return res
+
+    def tuning(self):
+        w, c, t = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().cg_spmm_get_tuning(self._h, C.byref(w), C.byref(c), C.byref(t)))
+        return int(w.value), int(c.value), bool(t.value)
+
 
 @dataclass
 class DavidsonResult:
@@ -300,7 +357,8 @@ def davidson_diagonalization(h: Hamiltonian, nstates: int = 10, want_vectors: bo
 
     Keyword arguments set :class:`DavidsonParams` fields (block, lim, maxiter,
     crite, critc, critr, ortho, tol_resid, switch_resid, precision, verbose,
-    ortho_block).  precision defaults to the matrix precision."""
+    ortho_block, algorithm, keep, precond).  precision defaults to the matrix
+    precision."""
     kw.setdefault("precision", h.precision)
     p = davidson_params(nstates, **kw)
     eig = np.zeros(nstates)

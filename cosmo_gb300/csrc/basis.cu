@@ -119,6 +119,7 @@ void enumerate_species(SpeciesTables& sp, int norb, int k, const int* m2, const 
   k_unrank_lex<<<unsigned((sp.nconf + T - 1) / T), T, 0, s>>>(norb, k, sp.nconf, binom.p, dm2.p, dpar.p, dmask.p,
                                                                dms.p, dps.p);
   CG_CUDA(cudaGetLastError());
+    count_launch();
   CG_CUDA(cudaMemcpyAsync(sp.lex_mask.data(), dmask.p, sp.nconf * 4, cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaMemcpyAsync(sp.lex_m2.data(), dms.p, sp.nconf * 4, cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaMemcpyAsync(sp.lex_par.data(), dps.p, sp.nconf * 4, cudaMemcpyDeviceToHost, s));
@@ -204,6 +205,7 @@ void basis_build(const System& sys, Basis& b) {
     k_expand_product<<<unsigned((b.n + T - 1) / T), T, 0, s>>>(b.n, int(bstart.size()), dbs.p, dbm.p, dbc.p, dcs.p,
                                                                 dcm.p, b.nn, b.state.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaStreamSynchronize(s));
   }
 }
@@ -218,6 +220,7 @@ void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out)
     int T = 256;
     k_tuples<<<unsigned((c + T - 1) / T), T, 0, b.stream>>>(first + c0, c, N, b.state.p, d.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaMemcpyAsync(out + c0 * N, d.p, c * N * sizeof(uint16_t), cudaMemcpyDeviceToHost, b.stream));
     CG_CUDA(cudaStreamSynchronize(b.stream));
   }

@@ -68,9 +68,17 @@ void same_device(int dev) {
   if (!(p)) throw cg::Error(CG_ERR_ARG, #p " is NULL")
 }  // namespace
 
+namespace cg {
+uint64_t& launch_counter() {
+  static uint64_t c = 0;
+  return c;
+}
+}  // namespace cg
+
 extern "C" {
 
 const char* cg_last_error(void) { return g_err.c_str(); }
+uint64_t cg_launch_count(void) { return cg::launch_counter(); }
 int32_t cg_version(void) { return 100; }
 int32_t cg_device_count(void) {
   int n = 0;
@@ -367,6 +375,45 @@ cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, vo
   });
 }
 
+cg_status cg_spmm_autotune(cg_hamiltonian* h, int32_t nvec, int32_t reps, int32_t* n_candidates, int32_t* warps,
+                           int32_t* ctas_per_sm, float* ms) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    same_device(h->h.device);
+    if (nvec < 1 || nvec > 16) throw cg::Error(CG_ERR_ARG, "nvec must be in 1..16");
+    auto c = cg::spmm_autotune(h->h, nvec, std::max(1, reps));
+    if (n_candidates) {
+      int cap = *n_candidates;
+      for (int i = 0; i < int(c.size()) && i < cap; ++i) {
+        if (warps) warps[i] = c[i].warps;
+        if (ctas_per_sm) ctas_per_sm[i] = c[i].ctas_per_sm;
+        if (ms) ms[i] = c[i].ms;
+      }
+      *n_candidates = int(c.size());
+    }
+  });
+}
+
+cg_status cg_spmm_set_tuning(cg_hamiltonian* h, int32_t warps, int32_t ctas_per_sm) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    if (warps != 4 && warps != 8 && warps != 16 && warps != 32) throw cg::Error(CG_ERR_ARG, "warps must be 4, 8, 16 or 32");
+    if (ctas_per_sm < 1 || ctas_per_sm > 16) throw cg::Error(CG_ERR_ARG, "ctas_per_sm must be in 1..16");
+    h->h.tuning.warps = warps;
+    h->h.tuning.ctas_per_sm = ctas_per_sm;
+    h->h.tuning.tuned = true;
+  });
+}
+
+cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* ctas_per_sm, int32_t* tuned) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    if (warps) *warps = h->h.tuning.warps;
+    if (ctas_per_sm) *ctas_per_sm = h->h.tuning.ctas_per_sm;
+    if (tuned) *tuned = h->h.tuning.tuned;
+  });
+}
+
 // -------------------------------------------------------------- Davidson
 void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   if (!prm) return;
@@ -384,6 +431,9 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   prm->precision = CG_PREC_FP64;
   prm->verbose = 0;
   prm->ortho_block = 0;
+  prm->algorithm = -1;
+  prm->keep = 0;
+  prm->precond = 1;
 }
 
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
@@ -415,7 +465,13 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     c.critr = final_tol;
     c.ortho = prm->ortho;
     c.verbose = prm->verbose;
-    c.seq_ortho = !prm->ortho_block;
+    // -1 (auto): the reference control flow for FP64, the residual-driven one for FP32
+    const int algo = prm->algorithm < 0 ? (prm->precision == CG_PREC_FP32 ? 1 : 0) : prm->algorithm;
+    if (algo != 0 && algo != 1) throw cg::Error(CG_ERR_ARG, "algorithm must be -1, 0 or 1");
+    c.seq_ortho = !prm->ortho_block && algo == 0;
+    c.modern = algo == 1;
+    c.keep = prm->keep;
+    c.precond = prm->precond;
     cg::DavidsonRequest rq;
     rq.nume = nume;
     rq.init = init;
@@ -432,9 +488,12 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
       rq.phase1 = c1;
       cg::DavConfig c2 = c;
       c2.spmm_prec = CG_PREC_REFINE;
+
       rq.phase2 = c2;
       rq.refine = true;
     }
+    if (prm->precision == CG_PREC_FP32 && !h->h.tuning.tuned)
+      cg::spmm_autotune(const_cast<cg_hamiltonian*>(h)->h, std::min(prm->block, 16), 3);
     cg::DavResult r = cg::davidson_solve(h->h, rq);
     const cg::DavOutcome& f = r.final_;
     for (int i = 0; i < nume; ++i) {

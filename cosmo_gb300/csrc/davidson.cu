@@ -34,7 +34,8 @@ namespace {
 
 constexpr int kTile = 32;   // rows per tile
 constexpr int kMaxK = 64;   // basis columns per tall-skinny call
-constexpr int kMaxJ = 16;   // right-hand columns per call
+constexpr int kMaxJ = 32;   // right-hand columns per call
+constexpr int kMaxC = 16;   // residual candidates per call
 constexpr int kThreads = 256;
 
 template <class T>
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) k_xty(uint64_t n, const T* __restric
   __shared__ T xs[kTile * kMaxK];
   __shared__ T ys[kTile * kMaxJ];
   const int nout = K * J;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   const uint64_t r0 = uint64_t(blockIdx.x) * rows_per_cta;
   const uint64_t r1 = min(n, r0 + rows_per_cta);
   for (uint64_t base = r0; base < r1; base += kTile) {
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(kThreads) k_xty(uint64_t n, const T* __restric
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 8; ++q) {
       int o = threadIdx.x + q * kThreads;
       if (o < nout) {
         int k = o / J, j = o - k * J;
@@ -72,18 +73,228 @@ __global__ void __launch_bounds__(kThreads) k_xty(uint64_t n, const T* __restric
     __syncthreads();
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 8; ++q) {
     int o = threadIdx.x + q * kThreads;
     if (o < nout) part[uint64_t(blockIdx.x) * nout + o] = acc[q];
   }
 }
 
+// out[o] = sum_c part[c * nout + o]: one CTA per output, strided per-thread
+// sums and a fixed-order tree, so the result is deterministic.
 __global__ void k_reduce_parts(const double* __restrict__ part, int nparts, int nout, double* __restrict__ out) {
-  int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= nout) return;
+  __shared__ double red[128];
+  const int o = blockIdx.x;
   double s = 0.0;
-  for (int c = 0; c < nparts; ++c) s += part[uint64_t(c) * nout + o];
-  out[o] = s;
+  for (int c = threadIdx.x; c < nparts; c += 128) s += part[uint64_t(c) * nout + o];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 64; w; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[o] = red[0];
+}
+
+// ---- streaming tall-skinny kernels -------------------------------------
+// G (K x J) partials = X[:, xo:xo+K]^T Y[:, yo:yo+J] over this CTA's rows.
+// KP = K rounded up to a power of two (<= 64) threads share one row, thread
+// k of the group owns column k of X and all J outputs of that column; FP32
+// products are summed over 64-row chunks and the chunks in FP64.
+template <class T, int JMAX>
+__global__ void __launch_bounds__(256) k_xty_s(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
+                                               const T* __restrict__ Y, int ldy, int yo, int J, int KP,
+                                               double* __restrict__ part, uint64_t rows_per_cta) {
+  __shared__ double red[256 * 2];
+  const int k = threadIdx.x % KP, rg = threadIdx.x / KP, ngroups = 256 / KP;
+  const bool active = k < K;
+  double acc[JMAX];
+  T ch[JMAX];
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) { acc[j] = 0.0; ch[j] = T(0); }
+  const uint64_t r0 = uint64_t(blockIdx.x) * rows_per_cta;
+  const uint64_t r1 = min(n, r0 + rows_per_cta);
+  int cnt = 0;
+  for (uint64_t r = r0 + rg; r < r1; r += ngroups) {
+    const T xv = active ? X[r * ldx + xo + k] : T(0);
+    const T* yr = Y + r * ldy + yo;
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j)
+      if (j < J) ch[j] = fma(xv, __ldg(yr + j), ch[j]);
+    if (++cnt == 64) {
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) { acc[j] += double(ch[j]); ch[j] = T(0); }
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) acc[j] += double(ch[j]);
+  // reduce the row groups: for each j, sum acc over rg (same k); J is uniform
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) {
+    if (j < J) {
+      red[threadIdx.x] = acc[j];
+      __syncthreads();
+      if (rg == 0 && active) {
+        double sum = 0.0;
+        for (int g = 0; g < ngroups; ++g) sum += red[g * KP + k];
+        part[uint64_t(blockIdx.x) * (K * J) + k * J + j] = sum;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Warp-per-row-chunk X^T Y: lane l owns columns l and l + 32 of X (K <= 64);
+// four rows are loaded before they are used so each warp keeps several rows of
+// loads in flight.  FP32 (or FP64) products, 64-row chunks summed in FP64;
+// per-warp partials go to part[warp][k * J + j].
+template <class T, int JMAX>
+__global__ void __launch_bounds__(256) k_xty_w(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
+                                               const T* __restrict__ Y, int ldy, int yo, int J,
+                                               double* __restrict__ part, uint64_t rows_per_warp) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t r0 = gw * rows_per_warp;
+  const uint64_t r1 = min(n, r0 + rows_per_warp);
+  const bool a0 = lane < K, a1 = lane + 32 < K;
+  T c0[JMAX], c1[JMAX];
+  double d0[JMAX], d1[JMAX];
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) { c0[j] = c1[j] = T(0); d0[j] = d1[j] = 0.0; }
+  int cnt = 0;
+  for (uint64_t r = r0; r < r1; r += 4) {
+    T x0[4], x1[4], yv[4][JMAX];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = r + u < r1;
+      const T* xr = X + (r + u) * ldx + xo;
+      x0[u] = (ok && a0) ? xr[lane] : T(0);
+      x1[u] = (ok && a1) ? xr[lane + 32] : T(0);
+      const T* yr = Y + (r + u) * ldy + yo;
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) yv[u][j] = (ok && j < J) ? __ldg(yr + j) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) {
+        c0[j] = fma(x0[u], yv[u][j], c0[j]);
+        c1[j] = fma(x1[u], yv[u][j], c1[j]);
+      }
+    cnt += 4;
+    if (cnt >= 64) {
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) { d0[j] += double(c0[j]); d1[j] += double(c1[j]); c0[j] = c1[j] = T(0); }
+      cnt = 0;
+    }
+  }
+  double* out = part + gw * uint64_t(K * J);
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) {
+    if (j < J) {
+      if (a0) out[lane * J + j] = d0[j] + double(c0[j]);
+      if (a1) out[(lane + 32) * J + j] = d1[j] + double(c1[j]);
+    }
+  }
+}
+
+// Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G with JP lanes per row (JP =
+// J rounded up to a power of two <= 32).  A row's readers and writers are in
+// one warp and every read of the row happens before __syncwarp(), so X and Y
+// may alias (in-place collapse).
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx, int xo, int K,
+                                                const double* __restrict__ G, T* Y, int ldy, int yo, int J, int JP,
+                                                double alpha, double beta) {
+  __shared__ T gs[64 * 32];
+  for (int i = threadIdx.x; i < K * J; i += blockDim.x) gs[i] = T(alpha * G[i]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, j = lane % JP, sub = lane / JP, rows_per_warp = 32 / JP;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const T tb = T(beta);
+  const bool act = j < J;
+  for (uint64_t base = uint64_t(warp) * rows_per_warp; base < n; base += uint64_t(nwarps) * rows_per_warp) {
+    const uint64_t r = base + sub;
+    T t = T(0), old = T(0);
+    const bool ok = act && r < n;
+    if (ok) {
+      const T* xr = X + r * ldx + xo;
+      int k = 0;
+      for (; k + 8 <= K; k += 8) {
+        T xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xv[u] = xr[k + u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t = fma(xv[u], gs[(k + u) * J + j], t);
+      }
+      for (; k < K; ++k) t = fma(xr[k], gs[k * J + j], t);
+      if (beta != 0.0) old = Y[r * ldy + yo + j];
+    }
+    __syncwarp();
+    if (ok) Y[r * ldy + yo + j] = (beta == 0.0) ? t : fma(tb, old, t);
+    __syncwarp();
+  }
+}
+
+// Thread per row: R[:, c] = AB s_c - lam_c B s_c for C candidates, plus
+// per-CTA partial |R[:, c]|^2 (FP32 over 16-row chunks, FP64 across).
+template <class T, int CMAX>
+__global__ void __launch_bounds__(256) k_resid_s(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
+                                                 int ld, int K, const double* __restrict__ Sc,
+                                                 const double* __restrict__ lam, int C, T* __restrict__ R, int ldr,
+                                                 double* __restrict__ part) {
+  __shared__ T ss[64 * CMAX];
+  __shared__ T ls[CMAX];
+  __shared__ double red[256];
+  for (int i = threadIdx.x; i < K * C; i += blockDim.x) ss[(i / C) * CMAX + (i % C)] = T(Sc[i]);
+  for (int i = threadIdx.x; i < CMAX; i += blockDim.x) ls[i] = i < C ? T(lam[i]) : T(0);
+  __syncthreads();
+  double nacc[CMAX];
+  T nch[CMAX];
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) { nacc[c] = 0.0; nch[c] = T(0); }
+  int cnt = 0;
+  for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
+    T a[CMAX], b[CMAX];
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c) { a[c] = T(0); b[c] = T(0); }
+    const T* br = B + r * ld;
+    const T* abr = AB + r * ld;
+    for (int k = 0; k < K; ++k) {
+      const T bv = br[k], av = abr[k];
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) {
+        a[c] = fma(av, ss[k * CMAX + c], a[c]);
+        b[c] = fma(bv, ss[k * CMAX + c], b[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c)
+      if (c < C) {
+        const T res = a[c] - ls[c] * b[c];
+        R[r * ldr + c] = res;
+        nch[c] = fma(res, res, nch[c]);
+      }
+    if (++cnt == 16) {
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) { nacc[c] += double(nch[c]); nch[c] = T(0); }
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    if (c < C) {
+      red[threadIdx.x] = nacc[c] + double(nch[c]);
+      __syncthreads();
+      for (int o = 128; o; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) part[uint64_t(blockIdx.x) * C + c] = red[0];
+      __syncthreads();
+    }
+  }
 }
 
 // Y[:, yo:yo+J] = beta * Y + alpha * X[:, xo:xo+K] G  (G is K x J, FP64).
@@ -125,7 +336,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(uint64_t n, const T* __re
                                                        int ldr, double* __restrict__ part, uint64_t rows_per_cta) {
   __shared__ T bs[kTile * kMaxK];
   __shared__ T abs_[kTile * kMaxK];
-  __shared__ T ss[kMaxK * kMaxJ];
+  __shared__ T ss[kMaxK * kMaxC];
   __shared__ double red[kThreads];
   for (int i = threadIdx.x; i < K * C; i += blockDim.x) ss[i] = T(Sc[i]);
   const int c = threadIdx.x % C, rstep = kThreads / C, r_first = threadIdx.x / C;
@@ -210,6 +421,16 @@ __global__ void k_copy_cols(uint64_t n, const T* S, int lds, int so, T* D, int l
   D[i * ldd + dof + j] = S[i * lds + so + j];
 }
 
+// W (n x pad, packed 32/64-byte rows) = B[:, c0:c0+m] padded with zero columns
+__global__ void k_stage_block(uint64_t n, const float* __restrict__ B, int ld, int c0, int m, float* __restrict__ W,
+                              int pad) {
+  uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * pad) return;
+  uint64_t i = idx / pad;
+  int j = int(idx - i * pad);
+  W[idx] = j < m ? B[i * ld + c0 + j] : 0.f;
+}
+
 template <class T>
 __global__ void k_set_units(T* __restrict__ B, int ld, const uint64_t* __restrict__ rows, int m) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -247,6 +468,8 @@ struct Engine {
   uint64_t n;
   int L;           // leading dimension of B / AB (>= lim, padded)
   int nparts;      // CTAs of the reduction kernels
+  int nsm_ = 1;
+  uint64_t xwarps_ = 8, xrows_ = 1;  // warps of the X^T Y kernel and rows per warp
   uint64_t rows_per_cta;
   DBuf<T> B, AB, R;
   int ldr;
@@ -254,11 +477,17 @@ struct Engine {
   DBuf<int> dsel;
   DBuf<uint64_t> drows;
   double spmm_s = 0;
+  // host wall time per phase (verbose >= 2 prints them)
+  double t_eig = 0, t_resid = 0, t_ortho = 0, t_collapse = 0, t_abs = 0;
+  static double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
   cudaEvent_t ev0, ev1;
   // reference state
   int kpass = 0, nume, lim, mblock;
   std::vector<double> S;      // lim x lim, FP64
   std::vector<double> eigs, old, zvec;  // zvec: kpass x kpass, columns eigenvectors
+  std::vector<double> wall_;            // all eigenvalues of the last projected problem
   std::vector<int> icv;
 
   Engine(const Hamiltonian& h, const DavConfig& c, cudaStream_t st) : H(h), cfg(c), s(st) {
@@ -269,10 +498,11 @@ struct Engine {
     int align = sizeof(T) == 4 ? 4 : 2;
     L = (lim + align - 1) / align * align;
     if (lim > kMaxK) throw Error(CG_ERR_ARG, "lim above 64 is not supported");
-    if (mblock > kMaxJ || nume > kMaxJ) throw Error(CG_ERR_ARG, "block and nstates must be <= 16");
+    if (mblock > kMaxC || nume > kMaxC) throw Error(CG_ERR_ARG, "block and nstates must be <= 16");
     int nsm = 0;
     CG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h.device));
-    nparts = std::max(1, std::min<int>(nsm * 2, int((n + kTile - 1) / kTile)));
+    nsm_ = nsm;
+    nparts = std::max(1, std::min<int>(nsm * 4, int((n + kTile - 1) / kTile)));
     rows_per_cta = (n + nparts - 1) / nparts;
     rows_per_cta = (rows_per_cta + kTile - 1) / kTile * kTile;
     nparts = int((n + rows_per_cta - 1) / rows_per_cta);
@@ -280,7 +510,13 @@ struct Engine {
     AB.alloc(n * L);
     ldr = (std::max(nume, 1) + align - 1) / align * align;
     R.alloc(n * ldr);
-    part.alloc(size_t(nparts) * kMaxK * kMaxJ);
+    xwarps_ = uint64_t(nsm) * 32;  // 4 CTAs of 8 warps per SM
+    xrows_ = (n + xwarps_ - 1) / xwarps_;
+    xrows_ = (xrows_ + 3) / 4 * 4;
+    xwarps_ = std::max<uint64_t>(8, (n + xrows_ - 1) / xrows_);
+    xwarps_ = (xwarps_ + 7) / 8 * 8;
+    part.alloc(std::max<size_t>(std::max<size_t>(size_t(nparts) * kMaxK * kMaxJ, size_t(nsm * 4) * kMaxC),
+                                size_t(xwarps_) * 64 * 16));
     small.alloc(kMaxK * kMaxK);
     small2.alloc(kMaxK * kMaxK);
     dlam.alloc(kMaxK);
@@ -302,9 +538,17 @@ struct Engine {
 
   // G (K x J, row-major, host) = X[:, xo:xo+K]^T Y[:, yo:yo+J]
   void xty(const T* X, int xo, int K, const T* Y, int yo, int J, std::vector<double>& G) {
-    k_xty<T><<<nparts, kThreads, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, rows_per_cta);
+    if (K == 0 || J == 0) { G.assign(size_t(K) * J, 0.0); return; }
+    if (J > 16 || K > 64) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
+    const unsigned blocks = unsigned(xwarps_ / 8);
+    if (J <= 4) k_xty_w<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    else if (J <= 8) k_xty_w<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    else k_xty_w<T, 16><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     CG_CUDA(cudaGetLastError());
-    k_reduce_parts<<<blocks_for(K * J), 256, 0, s>>>(part.p, nparts, K * J, small.p);
+    count_launch();
+    k_reduce_parts<<<K * J, 128, 0, s>>>(part.p, int(xwarps_), K * J, small.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
     G.resize(size_t(K) * J);
     CG_CUDA(cudaMemcpyAsync(G.data(), small.p, sizeof(double) * K * J, cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
@@ -312,14 +556,36 @@ struct Engine {
   // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
-    unsigned grid = unsigned(std::min<uint64_t>((n + kTile - 1) / kTile, uint64_t(nparts) * 4));
-    k_rows_gemm<T><<<grid, kThreads, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta);
+    int JP = 1;
+    while (JP < J) JP <<= 1;
+    unsigned grid = unsigned(std::min<uint64_t>((n * JP + 255) / 256, uint64_t(nsm_) * 8));
+    k_gemm_s<T><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, JP, alpha, beta);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaStreamSynchronize(s));  // G's staging buffer is reused by the next call
   }
+  DBuf<float> stage;  // FP32 engine: aligned SpMM input block (n x 16)
   void spmm(int c0, int m) {
     CG_CUDA(cudaEventRecord(ev0, s));
-    spmm_launch(H, cfg.spmm_prec, B.p + c0, L, AB.p + c0, L, m, s);
+    if constexpr (sizeof(T) == 4) {
+      if (cfg.spmm_prec == CG_PREC_FP32) {
+        if (!stage.p) stage.alloc(n * 16);
+        int pad = m <= 8 ? 8 : 16;
+        k_stage_block<<<blocks_for(n * pad), 256, 0, s>>>(n, reinterpret_cast<const float*>(B.p), L, c0, m,
+                                                            stage.p, pad);
+        CG_CUDA(cudaGetLastError());
+    count_launch();
+        spmm_f32_padded(H, stage.p, pad, reinterpret_cast<float*>(AB.p) + c0, L, m, s);
+      } else {
+        spmm_launch(H, cfg.spmm_prec, B.p + c0, L, AB.p + c0, L, m, s);
+      }
+    } else if (cfg.spmm_prec == CG_PREC_REFINE) {
+      if (!stage.p) stage.alloc(n * 16);
+      spmm_refine_df(H, reinterpret_cast<const double*>(B.p) + c0, L, reinterpret_cast<double*>(AB.p) + c0, L, m,
+                     stage.p, s);
+    } else {
+      spmm_launch(H, cfg.spmm_prec, B.p + c0, L, AB.p + c0, L, m, s);
+    }
     CG_CUDA(cudaEventRecord(ev1, s));
     CG_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;
@@ -328,6 +594,7 @@ struct Engine {
   }
   // new columns of S from AB[:, c0:c0+m] (Add_Vectors_To_AB_S, fsdavidson.cxx:161-211)
   void add_ab_s(int c0, int m, int64_t& nmv) {
+    double t0 = now();
     spmm(c0, m);
     nmv += m;
     std::vector<double> G;
@@ -340,14 +607,16 @@ struct Engine {
         S[size_t(j) * lim + i] = v;
       }
     }
+    t_abs += now() - t0;
   }
   void diagonalize() {
+    double t0 = now();
+    struct Acc { double& t; double t0; ~Acc() { t += now() - t0; } } acc_{t_eig, t0};
     std::vector<double> a(size_t(kpass) * kpass);
     for (int i = 0; i < kpass; ++i)
       for (int j = 0; j < kpass; ++j) a[size_t(i) * kpass + j] = S[size_t(i) * lim + j];
-    std::vector<double> w;
-    sym_eig(kpass, a, w, zvec);
-    for (int i = 0; i < nume; ++i) eigs[i] = w[i];
+    sym_eig(kpass, a, wall_, zvec);
+    for (int i = 0; i < nume; ++i) eigs[i] = wall_[i];
   }
   double svec(int state, int row) const { return zvec[size_t(row) * kpass + state]; }
   // B[:, 0:nume] = B[:, 0:kp] Z[:, 0:nume], same for AB
@@ -366,6 +635,7 @@ struct Engine {
   }
   // residuals of candidate states `st` (0-based); returns norms
   std::vector<double> residuals(const std::vector<int>& st) {
+    struct Acc { double& t; double t0; ~Acc() { t += now() - t0; } } acc_{t_resid, now()};
     int C = int(st.size());
     std::vector<double> Sc(size_t(kpass) * C), lam(C);
     for (int c = 0; c < C; ++c) {
@@ -374,10 +644,14 @@ struct Engine {
     }
     CG_CUDA(cudaMemcpyAsync(small2.p, Sc.data(), sizeof(double) * Sc.size(), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s));
-    k_residual<T><<<nparts, kThreads, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p,
-                                              rows_per_cta);
+    const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 4));
+    if (C <= 8) k_resid_s<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+    else k_resid_s<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
     CG_CUDA(cudaGetLastError());
-    k_reduce_parts<<<1, 256, 0, s>>>(part.p, nparts, C, small.p);
+    count_launch();
+    k_reduce_parts<<<C, 128, 0, s>>>(part.p, int(rgrid), C, small.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
     std::vector<double> nr(C);
     CG_CUDA(cudaMemcpyAsync(nr.data(), small.p, sizeof(double) * C, cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
@@ -391,16 +665,19 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * A, cudaMemcpyHostToDevice, s));
     k_precond_copy<T><<<blocks_for(n * A), 256, 0, s>>>(n, R.p, ldr, dsel.p, dlam.p, A, H.diag.p, B.p, L, bo);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
   void scale_col(int c, double f) {
     CG_CUDA(cudaMemcpyAsync(small2.p, &f, sizeof(double), cudaMemcpyHostToDevice, s));
     k_scale_cols<T><<<blocks_for(n), 256, 0, s>>>(n, B.p, L, c, 1, small2.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaStreamSynchronize(s));
   }
   void copy_col(int from, int to) {
     k_copy_cols<T><<<blocks_for(n), 256, 0, s>>>(n, B.p, L, from, B.p, L, to, 1);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
 
   // Orthogonalize_Basis (fsdavidson.cxx:313-390), one vector at a time.
@@ -458,9 +735,11 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(small2.p, f.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s));
     k_scale_cols<T><<<blocks_for(n * m), 256, 0, s>>>(n, B.p, L, basis_dim, m, small2.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaStreamSynchronize(s));
   }
   bool orthogonalize_block(int basis_dim, int& nncv) {
+    struct Acc { double& t; double t0; ~Acc() { t += now() - t0; } } acc_{t_ortho, now()};
     const double drop = sizeof(T) == 4 ? 1e-8 : 1e-20;  // squared norm after projection
     int m = nncv;
     if (m == 0) return true;
@@ -525,6 +804,129 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(drows.p, rows.data() + first, sizeof(uint64_t) * count, cudaMemcpyHostToDevice, s));
     k_set_units<T><<<1, 64, 0, s>>>(B.p + first, L, drows.p, count);
     CG_CUDA(cudaGetLastError());
+    count_launch();
+  }
+
+  // Residual-driven block Davidson with thick restart (the mixed-precision
+  // solve): every iteration re-checks the residual of every wanted pair, adds
+  // the preconditioned residuals of the unconverged ones (largest first), and
+  // when the basis is full keeps `keep` Ritz vectors instead of `nume`.
+  DavOutcome run_modern(int niv, const std::vector<double>& hdiag) {
+    auto t0 = std::chrono::steady_clock::now();
+    DavOutcome out;
+    int64_t nmv = 0;
+    if (niv >= nume && niv <= lim) {
+      int a = niv;
+      orthogonalize_block(0, a);
+      niv = a;
+    } else {
+      niv = 0;
+    }
+    if (niv < nume) {
+      std::vector<uint64_t> idx(n);
+      std::iota(idx.begin(), idx.end(), 0);
+      std::partial_sort(idx.begin(), idx.begin() + std::min<uint64_t>(nume, n), idx.end(),
+                        [&](uint64_t x, uint64_t y) { return hdiag[x] < hdiag[y] || (hdiag[x] == hdiag[y] && x < y); });
+      k_zero_cols<T><<<blocks_for(n * (nume - niv)), 256, 0, s>>>(n, B.p, L, niv, nume - niv);
+      set_unit_start(niv, nume - niv, idx);
+      int b2 = nume - niv;
+      orthogonalize_block(niv, b2);
+      niv += b2;
+    }
+    kpass = niv;
+    add_ab_s(0, kpass, nmv);
+    const int keep = std::max(nume, std::min(cfg.keep > 0 ? cfg.keep : 2 * nume, lim - mblock));
+    int nloops = 0;
+    bool done = false;
+    std::vector<double> rn;
+    std::fill(eigs.begin(), eigs.end(), 0.0);
+    for (;;) {
+      for (int i = 0; i < nume; ++i) old[i] = eigs[i];
+      diagonalize();
+      if (kpass + mblock > lim) {
+        double tc0 = now();
+        int kp = std::min(keep, kpass);
+        std::vector<double> G(size_t(kpass) * kp);
+        for (int k = 0; k < kpass; ++k)
+          for (int j = 0; j < kp; ++j) G[size_t(k) * kp + j] = svec(j, k);
+        gemm(B.p, 0, kpass, G, B.p, 0, kp, 1.0, 0.0);
+        gemm(AB.p, 0, kpass, G, AB.p, 0, kp, 1.0, 0.0);
+        std::fill(S.begin(), S.end(), 0.0);
+        for (int i = 0; i < kp; ++i) S[size_t(i) * lim + i] = wall_[i];
+        zvec.assign(size_t(kp) * kp, 0.0);
+        for (int i = 0; i < kp; ++i) zvec[size_t(i) * kp + i] = 1.0;
+        kpass = kp;
+        ++out.restarts;
+        t_collapse += now() - tc0;
+      }
+      std::vector<int> all(nume);
+      std::iota(all.begin(), all.end(), 0);
+      rn = residuals(all);
+      std::vector<int> unc;
+      for (int i = 0; i < nume; ++i)
+        if (!(rn[i] < cfg.critr)) unc.push_back(i);
+      if (cfg.verbose & 1) {
+        double mx = 0;
+        for (double r : rn) mx = std::max(mx, r);
+        std::fprintf(stderr, "dav[%s] it %d kpass %d unconverged %zu max_resid %.3e E0 %.8f E%d %.8f\n",
+                     sizeof(T) == 4 ? "fp32" : "fp64", nloops, kpass, unc.size(), mx, eigs[0], nume - 1,
+                     eigs[nume - 1]);
+      }
+      if (unc.empty()) { done = true; break; }
+      if (nloops >= cfg.maxiter) break;
+      std::stable_sort(unc.begin(), unc.end(), [&](int a, int b) { return rn[a] > rn[b]; });
+      int add = std::min<int>(int(unc.size()), std::min(mblock, lim - kpass));
+      std::vector<int> sel_r(unc.begin(), unc.begin() + add);
+      std::vector<double> lam(add);
+      for (int a = 0; a < add; ++a) lam[a] = eigs[sel_r[a]];
+      if (cfg.precond) precond_copy(sel_r, lam, kpass);
+      else copy_residuals(sel_r, kpass);
+      int nncv = add;
+      orthogonalize_block(kpass, nncv);
+      if (nncv == 0) { ierr_stall = true; break; }
+      add_ab_s(kpass, nncv, nmv);
+      kpass += nncv;
+      ++nloops;
+    }
+    out.de.resize(nume);
+    for (int i = 0; i < nume; ++i) out.de[i] = std::fabs(old[i] - eigs[i]);
+    // final Ritz vectors in B[:, 0:nume]
+    if (kpass != nume) {
+      std::vector<double> G(size_t(kpass) * nume);
+      for (int k = 0; k < kpass; ++k)
+        for (int j = 0; j < nume; ++j) G[size_t(k) * nume + j] = svec(j, k);
+      gemm(B.p, 0, kpass, G, B.p, 0, nume, 1.0, 0.0);
+      gemm(AB.p, 0, kpass, G, AB.p, 0, nume, 1.0, 0.0);
+      kpass = nume;
+      zvec.assign(size_t(nume) * nume, 0.0);
+      for (int i = 0; i < nume; ++i) zvec[size_t(i) * nume + i] = 1.0;
+    }
+    std::vector<int> all(nume);
+    std::iota(all.begin(), all.end(), 0);
+    out.resid = residuals(all);
+    out.eig.assign(eigs.begin(), eigs.begin() + nume);
+    out.iterations = nloops;
+    out.matvecs = nmv;
+    out.ierr = done ? 0 : (ierr_stall ? 1024 : 2048);
+    out.spmm_seconds = spmm_s;
+    out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (cfg.verbose >= 2)
+      std::fprintf(stderr,
+                   "dav[%s] phases: total %.3f s, spmm %.3f, ab+S %.3f, eig %.3f, resid %.3f, ortho %.3f, "
+                   "collapse %.3f (iterations %d)\n",
+                   sizeof(T) == 4 ? "fp32" : "fp64", out.seconds, spmm_s, t_abs, t_eig, t_resid, t_ortho,
+                   t_collapse, nloops);
+    return out;
+  }
+  bool ierr_stall = false;
+
+  // B[:, bo + a] = R[:, sel[a]] (no preconditioner)
+  void copy_residuals(const std::vector<int>& sel_r, int bo) {
+    for (int a = 0; a < int(sel_r.size()); ++a) {
+      k_copy_cols<T><<<blocks_for(n), 256, 0, s>>>(n, R.p, ldr, sel_r[a], B.p, L, bo + a, 1);
+      CG_CUDA(cudaGetLastError());
+    count_launch();
+    }
   }
 
   // Run the iteration.  niv: number of valid starting columns already in B.
@@ -701,12 +1103,14 @@ static void load_start(Engine<T>& e, const double* init_dev_cm, int ninit) {
   if (!ninit) return;
   k_cm_to_rm<T><<<blocks_for(e.n * ninit), 256, 0, e.s>>>(e.n, ninit, init_dev_cm, e.B.p, e.L, 0);
   CG_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 template <class T>
 static void store_vectors(Engine<T>& e, int m, double* dst_dev_cm) {
   k_rm_to_cm<T><<<blocks_for(e.n * m), 256, 0, e.s>>>(e.n, m, e.B.p, e.L, 0, dst_dev_cm);
   CG_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 DavResult davidson_solve(const Hamiltonian& h, const DavidsonRequest& rq) {
@@ -729,7 +1133,8 @@ DavResult davidson_solve(const Hamiltonian& h, const DavidsonRequest& rq) {
   if (rq.phase1.spmm_prec == CG_PREC_FP64) {
     Engine<double> e(h, rq.phase1, s);
     load_start(e, init.p, std::min(ninit, e.lim));
-    DavOutcome o = e.run(std::min(ninit, e.lim + 1), hdiag);
+    DavOutcome o = rq.phase1.modern ? e.run_modern(std::min(ninit, e.lim + 1), hdiag)
+                                    : e.run(std::min(ninit, e.lim + 1), hdiag);
     store_vectors(e, nume, vecs.p);
     res.phase1 = o;
     res.final_ = o;
@@ -738,7 +1143,8 @@ DavResult davidson_solve(const Hamiltonian& h, const DavidsonRequest& rq) {
     {
       Engine<float> e(h, rq.phase1, s);
       load_start(e, init.p, std::min(ninit, e.lim));
-      o1 = e.run(std::min(ninit, e.lim + 1), hdiag);
+      o1 = rq.phase1.modern ? e.run_modern(std::min(ninit, e.lim + 1), hdiag)
+                            : e.run(std::min(ninit, e.lim + 1), hdiag);
       store_vectors(e, nume, vecs.p);
     }
     res.phase1 = o1;
@@ -746,7 +1152,7 @@ DavResult davidson_solve(const Hamiltonian& h, const DavidsonRequest& rq) {
     if (rq.refine) {
       Engine<double> e(h, rq.phase2, s);
       load_start(e, vecs.p, nume);
-      DavOutcome o2 = e.run(nume, hdiag);
+      DavOutcome o2 = rq.phase2.modern ? e.run_modern(nume, hdiag) : e.run(nume, hdiag);
       store_vectors(e, nume, vecs.p);
       res.phase2 = o2;
       res.final_ = o2;

@@ -21,6 +21,10 @@ namespace cg {
                             std::to_string(__LINE__) + ")");                                     \
   } while (0)
 
+// Kernel launches issued by this library (for benchmark accounting).
+uint64_t& launch_counter();
+inline void count_launch(uint64_t k = 1) { launch_counter() += k; }
+
 // Owning device buffer.
 template <class T>
 struct DBuf {
@@ -109,6 +113,17 @@ constexpr int kMOff = 64;  // 2m in [-64, 64]
 void upload_operator(const System& sys, const Operator& op, DevOperator& d, cudaStream_t s);
 
 // ----------------------------------------------------------- Hamiltonian
+// Launch shape of the FP32 product (chosen by spmm_autotune).
+struct SpmmTuning {
+  int warps = 16;       // warps per CTA
+  int ctas_per_sm = 2;  // resident CTAs per SM the grid is sized for
+  bool tuned = false;
+};
+struct SpmmCandidate {
+  int warps, ctas_per_sm;
+  float ms;
+};
+
 struct Hamiltonian {
   int device = 0;
   int precision = CG_PREC_FP64;
@@ -120,6 +135,7 @@ struct Hamiltonian {
   DBuf<double> val64;     // nnz (CG_PREC_FP64)
   DBuf<float> hi, lo;     // nnz (CG_PREC_FP32)
   DBuf<double> diag;      // n
+  SpmmTuning tuning;
   cudaStream_t stream = nullptr;
   ~Hamiltonian();
   uint64_t device_bytes() const {
@@ -135,6 +151,15 @@ void hamiltonian_upper_rows(const Hamiltonian& h, uint64_t row0, uint64_t nrows,
 // Row-interleaved operands: element (i, k) at x[i*ldx + k].
 void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, void* y, int ldy, int m,
                  cudaStream_t s);
+// FP32 product of m <= 16 vectors from a staging block whose rows are 32-byte
+// aligned and padded with zero vectors to 8 or 16 (ldx >= 8 or 16); only the
+// first m outputs of each row are stored.
+void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m, cudaStream_t s);
+std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps);
+// Refinement product Y = H X (FP64 in and out, any m) computed in double-float
+// FP32 arithmetic from the stored (hi, lo) values; stage holds n x 16 floats.
+void spmm_refine_df(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m, float* stage,
+                    cudaStream_t s);
 // Host column-major doubles in and out (vector k at k*n), any m >= 1.
 void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, int m);
 

@@ -412,6 +412,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   CG_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), s));
   k_count<<<grid, T, 0, s>>>(c, b.binom.p, counts.p, derr.p);
   CG_CUDA(cudaGetLastError());
+    count_launch();
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
 
@@ -422,6 +423,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   if (n) {
     k_scan_local<<<unsigned(ntiles), kScanT, 0, s>>>(counts.p, n, h.rowptr.p, tsum.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
   std::vector<uint64_t> ht(ntiles);
   if (ntiles) CG_CUDA(cudaMemcpyAsync(ht.data(), tsum.p, ntiles * 8, cudaMemcpyDeviceToHost, s));
@@ -440,6 +442,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
     tsum.upload(ht, s);
     k_scan_add<<<unsigned((n + 255) / 256), 256, 0, s>>>(h.rowptr.p, n, tsum.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
   CG_CUDA(cudaMemcpyAsync(h.rowptr.p + n, &h.nnz, 8, cudaMemcpyHostToDevice, s));
   counts.release();
@@ -450,6 +453,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   if (n) {
     k_fill<<<grid, T, 0, s>>>(c, b.binom.p, h.rowptr.p, h.col.p, tmpval.p, h.diag.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
   if (precision == CG_PREC_FP64) {
     h.val64.alloc(std::max<uint64_t>(h.nnz, 1));
@@ -470,6 +474,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
     unsigned sg = unsigned(std::min<uint64_t>(n, 152ull * 16));
     k_sort_rows<<<sg, st, smem, s>>>(n, h.rowptr.p, h.col.p, tmpval.p, h.val64.p, h.hi.p, h.lo.p, dup.p);
     CG_CUDA(cudaGetLastError());
+    count_launch();
   }
   unsigned long long up = 0;
   CG_CUDA(cudaMemcpyAsync(&up, dup.p, 8, cudaMemcpyDeviceToHost, s));

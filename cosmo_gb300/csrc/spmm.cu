@@ -13,9 +13,9 @@
 //
 // Modes:
 //   CG_PREC_FP64   FP64 values, FP64 vectors, FP64 accumulation.
-//   CG_PREC_FP32   FP32 values and vectors; each lane accumulates its products
-//                  in FP32, the cross-lane (across row blocks) sum is FP64, the
-//                  result is rounded once to FP32.
+//   CG_PREC_FP32   FP32 values and vectors, FP32 accumulation in each lane and
+//                  across the warp (GB300 runs FP64 at ~1/60 of the FP32 rate;
+//                  the FP64 accumulation lives in the Davidson projections).
 //   CG_PREC_REFINE FP32 hi + FP32 lo values (h = hi + lo to ~2^-48), FP64
 //                  vectors and accumulation.
 #include <algorithm>
@@ -69,6 +69,11 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 
 // Each CTA owns rows [r0, r1); its warps take rows r0 + w, r0 + w + 8, ...
 template <int NV, int MODE, int VW>
@@ -100,8 +105,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_spmm(uint64_t n, const ui
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] = fmaf(h, xx[k], acc[k]);
       }
+      // cross-lane sum in FP32: on GB300 an FP64 warp reduction per row costs
+      // more FP64-pipe time than the whole row's memory traffic
 #pragma unroll
-      for (int k = 0; k < NV; ++k) tot[k] = warp_sum(double(acc[k]));
+      for (int k = 0; k < NV; ++k) tot[k] = double(warp_sumf(acc[k]));
     } else {
       double acc[NV];
 #pragma unroll
@@ -128,6 +135,68 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_spmm(uint64_t n, const ui
   }
 }
 
+// 256-bit gather of 8 consecutive FP32 components (one 32-byte sector).
+__device__ __forceinline__ void ld8(const float* __restrict__ p, float (&v)[8]) {
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "l"(p));
+}
+
+// FP32 product for NV = 8 or 16 vectors whose rows are 32-byte aligned.
+// Per stored entry one lane issues NV/8 sector-wide gathers (the L1 data pipe
+// is charged per sector touched by an instruction, so one wide load per 8
+// vectors is the cheapest gather).  The row sum uses a reduce-scatter across
+// the warp: at each halving step a lane keeps one half of its partial sums
+// and receives the partner's other half, so NV = 8 costs 9 shuffles per row
+// instead of 5 * NV.  Only the first m_out components are stored.
+template <int NV, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_spmm_f32w(uint64_t n, const uint64_t* __restrict__ rowptr,
+                                                                 const uint32_t* __restrict__ col,
+                                                                 const float* __restrict__ vals,
+                                                                 const float* __restrict__ x, int ldx,
+                                                                 float* __restrict__ y, int ldy, int m_out,
+                                                                 uint64_t rows_per_cta) {
+  static_assert(NV == 8 || NV == 16, "NV must be 8 or 16");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t r0 = uint64_t(blockIdx.x) * rows_per_cta;
+  const uint64_t r1 = min(n, r0 + rows_per_cta);
+  for (uint64_t row = r0 + warp; row < r1; row += WARPS) {
+    const uint64_t b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+    float acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.f;
+    for (uint64_t p = b + lane; p < e; p += 32) {
+      const uint32_t c = __ldcs(col + p);
+      const float h = __ldcs(vals + p);
+      const float* xp = x + uint64_t(c) * ldx;
+#pragma unroll
+      for (int g = 0; g < NV / 8; ++g) {
+        float xx[8];
+        ld8(xp + 8 * g, xx);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[8 * g + j] = fmaf(h, xx[j], acc[8 * g + j]);
+      }
+    }
+    // reduce-scatter: offsets 16, 8, 4 (and 2 for NV = 16) halve the values per lane
+#pragma unroll
+    for (int o = 16, c = NV; c > 1; o >>= 1, c >>= 1) {
+      const bool up = lane & o;
+#pragma unroll
+      for (int k = 0; k < c / 2; ++k) {
+        float send = up ? acc[k] : acc[c / 2 + k];
+        float keep = up ? acc[c / 2 + k] : acc[k];
+        acc[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    }
+    // the lane group sharing a vector index finishes with plain xor steps
+    constexpr int kShift = NV == 8 ? 2 : 1;  // lanes per vector index = 32 / NV
+#pragma unroll
+    for (int o = (1 << kShift) >> 1; o; o >>= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
+    const int vi = lane >> kShift;
+    if ((lane & ((1 << kShift) - 1)) == 0 && vi < m_out) y[row * uint64_t(ldy) + vi] = acc[0];
+  }
+}
+
 template <int MODE, int NV, int VW>
 void run_kernel(const Hamiltonian& h, const void* vals, const void* x, int ldx, void* y, int ldy, cudaStream_t s) {
   int nsm = 0;
@@ -143,13 +212,145 @@ void run_kernel(const Hamiltonian& h, const void* vals, const void* x, int ldx, 
   k_spmm<NV, MODE, VW><<<grid, kWarpsPerCta * 32, 0, s>>>(h.n, h.rowptr.p, h.col.p, vals, h.lo.p, x, ldx, y, ldy,
                                                            rpc);
   CG_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 // Widest vector load the operands allow: VW elements divide NV, the base
 // address and the row pitch.
+// ---- double-float refinement product ------------------------------------
+// Error-free transformations (Knuth two-sum, FMA two-product) on FP32 pairs
+// (hi, lo): ~48-bit accurate sums and products on the FP32 pipe, which GB300
+// runs ~60x faster than FP64.
+struct df32 {
+  float hi, lo;
+};
+__device__ __forceinline__ df32 two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ df32 quick_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+// acc += (ah + al) * (bh + bl)
+__device__ __forceinline__ void df_fma(df32& acc, float ah, float al, float bh, float bl) {
+  float p = ah * bh;
+  float pe = fmaf(ah, bh, -p);
+  pe = fmaf(ah, bl, fmaf(al, bh, pe));
+  df32 s = two_sum(acc.hi, p);
+  s.lo += acc.lo + pe;
+  acc = quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  df32 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+
+// Y = H X for 8 vectors in double-float.  X is staged as rows of 16 floats:
+// 8 hi parts then 8 lo parts (two sector-wide gathers per stored entry); the
+// matrix values are the stored (hi, lo) pair; Y is written as FP64.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_spmm_df8(uint64_t n, const uint64_t* __restrict__ rowptr,
+                                                         const uint32_t* __restrict__ col,
+                                                         const float* __restrict__ vhi,
+                                                         const float* __restrict__ vlo,
+                                                         const float* __restrict__ x, double* __restrict__ y,
+                                                         int ldy, int m_out, uint64_t rows_per_cta) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t r0 = uint64_t(blockIdx.x) * rows_per_cta;
+  const uint64_t r1 = min(n, r0 + rows_per_cta);
+  for (uint64_t row = r0 + warp; row < r1; row += WARPS) {
+    const uint64_t b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+    df32 acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = {0.f, 0.f};
+    for (uint64_t p = b + lane; p < e; p += 32) {
+      const uint32_t c = __ldcs(col + p);
+      const float hh = __ldcs(vhi + p), hl = __ldcs(vlo + p);
+      float xh[8], xl[8];
+      ld8(x + uint64_t(c) * 16, xh);
+      ld8(x + uint64_t(c) * 16 + 8, xl);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) df_fma(acc[k], hh, hl, xh[k], xl[k]);
+    }
+    // reduce-scatter across the warp (offsets 16, 8, 4), then offsets 2, 1
+#pragma unroll
+    for (int o = 16, cnt = 8; cnt > 1; o >>= 1, cnt >>= 1) {
+      const bool up = lane & o;
+#pragma unroll
+      for (int k = 0; k < cnt / 2; ++k) {
+        df32 send = up ? acc[k] : acc[cnt / 2 + k];
+        df32 keep = up ? acc[cnt / 2 + k] : acc[k];
+        df32 got{__shfl_xor_sync(0xffffffffu, send.hi, o), __shfl_xor_sync(0xffffffffu, send.lo, o)};
+        acc[k] = df_add(keep, got);
+      }
+    }
+#pragma unroll
+    for (int o = 2; o; o >>= 1) {
+      df32 got{__shfl_xor_sync(0xffffffffu, acc[0].hi, o), __shfl_xor_sync(0xffffffffu, acc[0].lo, o)};
+      acc[0] = df_add(acc[0], got);
+    }
+    const int vi = lane >> 2;
+    if ((lane & 3) == 0 && vi < m_out) y[row * uint64_t(ldy) + vi] = double(acc[0].hi) + double(acc[0].lo);
+  }
+}
+
+// x (FP64, row-interleaved, m <= 8 columns) -> staging rows of 8 hi + 8 lo floats
+__global__ void k_stage_df(uint64_t n, const double* __restrict__ x, int ldx, int m, float* __restrict__ w) {
+  uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * 8) return;
+  uint64_t i = idx >> 3;
+  int j = int(idx & 7);
+  double v = j < m ? x[i * ldx + j] : 0.0;
+  float h = float(v);
+  w[i * 16 + j] = h;
+  w[i * 16 + 8 + j] = float(v - double(h));
+}
+
+// Launch shape of the FP32 product: WARPS warps per CTA, CTAS CTAs per SM,
+// each CTA walking one contiguous row range (so the warps sharing an SM work on
+// neighbouring rows, whose columns overlap, and reuse gathered vectors in L1).
+template <int NV, int WARPS>
+void launch_wide(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m_out, int ctas_per_sm,
+                 cudaStream_t s) {
+  int nsm = 0;
+  CG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h.device));
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_f32w<NV, WARPS>, WARPS * 32, 0));
+  int use = std::max(1, std::min(per_sm, ctas_per_sm));
+  uint64_t ctas = uint64_t(nsm) * use;
+  uint64_t rpc = (h.n + ctas - 1) / ctas;
+  rpc = (rpc + WARPS - 1) / WARPS * WARPS;
+  if (rpc == 0) rpc = WARPS;
+  unsigned grid = unsigned((h.n + rpc - 1) / rpc);
+  if (grid == 0) return;
+  k_spmm_f32w<NV, WARPS><<<grid, WARPS * 32, 0, s>>>(h.n, h.rowptr.p, h.col.p, h.hi.p, x, ldx, y, ldy, m_out, rpc);
+  CG_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+template <int NV>
+void run_wide(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m_out, cudaStream_t s) {
+  const SpmmTuning& t = h.tuning;
+  switch (t.warps) {
+    case 4: return launch_wide<NV, 4>(h, x, ldx, y, ldy, m_out, t.ctas_per_sm, s);
+    case 8: return launch_wide<NV, 8>(h, x, ldx, y, ldy, m_out, t.ctas_per_sm, s);
+    case 16: return launch_wide<NV, 16>(h, x, ldx, y, ldy, m_out, t.ctas_per_sm, s);
+    case 32: return launch_wide<NV, 32>(h, x, ldx, y, ldy, m_out, t.ctas_per_sm, s);
+    default: throw Error(CG_ERR_ARG, "SpMM tuning: warps per CTA must be 4, 8, 16 or 32");
+  }
+}
+
 template <int MODE, int NV>
 void run_nv(const Hamiltonian& h, const void* vals, const void* x, int ldx, void* y, int ldy, cudaStream_t s) {
   constexpr size_t esz = MODE == CG_PREC_FP32 ? 4 : 8;
+  if constexpr (MODE == CG_PREC_FP32 && (NV == 8 || NV == 16)) {
+    if (reinterpret_cast<uintptr_t>(x) % 32 == 0 && ldx % 8 == 0)
+      return run_wide<NV>(h, static_cast<const float*>(x), ldx, static_cast<float*>(y), ldy, NV, s);
+  }
   auto ok = [&](size_t vw) {
     return NV % vw == 0 && reinterpret_cast<uintptr_t>(x) % (vw * esz) == 0 && (size_t(ldx) % vw) == 0;
   };
@@ -206,9 +407,20 @@ void spmm_host_t(const Hamiltonian& h, int precision, const double* x, double* y
     unsigned g = unsigned((n * mc + 255) / 256);
     if (g) k_cm_to_rm<T><<<g, 256, 0, s>>>(n, mc, cm.p + uint64_t(c0) * n, xi.p, ld);
     CG_CUDA(cudaGetLastError());
-    spmm_launch(h, precision, xi.p, ld, yi.p, ld, mc, s);
+    count_launch();
+    if constexpr (std::is_same<T, double>::value) {
+      if (precision == CG_PREC_REFINE) {
+        DBuf<float> stage(n * 16);
+        spmm_refine_df(h, xi.p, ld, yi.p, ld, mc, stage.p, s);
+      } else {
+        spmm_launch(h, precision, xi.p, ld, yi.p, ld, mc, s);
+      }
+    } else {
+      spmm_launch(h, precision, xi.p, ld, yi.p, ld, mc, s);
+    }
     if (g) k_rm_to_cm<T><<<g, 256, 0, s>>>(n, mc, yi.p, ld, cm.p + uint64_t(c0) * n);
     CG_CUDA(cudaGetLastError());
+    count_launch();
     CG_CUDA(cudaStreamSynchronize(s));
   }
   CG_CUDA(cudaMemcpyAsync(y, cm.p, n * m * 8, cudaMemcpyDeviceToHost, s));
@@ -221,6 +433,88 @@ void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, 
   if (m < 1) throw Error(CG_ERR_ARG, "m must be >= 1");
   if (precision == CG_PREC_FP32) spmm_host_t<float>(h, precision, x, y, m);
   else spmm_host_t<double>(h, precision, x, y, m);
+}
+
+// Autotuner: time every candidate launch shape of the FP32 product on this
+// matrix (CUDA events on the handle's stream, median of `reps`) and keep the
+// fastest in h.tuning.  Returns the per-candidate times.
+std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
+  if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "autotuning applies to FP32 matrices");
+  const int ld = m <= 8 ? 8 : 16;
+  cudaStream_t s = h.stream;
+  DBuf<float> x(h.n * ld), y(h.n * ld);
+  CG_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), s));
+  cudaEvent_t e0, e1;
+  CG_CUDA(cudaEventCreate(&e0));
+  CG_CUDA(cudaEventCreate(&e1));
+  std::vector<SpmmCandidate> out;
+  const SpmmTuning keep = h.tuning;
+  float best = 1e30f;
+  SpmmTuning bt = keep;
+  for (int w : {4, 8, 16, 32})
+    for (int c : {1, 2, 4, 8}) {
+      if (w * c > 64) continue;  // at most 64 resident warps per SM
+      h.tuning.warps = w;
+      h.tuning.ctas_per_sm = c;
+      spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);  // warm
+      std::vector<float> ts;
+      for (int r = 0; r < reps; ++r) {
+        CG_CUDA(cudaEventRecord(e0, s));
+        spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);
+        CG_CUDA(cudaEventRecord(e1, s));
+        CG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ts.push_back(ms);
+      }
+      std::sort(ts.begin(), ts.end());
+      float med = ts[ts.size() / 2];
+      out.push_back({w, c, med});
+      if (med < best) { best = med; bt = h.tuning; }
+    }
+  h.tuning = bt;
+  h.tuning.tuned = true;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return out;
+}
+
+void spmm_refine_df(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m, float* stage,
+                    cudaStream_t s) {
+  if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "refinement product needs an FP32 (hi+lo) matrix");
+  for (int c0 = 0; c0 < m; c0 += 8) {
+    const int mc = std::min(8, m - c0);
+    k_stage_df<<<unsigned((h.n * 8 + 255) / 256), 256, 0, s>>>(h.n, x + c0, ldx, mc, stage);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    int nsm = 0;
+    CG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h.device));
+    constexpr int W = 8;
+    int per_sm = 0;
+    CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_df8<W>, W * 32, 0));
+    uint64_t ctas = uint64_t(nsm) * std::max(per_sm, 1);
+    uint64_t rpc = (h.n + ctas - 1) / ctas;
+    rpc = (rpc + W - 1) / W * W;
+    if (rpc == 0) rpc = W;
+    unsigned grid = unsigned((h.n + rpc - 1) / rpc);
+    if (grid)
+      k_spmm_df8<W><<<grid, W * 32, 0, s>>>(h.n, h.rowptr.p, h.col.p, h.hi.p, h.lo.p, stage, y + c0, ldy, mc, rpc);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+  }
+}
+
+void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m, cudaStream_t s) {
+  if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "FP32 product needs an FP32 matrix");
+  if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "padded FP32 SpMM takes 1..16 vectors");
+  if (reinterpret_cast<uintptr_t>(x) % 32 || ldx % 8) throw Error(CG_ERR_ARG, "padded FP32 SpMM needs 32-byte rows");
+  if (m <= 8) {
+    if (ldx < 8) throw Error(CG_ERR_ARG, "ldx < 8");
+    run_wide<8>(h, x, ldx, y, ldy, m, s);
+  } else {
+    if (ldx < 16) throw Error(CG_ERR_ARG, "ldx < 16");
+    run_wide<16>(h, x, ldx, y, ldy, m, s);
+  }
 }
 
 void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, void* y, int ldy, int m,

@@ -36,7 +36,7 @@ typedef int32_t cg_status;
 
 /* precision of a stored Hamiltonian / of an SpMM call */
 #define CG_PREC_FP64 0   /* FP64 values, FP64 vectors                        */
-#define CG_PREC_FP32 1   /* FP32 values and vectors, FP32 in-row, FP64 across */
+#define CG_PREC_FP32 1   /* FP32 values and vectors, FP32 accumulation          */
 #define CG_PREC_REFINE 2 /* FP32 hi + FP32 lo values (~FP64), FP64 vectors    */
 
 /* Last error message of the calling thread ("" if none). */
@@ -45,6 +45,8 @@ const char* cg_last_error(void);
 int32_t cg_version(void);
 /* Number of CUDA devices visible, or a negative status. */
 int32_t cg_device_count(void);
+/* Kernel launches this library has issued in this process (monotonic). */
+uint64_t cg_launch_count(void);
 
 /* --------------------------------------------------------------- problem */
 /* Host-side CI problem: valence space, s.p. states, system quantum numbers and
@@ -168,6 +170,16 @@ cg_status cg_spmm(const cg_hamiltonian* h, const double* x, double* y, int32_t m
 cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, void* y, int32_t ldy, int32_t m,
                          int32_t precision);
 
+/* Launch-shape autotuner of the FP32 product: times every candidate (warps per
+ * CTA x CTAs per SM, each CTA on one contiguous row range) with `nvec` vectors
+ * on this matrix, keeps the fastest in the handle, and reports all candidates
+ * (arrays of capacity *n_candidates on entry, count on return). */
+cg_status cg_spmm_autotune(cg_hamiltonian* h, int32_t nvec, int32_t reps, int32_t* n_candidates, int32_t* warps,
+                           int32_t* ctas_per_sm, float* ms);
+/* Set (e.g. from a cached tuning) or read the launch shape of the FP32 product. */
+cg_status cg_spmm_set_tuning(cg_hamiltonian* h, int32_t warps, int32_t ctas_per_sm);
+cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* ctas_per_sm, int32_t* tuned);
+
 /* -------------------------------------------------------------- Davidson */
 /* Block Davidson for the lowest eigenpairs (Davidson-Liu with diagonal
  * preconditioning, classical Gram-Schmidt with re-orthogonalisation, restart by
@@ -192,6 +204,13 @@ typedef struct {
   int32_t verbose;   /* 0 silent, 1 per-iteration line on stderr          */
   int32_t ortho_block; /* FP64 only: 0 = one vector at a time as the reference,
                           1 = block Gram-Schmidt (the FP32 phase always uses blocks) */
+  int32_t algorithm; /* -1 (default): 0 for FP64, 1 for FP32;
+                        0: the reference control flow (convergence bookkeeping of
+                        Test_Convergence, collapse to nstates vectors);
+                        1: residual-driven block Davidson: every wanted residual is
+                        re-checked each iteration, restarts keep `keep` Ritz vectors */
+  int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates) */
+  int32_t precond;   /* algorithm 1: 1 = diagonal preconditioner (lambda - H_ii), 0 = none */
 } cg_davidson_params;
 
 typedef struct {
