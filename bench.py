@@ -107,6 +107,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(seconds: float, dist=None, device=None) -> float:
+    """Slowest rank's time (replicas: every rank solves its own copy)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -216,11 +226,7 @@ def run_ours(args):
     t1 = time.perf_counter()
     launches = cg.launch_count() - l0
     clocks.stop()
-    elapsed = t1 - t0
-    if dist:
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(t1 - t0, dist, "cuda")
     per_solve = elapsed / args.steps
     last = results[-1]
 
