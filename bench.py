@@ -43,9 +43,14 @@ WORKLOAD = dict(workload="fp-shell 4p+4n M=0, lowest 10 eigenpairs, |dE|<=1e-4 M
                 l2="inputs larger than L2 (stored H ~15 GB, vectors ~300 MB)")
 # Davidson settings of the mixed solve (block vectors per SpMM, basis limit)
 MIXED = dict(block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5)
-# iterations of the reference algorithm to reach resid <= 1e-5 on this problem,
-# measured with the same algorithm in FP64 (used to scale the CPU sample)
-REF_ITERS_DEFAULT = None
+# Iterations the reference algorithm (block 10, limit 30) runs on this problem:
+# its 400-iteration cap (max(40 * nstates, 200)), which it reaches without
+# converging all 10 pairs to 1e-5 (measured with the same algorithm in FP64 on
+# the GPU), so CPU samples scaled by it are a lower bound of the CPU solve time.
+REF_ITERS_DEFAULT = 400
+# DRAM bytes (read + write) of one k_spmm_f32w<8> launch on this workload,
+# measured with ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum.
+NCU_TRAFFIC_BYTES = {("k_spmm_f32w<8>", "fp44"): 11.71e9 + 64.59e6}
 
 
 def env_rank():
@@ -249,6 +254,11 @@ def run_ours(args):
 
     # SpMM roofline (FP32 mixed kernel, block of 10 vectors)
     spmm_s, alg_bytes = spmm_roofline(cg, H, MIXED["block"])
+    # the product's dominant traffic is one 32-byte vector gather per stored
+    # entry; its ceiling is the device's random-gather rate over a table the
+    # size of the vector block (L2 resident)
+    gathers = int(H.info.nnz_full)
+    g_peak = cg.gather_ceiling(int(H.n), 1)
     kernel_name = f"k_spmm_f32w<{8 if MIXED['block'] <= 8 else 16}>"
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / spmm_s / 1e9
@@ -285,8 +295,12 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": kernel_name,
+                     "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES.get((kernel_name, "fp44")),
+                     "kernel": kernel_name,
                      "peak_source": peak_kind, "launch_ms": spmm_s * 1e3, "alg_bytes": alg_bytes},
+        "gather_roofline": {"achieved": gathers / spmm_s, "peak": g_peak, "unit": "gathers/s",
+                            "frac": gathers / spmm_s / g_peak,
+                            "note": "32-byte gathers of the 8-vector block, probe over an n-row table"},
         "clocks": clocks.summary(),
         "spmm_tuning": {k: v for k, v in tuning.items() if k != "candidates"},
         "solve": {"iterations": int(last.stats.iterations), "refine_iterations": int(last.stats.refine_iterations),
@@ -367,7 +381,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--fp64-maxiter", type=int, default=400)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--ref-iters", type=int, default=200)
+    ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--mode", default="solve", choices=["solve", "spmm"])
     ap.add_argument("--config", default="fp44", choices=sorted(CONFIGS))
     ap.add_argument("--nvec", type=int, default=10)

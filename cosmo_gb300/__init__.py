@@ -101,6 +101,7 @@ _SIGS = {
     "cg_spmm_device": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32]),
     "cg_spmm_autotune": (C.c_int32, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _P, _P, _P]),
     "cg_spmm_set_tuning": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
     "cg_davidson": (C.c_int32, [_P, C.POINTER(DavidsonParams), _P, C.c_int32, _P, _P, _P, _P,
@@ -137,6 +138,13 @@ def _ptr(a: np.ndarray) -> int:
 
 def device_count() -> int:
     return int(lib().cg_device_count())
+
+
+def gather_ceiling(rows: int, share: int = 1) -> float:
+    """Random 32-byte gathers per second from a table of `rows` rows (device probe)."""
+    g = C.c_double()
+    _check(lib().cg_gather_ceiling(rows, share, C.byref(g)))
+    return float(g.value)
 
 
 def launch_count() -> int:

@@ -394,6 +394,16 @@ cg_status cg_spmm_autotune(cg_hamiltonian* h, int32_t nvec, int32_t reps, int32_
   });
 }
 
+cg_status cg_gather_ceiling(uint64_t rows, int32_t share, double* gathers_per_second) {
+  return guard([&] {
+    CG_NOT_NULL(gathers_per_second);
+    require_device();
+    int dev = 0;
+    CG_CUDA(cudaGetDevice(&dev));
+    *gathers_per_second = cg::gather_probe(dev, rows, share);
+  });
+}
+
 cg_status cg_spmm_set_tuning(cg_hamiltonian* h, int32_t warps, int32_t ctas_per_sm) {
   return guard([&] {
     CG_NOT_NULL(h);

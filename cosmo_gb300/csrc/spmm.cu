@@ -165,7 +165,33 @@ __global__ void __launch_bounds__(WARPS * 32) k_spmm_f32w(uint64_t n, const uint
     float acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.f;
-    for (uint64_t p = b + lane; p < e; p += 32) {
+    // four entries per lane per step, all loads issued before any use, so each
+    // lane keeps four gathers in flight (the loop is latency bound otherwise)
+    uint64_t p = b + lane;
+    for (; p + 96 < e; p += 128) {
+      uint32_t c[4];
+      float h[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = __ldcs(col + p + 32 * u);
+        h[u] = __ldcs(vals + p + 32 * u);
+      }
+      float xx[4][NV];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int g = 0; g < NV / 8; ++g) {
+          float t[8];
+          ld8(x + uint64_t(c[u]) * ldx + 8 * g, t);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) xx[u][8 * g + j] = t[j];
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = fmaf(h[u], xx[u][k], acc[k]);
+    }
+    for (; p < e; p += 32) {
       const uint32_t c = __ldcs(col + p);
       const float h = __ldcs(vals + p);
       const float* xp = x + uint64_t(c) * ldx;
@@ -267,7 +293,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_spmm_df8(uint64_t n, const uint6
     df32 acc[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) acc[k] = {0.f, 0.f};
-    for (uint64_t p = b + lane; p < e; p += 32) {
+    uint64_t p = b + lane;
+    for (; p + 32 < e; p += 64) {
+      uint32_t c[2];
+      float hh[2], hl[2], xh[2][8], xl[2][8];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        c[u] = __ldcs(col + p + 32 * u);
+        hh[u] = __ldcs(vhi + p + 32 * u);
+        hl[u] = __ldcs(vlo + p + 32 * u);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        ld8(x + uint64_t(c[u]) * 16, xh[u]);
+        ld8(x + uint64_t(c[u]) * 16 + 8, xl[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) df_fma(acc[k], hh[u], hl[u], xh[u][k], xl[u][k]);
+    }
+    for (; p < e; p += 32) {
       const uint32_t c = __ldcs(col + p);
       const float hh = __ldcs(vhi + p), hl = __ldcs(vlo + p);
       float xh[8], xl[8];
@@ -477,6 +523,73 @@ std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return out;
+}
+
+// ---- gather-rate probe ---------------------------------------------------
+// Random 32-byte gathers (one sector per lane, four in flight per lane) from a
+// table of `rows` 32-byte rows; `share` consecutive lanes read consecutive rows
+// (share = 4 puts four lanes in one 128-byte line).  Measures the ceiling of
+// the SpMM's dominant traffic on this device.
+__global__ void k_gather_probe(const uint32_t* __restrict__ idx, uint64_t nidx, const float* __restrict__ x,
+                               float* __restrict__ out) {
+  float acc = 0.f;
+  const uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x, stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = t; i < nidx; i += stride * 4) {
+    uint32_t c[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) c[u] = (i + u * stride < nidx) ? __ldg(idx + i + u * stride) : 0u;
+    float v[4][8];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ld8(x + 8ull * c[u], v[u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc += v[u][j];
+  }
+  if (acc == 1234.5f) out[0] = acc;  // keeps the loads live
+}
+
+__global__ void k_probe_index(uint32_t* __restrict__ idx, uint64_t n, uint64_t rows, int share, uint64_t seed) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  uint64_t g = i / share;
+  uint64_t z = (g + seed) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  uint64_t base = z % (rows / share);
+  idx[i] = uint32_t(base * share + i % share);
+}
+
+double gather_probe(int device, uint64_t rows, int share) {
+  if (share < 1 || rows < uint64_t(share)) throw Error(CG_ERR_ARG, "bad probe shape");
+  CG_CUDA(cudaSetDevice(device));
+  cudaStream_t s;
+  CG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const uint64_t n = 1ull << 26;
+  DBuf<uint32_t> idx(n);
+  DBuf<float> x(rows * 8), out(1);
+  CG_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), s));
+  k_probe_index<<<unsigned((n + 255) / 256), 256, 0, s>>>(idx.p, n, rows, share, 12345);
+  CG_CUDA(cudaGetLastError());
+  int nsm = 0;
+  CG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  cudaEvent_t e0, e1;
+  CG_CUDA(cudaEventCreate(&e0));
+  CG_CUDA(cudaEventCreate(&e1));
+  k_gather_probe<<<nsm * 8, 256, 0, s>>>(idx.p, n, x.p, out.p);
+  CG_CUDA(cudaEventRecord(e0, s));
+  const int reps = 3;
+  for (int r = 0; r < reps; ++r) k_gather_probe<<<nsm * 8, 256, 0, s>>>(idx.p, n, x.p, out.p);
+  CG_CUDA(cudaEventRecord(e1, s));
+  CG_CUDA(cudaEventSynchronize(e1));
+  CG_CUDA(cudaGetLastError());
+  float ms = 0;
+  CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  return double(n) * reps / (ms * 1e-3);
 }
 
 void spmm_refine_df(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m, float* stage,

@@ -176,6 +176,10 @@ cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, vo
  * (arrays of capacity *n_candidates on entry, count on return). */
 cg_status cg_spmm_autotune(cg_hamiltonian* h, int32_t nvec, int32_t reps, int32_t* n_candidates, int32_t* warps,
                            int32_t* ctas_per_sm, float* ms);
+/* Calibration: random 32-byte gathers per second on the current device from a
+ * table of `rows` 32-byte rows (share = lanes reading consecutive rows).  The
+ * stored-H SpMM's dominant traffic is one such gather per stored entry. */
+cg_status cg_gather_ceiling(uint64_t rows, int32_t share, double* gathers_per_second);
 /* Set (e.g. from a cached tuning) or read the launch shape of the FP32 product. */
 cg_status cg_spmm_set_tuning(cg_hamiltonian* h, int32_t warps, int32_t ctas_per_sm);
 cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* ctas_per_sm, int32_t* tuned);
