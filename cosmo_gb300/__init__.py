@@ -26,6 +26,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libcosmo_gb300.so")
 
 CG_OK = 0
+CG_ERR_ARG = -1
 CG_PREC_FP64, CG_PREC_FP32, CG_PREC_REFINE = 0, 1, 2
 STATUS_NAMES = {0: "CG_OK", -1: "CG_ERR_ARG", -2: "CG_ERR_IO", -3: "CG_ERR_PARSE", -4: "CG_ERR_CUDA",
                 -5: "CG_ERR_NOMEM", -6: "CG_ERR_UNSUPPORTED", -7: "CG_ERR_NOT_CONVERGED",
@@ -101,6 +102,8 @@ _SIGS = {
     "cg_spmm_device": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32]),
     "cg_spmm_autotune": (C.c_int32, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _P, _P, _P]),
     "cg_spmm_set_tuning": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "cg_spmm_refine_static": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32]),
+    "cg_spmm_refine_static_max_rows": (C.c_int32, [C.POINTER(C.c_uint64)]),
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),

@@ -394,6 +394,24 @@ cg_status cg_spmm_autotune(cg_hamiltonian* h, int32_t nvec, int32_t reps, int32_
   });
 }
 
+cg_status cg_spmm_refine_static(const cg_hamiltonian* h, const double* x, int32_t ldx, double* y, int32_t ldy,
+                                int32_t m) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(x);
+    CG_NOT_NULL(y);
+    same_device(h->h.device);
+    cg::spmm_refine_static(h->h, x, ldx, y, ldy, m, h->h.stream);
+  });
+}
+
+cg_status cg_spmm_refine_static_max_rows(uint64_t* rows) {
+  return guard([&] {
+    CG_NOT_NULL(rows);
+    *rows = cg::spmm_refine_static_max_rows();
+  });
+}
+
 cg_status cg_gather_ceiling(uint64_t rows, int32_t share, double* gathers_per_second) {
   return guard([&] {
     CG_NOT_NULL(gathers_per_second);

@@ -156,6 +156,11 @@ void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, vo
 // first m outputs of each row are stored.
 void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m, cudaStream_t s);
 std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps);
+// Double-float product with its staging area in a static device array (no
+// allocation); h.n must not exceed spmm_refine_static_max_rows().
+void spmm_refine_static(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m,
+                        cudaStream_t s);
+uint64_t spmm_refine_static_max_rows();
 // Random 32-byte gathers per second from a table of `rows` 32-byte rows.
 double gather_probe(int device, uint64_t rows, int share);
 // Refinement product Y = H X (FP64 in and out, any m) computed in double-float

@@ -19,6 +19,8 @@
 //   CG_PREC_REFINE FP32 hi + FP32 lo values (h = hi + lo to ~2^-48), FP64
 //                  vectors and accumulation.
 #include <algorithm>
+#include <mutex>
+#include <string>
 #include <type_traits>
 
 #include "device.h"
@@ -615,6 +617,57 @@ void spmm_refine_df(const Hamiltonian& h, const double* x, int ldx, double* y, i
     CG_CUDA(cudaGetLastError());
     count_launch();
   }
+}
+
+// ---- allocation-free refinement product ------------------------------------
+// The double-float product stages each block of 8 columns of x as 16 floats per
+// row (8 high parts, then 8 low parts).  spmm_refine_static keeps that staging
+// area in the fixed device array below instead of a per-call allocation, for
+// callers that cannot allocate device memory: a host eigensolver that drives
+// the product while the stored matrix and its vector basis hold the device's
+// memory, or a caller that must not stall other streams (cudaMalloc/cudaFree
+// can synchronize the whole device).  The array is one per device and shared
+// by every call; k_stage_df writes every element it later reads, so nothing in
+// it has to start at zero.
+constexpr uint64_t kStaticStageBytes = uint64_t(8) << 20;  // 8 MiB
+constexpr uint64_t kStaticStageRows = kStaticStageBytes / (16 * sizeof(float));  // 131,072 rows
+constexpr int kStaticMaxDevices = 64;
+static __device__ __align__(256) float g_static_stage[kStaticStageBytes / sizeof(float)];
+
+namespace {
+// Address of g_static_stage on `device`, looked up once per device (the first
+// call on a device does this set-up; make it before any stream capture
+// begins).  The caller has made `device` current.
+float* static_stage(int device) {
+  static std::mutex mu;
+  static float* addr[kStaticMaxDevices] = {};
+  if (device < 0 || device >= kStaticMaxDevices) throw Error(CG_ERR_ARG, "device ordinal beyond 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_stage);
+    if (e != cudaSuccess || !p)
+      throw Error(CG_ERR_CUDA, std::string("cudaGetSymbolAddress(static staging area): ") + cudaGetErrorString(e));
+    addr[device] = static_cast<float*>(p);
+  }
+  return addr[device];
+}
+}  // namespace
+
+uint64_t spmm_refine_static_max_rows() { return kStaticStageRows; }
+
+void spmm_refine_static(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m,
+                        cudaStream_t s) {
+  if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "refinement product needs an FP32 (hi+lo) matrix");
+  if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "the allocation-free product takes 1..16 vectors per call");
+  if (ldx < m || ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
+  if (reinterpret_cast<uintptr_t>(x) % 8 || reinterpret_cast<uintptr_t>(y) % 8)
+    throw Error(CG_ERR_ARG, "x and y must be 8-byte aligned FP64 buffers");
+  if (h.n > kStaticStageRows)
+    throw Error(CG_ERR_ARG, "allocation-free product: " + std::to_string(h.n) +
+                                " rows exceed its static staging area of " + std::to_string(kStaticStageRows) +
+                                " rows (8 MiB); use cg_spmm_device or cg_spmm");
+  spmm_refine_df(h, x, ldx, y, ldy, m, static_stage(h.device), s);
 }
 
 void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m, cudaStream_t s) {

@@ -170,6 +170,27 @@ cg_status cg_spmm(const cg_hamiltonian* h, const double* x, double* y, int32_t m
 cg_status cg_spmm_device(const cg_hamiltonian* h, const void* x, int32_t ldx, void* y, int32_t ldy, int32_t m,
                          int32_t precision);
 
+/* Allocation-free FP64 product, no counterpart in the reference: y = H x for
+ * m = 1..16 vectors, x and y device FP64 buffers, row-interleaved (x[i*ldx + k]),
+ * computed by the double-float kernel of CG_PREC_REFINE from an FP32 (hi + lo)
+ * matrix, enqueued on the handle's stream (the call returns before it finishes).
+ * The kernel's staging area is a fixed 8 MiB device array inside the library
+ * instead of a device allocation, so this call allocates no memory; it serves
+ * callers that cannot allocate: a host eigensolver whose stored matrix and
+ * vector basis already hold the device's memory, or one that must not stall
+ * other streams (cudaMalloc/cudaFree can synchronize the device).
+ * Limits: n <= 131,072 rows (8 MiB / 64 bytes a row; larger matrices are
+ * rejected with CG_ERR_ARG: use cg_spmm_device or cg_spmm).  The first call on
+ * each device looks up the array's device address (set-up); make that first
+ * call before any stream capture begins.  Every call on a device shares the
+ * one array (nothing in it needs to start at zero): calls whose work can
+ * overlap on the device (other streams, other threads, other handles) race on
+ * it and give wrong results, so order them, e.g. by synchronizing the previous
+ * call's stream first. */
+cg_status cg_spmm_refine_static(const cg_hamiltonian* h, const double* x, int32_t ldx, double* y, int32_t ldy,
+                                int32_t m);
+/* Row limit of cg_spmm_refine_static (131,072). */
+cg_status cg_spmm_refine_static_max_rows(uint64_t* rows);
 /* Launch-shape autotuner of the FP32 product: times every candidate (warps per
  * CTA x CTAs per SM, each CTA on one contiguous row range) with `nvec` vectors
  * on this matrix, keeps the fastest in the handle, and reports all candidates
