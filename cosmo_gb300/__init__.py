@@ -104,6 +104,11 @@ _SIGS = {
     "cg_spmm_set_tuning": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "cg_spmm_refine_static": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32]),
     "cg_spmm_refine_static_max_rows": (C.c_int32, [C.POINTER(C.c_uint64)]),
+    "cg_hamiltonian_build_virtual": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(_P)]),
+    "cg_hamiltonian_is_virtual": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "cg_jt_expectations": (C.c_int32, [_P, _P, C.c_int32, _P, _P]),
+    "cg_jj_spin": (C.c_int32, [C.c_double, C.c_int32]),
+    "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
@@ -148,6 +153,31 @@ def gather_ceiling(rows: int, share: int = 1) -> float:
     g = C.c_double()
     _check(lib().cg_gather_ceiling(rows, share, C.byref(g)))
     return float(g.value)
+
+
+def jt_expectations(basis: "ManyBodyStates", vecs) -> tuple[np.ndarray, np.ndarray]:
+    """<J-J+> and <T-T+> of the rows of vecs (nstates x n), computed on the GPU
+    (XSHLJT, include/xsm/XSHLJT.cxx:94-126)."""
+    v = np.ascontiguousarray(np.asarray(vecs, dtype=np.float64).reshape(-1, basis.n))
+    k = v.shape[0]
+    jj = np.zeros(k)
+    tt = np.zeros(k)
+    _check(lib().cg_jt_expectations(basis._h, _ptr(v), k, _ptr(jj), _ptr(tt)))
+    return jj, tt
+
+
+def jj_spin(x: float, two_m: int) -> int:
+    """2J from <J-J+> and 2M (SM::JJSpin); -1 if not a valid spin."""
+    return int(lib().cg_jj_spin(float(x), int(two_m)))
+
+
+def xshljt(xml: str, ee: str, nstates: int = 0, out: str | None = None, system: str | None = None) -> int:
+    """Spin/isospin analysis of an .EE file into <state> nodes of the system XML
+    (XSHLJT); returns the number of states recorded."""
+    k = C.c_int32()
+    _check(lib().cg_xshljt(xml.encode(), system.encode() if system else None, ee.encode(), nstates,
+                           out.encode() if out else None, C.byref(k)))
+    return int(k.value)
 
 
 def launch_count() -> int:
@@ -250,12 +280,16 @@ class ManyBodyStates:
 
 
 class Hamiltonian:
-    """Stored H + lambda J-J+ on the GPU (both triangles, row-sliced)."""
+    """H + lambda J-J+ on the GPU: stored (both triangles, row-sliced), or with
+    ``virtual=True`` regenerated on the fly by every product (SM::PPMatrix)."""
 
-    def __init__(self, problem: Problem, basis: ManyBodyStates, precision: int = CG_PREC_FP64):
+    def __init__(self, problem: Problem, basis: ManyBodyStates, precision: int = CG_PREC_FP64,
+                 virtual: bool = False):
         h = _P()
-        _check(lib().cg_hamiltonian_build(problem._h, basis._h, precision, C.byref(h)))
+        build = lib().cg_hamiltonian_build_virtual if virtual else lib().cg_hamiltonian_build
+        _check(build(problem._h, basis._h, precision, C.byref(h)))
         self._h = h
+        self.virtual = bool(virtual)
         self.refresh_info()
 
     def refresh_info(self):

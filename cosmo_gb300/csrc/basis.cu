@@ -86,6 +86,8 @@ __global__ void k_tuples(uint64_t first, uint64_t count, int N, const uint64_t* 
   }
 }
 
+}  // namespace
+
 uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom) {
   uint64_t r = 0;
   int i = 0;
@@ -97,6 +99,8 @@ uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom) {
   }
   return r;
 }
+
+namespace {
 
 void enumerate_species(SpeciesTables& sp, int norb, int k, const int* m2, const int* par, const DBuf<uint64_t>& binom,
                        const std::vector<uint64_t>& hb, cudaStream_t s) {
@@ -190,6 +194,12 @@ void basis_build(const System& sys, Basis& b) {
     off += cnt;
   }
   b.n = off;
+  cstart.push_back(uint32_t(cmasks.size()));
+  b.h_bstart = bstart;
+  b.h_bmask = bmask;
+  b.h_bclass = bclass;
+  b.h_cstart = cstart;
+  b.h_cmasks = cmasks;
   b.noff.upload(b.h_noff, s);
   b.pcrank.upload(b.h_pcrank, s);
   b.state.alloc(std::max<uint64_t>(b.n, 1));

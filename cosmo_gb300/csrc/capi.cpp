@@ -8,12 +8,15 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <sstream>
 #include <string>
 
 #include "cosmo_gb300.h"
 #include "davidson.h"
 #include "device.h"
 #include "model.h"
+#include "virtual.h"
+#include "xshljt.h"
 
 struct cg_problem {
   cg::System sys;
@@ -285,6 +288,30 @@ cg_status cg_hamiltonian_build(const cg_problem* p, const cg_basis* b, int32_t p
     *out = h.release();
   });
 }
+cg_status cg_hamiltonian_build_virtual(const cg_problem* p, const cg_basis* b, int32_t precision,
+                                       cg_hamiltonian** out) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    same_device(b->b.device);
+    if (p->sys.sps.size() != b->sys.sps.size() || p->sys.nv != b->sys.nv || p->sys.zv != b->sys.zv)
+      throw cg::Error(CG_ERR_ARG, "basis was built for another problem");
+    auto h = std::make_unique<cg_hamiltonian>();
+    cg::virtual_build(p->sys, p->op, b->b, precision, h->h);
+    *out = h.release();
+  });
+}
+
+cg_status cg_hamiltonian_is_virtual(const cg_hamiltonian* h, int32_t* is_virtual) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(is_virtual);
+    *is_virtual = h->h.virt ? 1 : 0;
+  });
+}
+
 void cg_hamiltonian_destroy(cg_hamiltonian* h) { delete h; }
 
 cg_status cg_hamiltonian_get_info(const cg_hamiltonian* h, cg_hamiltonian_info* info) {
@@ -316,6 +343,7 @@ cg_status cg_hamiltonian_upper_rows(const cg_hamiltonian* h, uint64_t row0, uint
     CG_NOT_NULL(h);
     CG_NOT_NULL(rowptr);
     same_device(h->h.device);
+    if (h->h.virt) throw cg::Error(CG_ERR_UNSUPPORTED, "an on-the-fly Hamiltonian stores no rows");
     cg::hamiltonian_upper_rows(h->h, row0, nrows, rowptr, cols, vals);
   });
 }
@@ -325,6 +353,7 @@ cg_status cg_hamiltonian_write_hh(const cg_hamiltonian* h, const char* path) {
     CG_NOT_NULL(h);
     CG_NOT_NULL(path);
     same_device(h->h.device);
+    if (h->h.virt) throw cg::Error(CG_ERR_UNSUPPORTED, "an on-the-fly Hamiltonian stores no rows");
     std::ofstream f(path, std::ios::binary);
     if (!f) throw cg::Error(CG_ERR_IO, std::string("cannot write ") + path);
     uint64_t n = h->h.n;
@@ -412,6 +441,44 @@ cg_status cg_spmm_refine_static_max_rows(uint64_t* rows) {
   });
 }
 
+cg_status cg_jt_expectations(const cg_basis* b, const double* vecs, int32_t nstates, double* jj, double* tt) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(vecs);
+    CG_NOT_NULL(jj);
+    CG_NOT_NULL(tt);
+    same_device(b->b.device);
+    cg::jt_expectations(b->sys, b->b, vecs, nstates, jj, tt);
+  });
+}
+
+int32_t cg_jj_spin(double jj, int32_t two_m) { return cg::jj_spin(jj, two_m); }
+
+cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* ee_path, int32_t nstates,
+                    const char* xml_out, int32_t* n_added) {
+  return guard([&] {
+    CG_NOT_NULL(xml_path);
+    CG_NOT_NULL(ee_path);
+    require_device();
+    const std::string sname = system_name ? system_name : "";
+    cg::System sys = cg::load_system(xml_path, sname);
+    cg::Basis b;
+    cg::basis_build(sys, b);
+    std::string file_attr = ee_path;
+    auto states = cg::xshljt_states(sys, b, ee_path, nstates, file_attr, nullptr, nullptr);
+    std::ifstream in(xml_path, std::ios::binary);
+    if (!in) throw cg::Error(CG_ERR_IO, std::string("cannot open ") + xml_path);
+    std::stringstream ss;
+    ss << in.rdbuf();
+    std::string text = cg::xml_add_states(ss.str(), sys.name, states);
+    const char* dst = xml_out ? xml_out : xml_path;
+    std::ofstream out(dst, std::ios::binary);
+    if (!out) throw cg::Error(CG_ERR_IO, std::string("cannot write ") + dst);
+    out << text;
+    if (n_added) *n_added = int32_t(states.size());
+  });
+}
+
 cg_status cg_gather_ceiling(uint64_t rows, int32_t share, double* gathers_per_second) {
   return guard([&] {
     CG_NOT_NULL(gathers_per_second);
@@ -479,7 +546,7 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     if (n_init < 0 || (n_init > 0 && !init)) throw cg::Error(CG_ERR_ARG, "bad initial vectors");
     if (prm->precision != CG_PREC_FP64 && prm->precision != CG_PREC_FP32)
       throw cg::Error(CG_ERR_ARG, "precision must be CG_PREC_FP64 or CG_PREC_FP32");
-    if (prm->precision != h->h.precision)
+    if (prm->precision != h->h.precision && !h->h.virt)
       throw cg::Error(CG_ERR_ARG, "Davidson precision must match the stored Hamiltonian precision");
     const double final_tol = prm->tol_resid > 0 ? prm->tol_resid : prm->critr;
     cg::DavConfig c;
@@ -520,7 +587,7 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
       rq.phase2 = c2;
       rq.refine = true;
     }
-    if (prm->precision == CG_PREC_FP32 && !h->h.tuning.tuned)
+    if (prm->precision == CG_PREC_FP32 && !h->h.tuning.tuned && !h->h.virt)
       cg::spmm_autotune(const_cast<cg_hamiltonian*>(h)->h, std::min(prm->block, 16), 3);
     cg::DavResult r = cg::davidson_solve(h->h, rq);
     const cg::DavOutcome& f = r.final_;

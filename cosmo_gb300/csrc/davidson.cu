@@ -26,6 +26,7 @@
 #include <numeric>
 
 #include "davidson.h"
+#include "virtual.h"
 #include "dense.h"
 #include "device.h"
 
@@ -567,7 +568,24 @@ struct Engine {
   DBuf<float> stage;  // FP32 engine: aligned SpMM input block (n x 16)
   void spmm(int c0, int m) {
     CG_CUDA(cudaEventRecord(ev0, s));
-    if constexpr (sizeof(T) == 4) {
+    if (H.virt) {
+      // on-the-fly product: pack 8 (FP32) or 4 (FP64) columns at a time
+      if (!stage.p) stage.alloc(n * 16);
+      if constexpr (sizeof(T) == 4) {
+        for (int c = 0; c < m; c += kVirtualVB32) {
+          const int mc = std::min(kVirtualVB32, m - c);
+          virtual_pack_f32(n, reinterpret_cast<const float*>(B.p), L, c0 + c, mc, stage.p, s);
+          virtual_product_f32(H, stage.p, reinterpret_cast<float*>(AB.p) + c0 + c, L, mc, s);
+        }
+      } else {
+        double* w = reinterpret_cast<double*>(stage.p);
+        for (int c = 0; c < m; c += kVirtualVB64) {
+          const int mc = std::min(kVirtualVB64, m - c);
+          virtual_pack_f64(n, reinterpret_cast<const double*>(B.p), L, c0 + c, mc, w, s);
+          virtual_product_f64(H, w, reinterpret_cast<double*>(AB.p) + c0 + c, L, mc, s);
+        }
+      }
+    } else if constexpr (sizeof(T) == 4) {
       if (cfg.spmm_prec == CG_PREC_FP32) {
         if (!stage.p) stage.alloc(n * 16);
         int pad = m <= 8 ? 8 : 16;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,12 @@ struct Basis {
   DBuf<uint64_t> noff;             // by neutron colex rank: first index of that neutron block, ~0 if none
   DBuf<uint32_t> pcrank;           // by proton colex rank: rank inside its (2m, parity) class
   DBuf<uint64_t> binom;            // kBinom x kBinom
+  // neutron blocks (basis order) and proton classes, host copies
+  std::vector<uint64_t> h_bstart;  // first index of each neutron block
+  std::vector<uint32_t> h_bmask;   // neutron mask of each block
+  std::vector<uint32_t> h_bclass;  // proton class of each block
+  std::vector<uint32_t> h_cstart;  // first position of each proton class in h_cmasks
+  std::vector<uint32_t> h_cmasks;  // proton masks, class by class, rank order
   // host copies used for locate and .mbs output
   std::vector<uint64_t> h_noff;
   std::vector<uint32_t> h_pcrank;
@@ -97,6 +104,12 @@ struct Basis {
 };
 
 void basis_build(const System& sys, Basis& b);
+uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom);
+
+// <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nst host vectors (state k at vecs + k*n).
+void jt_expectations(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt);
+// twice the spin from <J-J+> and twice the projection; -1 if not (half-)integer within 0.1
+int jj_spin(double x, int two_m);
 void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);
 uint64_t basis_locate_host(const Basis& b, const uint16_t* tuple);
 
@@ -124,6 +137,7 @@ struct SpmmCandidate {
   float ms;
 };
 
+struct VirtualOp;
 struct Hamiltonian {
   int device = 0;
   int precision = CG_PREC_FP64;
@@ -136,11 +150,10 @@ struct Hamiltonian {
   DBuf<float> hi, lo;     // nnz (CG_PREC_FP32)
   DBuf<double> diag;      // n
   SpmmTuning tuning;
+  std::shared_ptr<VirtualOp> virt;  // set for the on-the-fly product (nothing stored)
   cudaStream_t stream = nullptr;
   ~Hamiltonian();
-  uint64_t device_bytes() const {
-    return rowptr.bytes() + col.bytes() + val64.bytes() + hi.bytes() + lo.bytes() + diag.bytes();
-  }
+  uint64_t device_bytes() const;  // HBM held by the matrix (or the on-the-fly tables)
 };
 
 void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h);

@@ -165,7 +165,6 @@ XmlNode parse_xml_file(const std::string& path) {
 }
 
 // ------------------------------------------------------------ numbers
-namespace {
 // Doubled spin from text: "5/2" -> 5, "3" -> 6, "1.5" -> 3, as the reference
 // `spin(const char*)` constructor (include/sm/spinclass.cxx:57-79).
 int parse_spin2(const std::string& t) {
@@ -179,6 +178,7 @@ int parse_spin2(const std::string& t) {
   if (std::fabs(r - 2.0 * x) > 0.01) throw Error(CG_ERR_PARSE, "spin " + t + " is not (half-)integer");
   return r;
 }
+namespace {
 int attr_int(const XmlNode& n, const char* k, int dflt, bool required = false) {
   const std::string* v = n.attr(k);
   if (!v) {
@@ -271,6 +271,8 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   }
   if (sys.nv + sys.zv != A) throw Error(CG_ERR_PARSE, "Nv + Zv != Av");
   sys.twom = sn->attr("Jz") ? parse_spin2(*sn->attr("Jz")) : (A % 2);
+  if (const std::string* fj = sn->attr("J")) sys.filter_twoJ = parse_spin2(*fj);
+  if (const std::string* ft = sn->attr("T")) sys.filter_twoT = parse_spin2(*ft);
   if (!sn->attr("P")) throw Error(CG_ERR_PARSE, "system needs P");
   sys.parity = ((*sn->attr("P"))[0] == '-') ? 1 : 0;
   if (const XmlNode* mb = sn->child("ManyBodyStates"))

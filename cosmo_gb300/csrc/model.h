@@ -30,6 +30,8 @@ struct XmlNode {
   int count(const std::string& t) const;
 };
 XmlNode parse_xml_file(const std::string& path);
+// doubled spin from its text form ("5/2" -> 5, "3" -> 6)
+int parse_spin2(const std::string& t);
 
 // ---------------------------------------------------------- s.p. states
 // One m-scheme single-particle state.  Quantum numbers are stored doubled
@@ -64,6 +66,8 @@ struct System {
   std::vector<std::string> int_files;
   std::vector<std::array<double, 10>> int_scale;  // per file, rank-indexed scaling
   std::string mbs_name;          // ManyBodyStates name attribute (may be empty)
+  int filter_twoJ = -1;          // system J / T attributes: XSHLJT keeps only these states
+  int filter_twoT = -1;
   std::string xml_dir;
 };
 

@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "device.h"
+#include "virtual.h"
 
 namespace cg {
 namespace {
@@ -487,6 +488,7 @@ void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, 
 // matrix (CUDA events on the handle's stream, median of `reps`) and keep the
 // fastest in h.tuning.  Returns the per-candidate times.
 std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
+  if (h.virt) throw Error(CG_ERR_UNSUPPORTED, "launch-shape tuning applies to stored matrices");
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "autotuning applies to FP32 matrices");
   const int ld = m <= 8 ? 8 : 16;
   cudaStream_t s = h.stream;
@@ -596,6 +598,7 @@ double gather_probe(int device, uint64_t rows, int share) {
 
 void spmm_refine_df(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m, float* stage,
                     cudaStream_t s) {
+  if (h.virt) return virtual_launch(h, CG_PREC_REFINE, x, ldx, y, ldy, m, s);
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "refinement product needs an FP32 (hi+lo) matrix");
   for (int c0 = 0; c0 < m; c0 += 8) {
     const int mc = std::min(8, m - c0);
@@ -658,6 +661,7 @@ uint64_t spmm_refine_static_max_rows() { return kStaticStageRows; }
 
 void spmm_refine_static(const Hamiltonian& h, const double* x, int ldx, double* y, int ldy, int m,
                         cudaStream_t s) {
+  if (h.virt) throw Error(CG_ERR_ARG, "the allocation-free product needs a stored FP32 (hi+lo) matrix");
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "refinement product needs an FP32 (hi+lo) matrix");
   if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "the allocation-free product takes 1..16 vectors per call");
   if (ldx < m || ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
@@ -671,6 +675,7 @@ void spmm_refine_static(const Hamiltonian& h, const double* x, int ldx, double* 
 }
 
 void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, int ldy, int m, cudaStream_t s) {
+  if (h.virt) return virtual_launch(h, CG_PREC_FP32, x, ldx, y, ldy, m, s);
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "FP32 product needs an FP32 matrix");
   if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "padded FP32 SpMM takes 1..16 vectors");
   if (reinterpret_cast<uintptr_t>(x) % 32 || ldx % 8) throw Error(CG_ERR_ARG, "padded FP32 SpMM needs 32-byte rows");
@@ -686,6 +691,7 @@ void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, in
 void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, void* y, int ldy, int m,
                  cudaStream_t s) {
   if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "SpMM supports 1..16 vectors per call");
+  if (h.virt) return virtual_launch(h, precision, x, ldx, y, ldy, m, s);
   if (ldx < m || ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
   switch (precision) {
     case CG_PREC_FP64:

@@ -1,0 +1,868 @@
+// On-the-fly H + lambda * J-J+ product (the element kinds and their tables are
+// described in virtual.h).
+//
+// Host: transition tables of every neutron block and proton configuration,
+// built from the same forward-ordered operator terms and the same fermion
+// phase rule as the stored builder (SM::ActFermiOperator,
+// include/sm/cioperators.cxx:36-62; SM::Annihilation / SM::Creation,
+// include/sm/operators.cxx:121-187).
+//
+// Device: one CTA per neutron block beta (rows start(beta) .. + L), each thread
+// owning up to RPT rows and VB vectors of each row in registers.  The own
+// block's terms (diagonal, PP2, P1) read x through L1 (the block is reused by
+// every row of the CTA); NN2 reads x[nu', pi] for consecutive pi, coalesced
+// across the CTA; for every neutron one-body transition beta -> beta' the
+// whole block x[beta'] (contiguous, L' rows) is brought into shared memory by
+// one bulk TMA copy (cp.async.bulk, completion on an mbarrier, two buffers so
+// the next block streams in while this one is used) together with the
+// W[a][c][.][.] slice, and each row walks its proton transitions of the
+// balancing 2m change, gathering from shared memory.
+#include <algorithm>
+#include <chrono>
+#include <map>
+#include <numeric>
+
+#include "virtual.h"
+
+namespace cg {
+
+namespace {
+
+constexpr double kDropV = 1e-14;
+constexpr int kVirtualSmemHead = 128;  // three mbarriers; keeps the staging buffers 128-byte aligned
+
+inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+inline uint64_t below_h(int b) { return b >= 64 ? ~0ull : (1ull << b) - 1ull; }
+
+struct HostOp {
+  int ns = 0, np_pairs = 0;
+  std::vector<double> e1;      // ns x ns
+  std::vector<double> v2;      // npairs x npairs
+  std::vector<int32_t> pidx;   // ns x ns
+  double V(int a, int b, int c, int d) const {  // a < b, c < d
+    return v2[size_t(pidx[a * ns + b]) * np_pairs + pidx[c * ns + d]];
+  }
+  // forward two-body term (b0 < b1 annihilated, b2 < b3 created) on S0
+  double term2(uint64_t S0, int b0, int b1, int b2, int b3) const {
+    double v = V(b0, b1, b2, b3);
+    int p = popc(S0 & below_h(b0)) + popc(S0 & below_h(b1)) - 1;
+    uint64_t I = S0 & ~((1ull << b0) | (1ull << b1));
+    p += popc(I & below_h(b2)) + popc(I & below_h(b3));
+    return (p & 1) ? -v : v;
+  }
+  double term1(uint64_t S0, int x, int y) const {
+    double v = e1[x * ns + y];
+    int p = popc(S0 & below_h(x)) + popc((S0 & ~(1ull << x)) & below_h(y));
+    return (p & 1) ? -v : v;
+  }
+};
+
+HostOp host_operator(const System& sys, const Operator& op) {
+  HostOp h;
+  const int ns = int(sys.sps.size());
+  h.ns = ns;
+  h.pidx.assign(ns * ns, -1);
+  int np = 0;
+  for (int a = 0; a < ns; ++a)
+    for (int b = a + 1; b < ns; ++b) h.pidx[a * ns + b] = np++;
+  h.np_pairs = np;
+  h.e1.assign(ns * ns, 0.0);
+  for (auto& kv : op.one) h.e1[kv.first[0] * ns + kv.first[1]] = kv.second;
+  h.v2.assign(size_t(std::max(np, 1)) * std::max(np, 1), 0.0);
+  for (auto& kv : op.two) {
+    const Key4& k = kv.first;
+    if (k[0] >= k[1] || k[2] >= k[3]) continue;  // cannot act on a determinant
+    h.v2[size_t(h.pidx[k[0] * ns + k[1]]) * np + h.pidx[k[2] * ns + k[3]]] = kv.second;
+  }
+  return h;
+}
+
+// one-body move x -> y inside a species mask: phase parity of the other
+// occupied orbitals strictly between (the same from either end)
+inline int move_sign(uint64_t mask, int from, int to) {
+  uint64_t o = mask & ~(1ull << from);
+  return (popc(o & below_h(from)) + popc(o & below_h(to))) & 1;
+}
+
+// ------------------------------------------------------------------ device
+struct VArgs {
+  int nn, np, ndm, dm0, lmax;
+  const uint64_t* bstart;
+  const uint32_t *blen, *bclass, *bmask, *order;
+  const uint32_t *cstart, *cmask;
+  const uint32_t* nt_off;
+  const NTrans* nt;
+  const uint32_t* nn_off;
+  const VPair* nn2;
+  const uint32_t* cslice;  // first 32-row slice of each proton class
+  const uint32_t* sl_off;  // per (slice, slot): first proton-transition entry (32 lanes x count)
+  const uint32_t* sl_e;    // rank | (b * np + d) << 16 | sign << 27
+  const uint32_t* pp_off;  // per slice: first PP2 entry (32 lanes x count)
+  const uint32_t* pp_rank;
+  const double* diag;
+};
+
+template <class T>
+struct VTab {
+  const T *W, *Un, *Up;
+  const T* sl_c;  // P1 value without neutron spectators, parallel to sl_e
+  const T* pp_h;  // PP2 values, parallel to pp_rank
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// one elected thread: arm the barrier with the byte count and start the copy
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// bounded wait for the barrier phase with the given parity; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <class T, int VB>
+struct Row;
+template <>
+struct Row<float, 8> {
+  float v[8];
+  __device__ __forceinline__ void load_g(const float* p) {
+    float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  }
+  __device__ __forceinline__ void load_s(const float* p) {
+    float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  }
+};
+template <>
+struct Row<double, 4> {
+  double v[4];
+  __device__ __forceinline__ void load_g(const double* p) {
+    double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+  __device__ __forceinline__ void load_s(const double* p) {
+    double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+
+template <class T, int VB, int RPT>
+__global__ void __launch_bounds__(512) k_virtual(VArgs a, VTab<T> tb, const T* __restrict__ x, T* __restrict__ y,
+                                                 int ldy, int m, int* __restrict__ err) {
+  // shared memory: [3 mbarriers | pad to 128 B] own buf0 buf1 (lmax x VB each)
+  //                wsl0 wsl1 (np*np + 1, last = 0) un0 un1 (32) Pp (np*np + 1, last = 0)
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int npp = a.np * a.np, nw = npp + 4;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
+  T* own = reinterpret_cast<T*>(smem_raw + kVirtualSmemHead);
+  T* buf0 = own + size_t(a.lmax) * VB;
+  T* buf1 = buf0 + size_t(a.lmax) * VB;
+  T* wsl0 = buf1 + size_t(a.lmax) * VB;
+  T* wsl1 = wsl0 + nw;
+  T* un0 = wsl1 + nw;
+  T* un1 = un0 + 32;
+  T* Pp = un1 + 32;
+
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
+  const uint32_t beta = a.order[blockIdx.x];
+  const uint64_t start = a.bstart[beta];
+  const int L = int(a.blen[beta]);
+  const uint32_t cls = a.bclass[beta];
+  const uint32_t cs = a.cstart[cls], slice0 = a.cslice[cls];
+  const uint32_t nmask = a.bmask[beta];
+  const uint32_t t0 = a.nt_off[beta], t1 = a.nt_off[beta + 1];
+
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    fence_mbar_init();
+  }
+  // P1 neutron-spectator sums of this block: Pp[b*np+d] = sum_{q in nu} Up[b][d][q]
+  for (int i = tid; i <= npp; i += NT) {
+    T s = 0;
+    if (i < npp)
+      for (uint32_t w = nmask; w; w &= w - 1) s += tb.Up[size_t(i) * a.nn + (__ffs(w) - 1)];
+    Pp[i] = s;
+  }
+  if (tid == 0) {
+    wsl0[npp] = T(0);
+    wsl1[npp] = T(0);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    bulk_load(own, x + start * VB, uint32_t(L) * uint32_t(VB * sizeof(T)), &mbar[2]);
+    if (t0 < t1) {
+      const uint32_t tg = a.nt[t0].target;
+      bulk_load(buf0, x + a.bstart[tg] * VB, a.blen[tg] * uint32_t(VB * sizeof(T)), &mbar[0]);
+    }
+  }
+
+  T acc[RPT][VB];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k)
+#pragma unroll
+    for (int j = 0; j < VB; ++j) acc[k][j] = 0;
+
+  // NN2 first (global x, consecutive rows of the target block), while the own block streams in
+  for (uint32_t e = a.nn_off[beta], e1 = a.nn_off[beta + 1]; e < e1; ++e) {
+    const VPair q = a.nn2[e];
+    const uint64_t ts = a.bstart[q.target];
+    const T h = T(q.h);
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int r = tid + k * NT;
+      if (r < L) {
+        Row<T, VB> xr;
+        xr.load_g(x + (ts + r) * VB);
+#pragma unroll
+        for (int j = 0; j < VB; ++j) acc[k][j] += h * xr.v[j];
+      }
+    }
+  }
+  {
+    const bool ok = mbar_wait(&mbar[2], 0);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(err, 1);
+        mbar_wait(&mbar[2], 0);
+        if (t0 < t1) mbar_wait(&mbar[0], 0);
+      }
+      __syncthreads();
+      return;
+    }
+  }
+  // diagonal, PP2 and P1 from the own block.  Rows come in 32-row slices
+  // (warp-uniform), whose transition lists are stored lane-interleaved.
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int rb = (tid & ~31) + k * NT;  // first row of this warp's slice
+    if (rb < L) {
+      const int r = rb + lane;
+      const uint32_t sl = slice0 + uint32_t(rb >> 5);
+      Row<T, VB> xr;
+      if (r < L) {
+        xr.load_s(own + size_t(r) * VB);
+        const T d = T(a.diag[start + r]);
+#pragma unroll
+        for (int j = 0; j < VB; ++j) acc[k][j] += d * xr.v[j];
+      }
+      for (uint32_t e = a.pp_off[sl] + lane, e1 = a.pp_off[sl + 1]; e < e1; e += 32) {
+        const T h = tb.pp_h[e];
+        xr.load_s(own + size_t(a.pp_rank[e]) * VB);
+#pragma unroll
+        for (int j = 0; j < VB; ++j) acc[k][j] += h * xr.v[j];
+      }
+      const size_t o = size_t(sl) * a.ndm + a.dm0;
+      for (uint32_t e = a.sl_off[o] + lane, e1 = a.sl_off[o + 1]; e < e1; e += 32) {
+        const uint32_t q = a.sl_e[e];
+        T v = Pp[(q >> 16) & 0x7ff];
+        v = tb.sl_c[e] + (((q >> 27) & 1) ? -v : v);
+        xr.load_s(own + size_t(q & 0xffff) * VB);
+#pragma unroll
+        for (int j = 0; j < VB; ++j) acc[k][j] += v * xr.v[j];
+      }
+    }
+  }
+  // neutron one-body transitions: N1 (same 2m) and NP
+  uint32_t u = 0;
+  for (uint32_t t = t0; t < t1; ++t, ++u) {
+    const int jb = u & 1;
+    const NTrans tr = a.nt[t];
+    T* wsl = jb ? wsl1 : wsl0;
+    T* un = jb ? un1 : un0;
+    const T* Wrow = tb.W + (size_t(tr.a) * a.nn + tr.c) * npp;
+    for (int i = tid; i < npp; i += NT) wsl[i] = tr.sign ? -Wrow[i] : Wrow[i];
+    const bool same_m = tr.dmi == a.dm0;
+    if (same_m && tid < a.np) {
+      const T w = tb.Un[(size_t(tr.a) * a.nn + tr.c) * a.np + tid];
+      un[tid] = tr.sign ? -w : w;
+    }
+    __syncthreads();
+    if (tid == 0 && t + 1 < t1) {
+      const uint32_t tg = a.nt[t + 1].target;
+      bulk_load(jb ? buf0 : buf1, x + a.bstart[tg] * VB, a.blen[tg] * uint32_t(VB * sizeof(T)), &mbar[jb ^ 1]);
+    }
+    const bool ok = mbar_wait(&mbar[jb], (u >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      // give the copies in flight a second bounded wait, report, leave
+      if (tid == 0) {
+        atomicOr(err, 1);
+        mbar_wait(&mbar[jb], (u >> 1) & 1);
+        if (t + 1 < t1) mbar_wait(&mbar[jb ^ 1], ((u + 1) >> 1) & 1);
+      }
+      __syncthreads();
+      return;
+    }
+    const T* bf = jb ? buf1 : buf0;
+    const int dmp = a.ndm - 2 - (tr.dmi & ~1) + (tr.dmi & 1);  // opposite 2m change, same parity change
+    const T cn = T(tr.cn);
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int rb = (tid & ~31) + k * NT;
+      if (rb < L) {
+        const int r = rb + lane;
+        const uint32_t sl = slice0 + uint32_t(rb >> 5);
+        const size_t o = size_t(sl) * a.ndm + dmp;
+        for (uint32_t e = a.sl_off[o] + lane, e1 = a.sl_off[o + 1]; e < e1; e += 32) {
+          const uint32_t q = a.sl_e[e];
+          T w = wsl[(q >> 16) & 0x7ff];
+          w = ((q >> 27) & 1) ? -w : w;
+          Row<T, VB> xr;
+          xr.load_s(bf + size_t(q & 0xffff) * VB);
+#pragma unroll
+          for (int j = 0; j < VB; ++j) acc[k][j] += w * xr.v[j];
+        }
+        if (same_m && r < L) {
+          T v = cn;
+          for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v += un[__ffs(w) - 1];
+          Row<T, VB> xr;
+          xr.load_s(bf + size_t(r) * VB);
+#pragma unroll
+          for (int j = 0; j < VB; ++j) acc[k][j] += v * xr.v[j];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int r = tid + k * NT;
+    if (r < L) {
+      T* yr = y + (start + r) * size_t(ldy);
+#pragma unroll
+      for (int j = 0; j < VB; ++j)
+        if (j < m) yr[j] = acc[k][j];
+    }
+  }
+}
+
+// diagonal of every row: En(block) + Ep(proton configuration) + pn part
+__global__ void k_virtual_diag(uint64_t n, int nblocks, const uint64_t* __restrict__ bstart,
+                               const uint32_t* __restrict__ bclass, const uint32_t* __restrict__ bmask,
+                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ cmask,
+                               const double* __restrict__ En, const double* __restrict__ Ep,
+                               const double* __restrict__ Vd, int np, double* __restrict__ diag) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  int lo = 0, hi = nblocks - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (bstart[mid] <= i) lo = mid; else hi = mid - 1;
+  }
+  const uint32_t g = cstart[bclass[lo]] + uint32_t(i - bstart[lo]);
+  double d = En[lo] + Ep[g];
+  const uint32_t pm = cmask[g];
+  for (uint32_t w = bmask[lo]; w; w &= w - 1) {
+    const int an = __ffs(w) - 1;
+    for (uint32_t z = pm; z; z &= z - 1) d += Vd[an * np + (__ffs(z) - 1)];
+  }
+  diag[i] = d;
+}
+
+template <class T, int VB, int RPT>
+void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const T* x, T* y, int ldy, int m,
+                int threads, size_t smem, int* err, cudaStream_t s) {
+  auto kern = k_virtual<T, VB, RPT>;
+  CG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  kern<<<unsigned(a.lmax ? h.virt->nblocks : 0), threads, smem, s>>>(a, tb, x, y, ldy, m, err);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+VArgs make_args(const VirtualOp& v, const Hamiltonian& h) {
+  VArgs a;
+  a.nn = v.nn; a.np = v.np; a.ndm = v.ndm; a.dm0 = v.dm0; a.lmax = v.lmax;
+  a.bstart = v.bstart.p; a.blen = v.blen.p; a.bclass = v.bclass.p; a.bmask = v.bmask.p; a.order = v.order.p;
+  a.cstart = v.cstart.p; a.cmask = v.cmask.p;
+  a.nt_off = v.nt_off.p; a.nt = v.nt.p; a.nn_off = v.nn_off.p; a.nn2 = v.nn2.p;
+  a.cslice = v.cslice.p; a.sl_off = v.sl_off.p; a.sl_e = v.sl_e.p; a.pp_off = v.pp_off.p; a.pp_rank = v.pp_rank.p;
+  a.diag = h.diag.p;
+  return a;
+}
+
+template <class T, int VB>
+void virtual_product(const Hamiltonian& h, const T* x, T* y, int ldy, int m, const VTab<T>& tb, cudaStream_t s) {
+  if (!h.virt) throw Error(CG_ERR_INTERNAL, "not an on-the-fly Hamiltonian");
+  const VirtualOp& v = *h.virt;
+  if (m < 1 || m > VB) throw Error(CG_ERR_ARG, "on-the-fly product: too many vectors for one pass");
+  if (ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
+  if (reinterpret_cast<uintptr_t>(x) % 16) throw Error(CG_ERR_ARG, "on-the-fly product needs 16-byte aligned x");
+  if (v.nblocks == 0) return;
+  VArgs a = make_args(v, h);
+  const int npp = v.np * v.np;
+  const size_t smem = kVirtualSmemHead + (size_t(3) * v.lmax * VB + 3 * size_t(npp + 4) + 64) * sizeof(T);
+  if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "neutron block too long for the shared-memory staging");
+  int rpt = 1;
+  while ((v.lmax + rpt - 1) / rpt > 512) rpt <<= 1;
+  int threads = (v.lmax + rpt - 1) / rpt;
+  threads = std::max(64, (threads + 31) / 32 * 32);
+  if (rpt > 8) throw Error(CG_ERR_UNSUPPORTED, "neutron block longer than 4096 rows");
+  DBuf<int>& err = v.err;
+  CG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  switch (rpt) {
+    case 1: launch_rpt<T, VB, 1>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
+    case 2: launch_rpt<T, VB, 2>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
+    case 4: launch_rpt<T, VB, 4>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
+    default: launch_rpt<T, VB, 8>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
+  }
+  int herr = 0;
+  CG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  if (herr) throw Error(CG_ERR_TIMEOUT, "on-the-fly product: a staged copy did not complete");
+}
+
+// W (n x VB packed) = columns c0 .. c0+m of x (row-interleaved, ld), zero-padded
+template <class T, int VB>
+__global__ void k_pack(uint64_t n, const T* __restrict__ x, int ld, int c0, int m, T* __restrict__ w) {
+  uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * VB) return;
+  uint64_t i = idx / VB;
+  int j = int(idx - i * VB);
+  w[idx] = j < m ? x[i * ld + c0 + j] : T(0);
+}
+
+template <class T, int VB>
+void pack(uint64_t n, const T* x, int ld, int c0, int m, T* w, cudaStream_t s) {
+  if (!n) return;
+  k_pack<T, VB><<<unsigned((n * VB + 255) / 256), 256, 0, s>>>(n, x, ld, c0, m, w);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+}  // namespace
+
+void virtual_pack_f32(uint64_t n, const float* x, int ld, int c0, int m, float* w, cudaStream_t s) {
+  pack<float, kVirtualVB32>(n, x, ld, c0, m, w, s);
+}
+void virtual_pack_f64(uint64_t n, const double* x, int ld, int c0, int m, double* w, cudaStream_t s) {
+  pack<double, kVirtualVB64>(n, x, ld, c0, m, w, s);
+}
+
+void virtual_launch(const Hamiltonian& h, int precision, const void* x, int ldx, void* y, int ldy, int m,
+                    cudaStream_t s) {
+  if (m < 1) throw Error(CG_ERR_ARG, "m must be >= 1");
+  if (ldx < m || ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
+  const uint64_t n = h.n;
+  if (precision == CG_PREC_FP32) {
+    DBuf<float> w(std::max<uint64_t>(n * kVirtualVB32, 1));
+    for (int c0 = 0; c0 < m; c0 += kVirtualVB32) {
+      const int mc = std::min(kVirtualVB32, m - c0);
+      virtual_pack_f32(n, static_cast<const float*>(x), ldx, c0, mc, w.p, s);
+      virtual_product_f32(h, w.p, static_cast<float*>(y) + c0, ldy, mc, s);
+    }
+  } else if (precision == CG_PREC_FP64 || precision == CG_PREC_REFINE) {
+    DBuf<double> w(std::max<uint64_t>(n * kVirtualVB64, 1));
+    for (int c0 = 0; c0 < m; c0 += kVirtualVB64) {
+      const int mc = std::min(kVirtualVB64, m - c0);
+      virtual_pack_f64(n, static_cast<const double*>(x), ldx, c0, mc, w.p, s);
+      virtual_product_f64(h, w.p, static_cast<double*>(y) + c0, ldy, mc, s);
+    }
+  } else {
+    throw Error(CG_ERR_ARG, "unknown precision");
+  }
+}
+
+void virtual_product_f32(const Hamiltonian& h, const float* x, float* y, int ldy, int m, cudaStream_t s) {
+  VTab<float> tb{h.virt->Wf.p, h.virt->Unf.p, h.virt->Upf.p, h.virt->sl_cf.p, h.virt->pp_hf.p};
+  virtual_product<float, kVirtualVB32>(h, x, y, ldy, m, tb, s);
+}
+
+void virtual_product_f64(const Hamiltonian& h, const double* x, double* y, int ldy, int m, cudaStream_t s) {
+  VTab<double> tb{h.virt->W.p, h.virt->Un.p, h.virt->Up.p, h.virt->sl_c.p, h.virt->pp_h.p};
+  virtual_product<double, kVirtualVB64>(h, x, y, ldy, m, tb, s);
+}
+
+uint64_t Hamiltonian::device_bytes() const {
+  return rowptr.bytes() + col.bytes() + val64.bytes() + hi.bytes() + lo.bytes() + diag.bytes() +
+         (virt ? virt->bytes() : 0);
+}
+
+// ------------------------------------------------------------------- build
+void virtual_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h) {
+  if (precision != CG_PREC_FP64 && precision != CG_PREC_FP32)
+    throw Error(CG_ERR_ARG, "Hamiltonian precision must be CG_PREC_FP64 or CG_PREC_FP32");
+  auto t_begin = std::chrono::steady_clock::now();
+  CG_CUDA(cudaGetDevice(&h.device));
+  if (h.device != b.device) throw Error(CG_ERR_ARG, "basis lives on another device");
+  if (!h.stream) CG_CUDA(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+  cudaStream_t s = h.stream;
+  h.precision = precision;
+  h.n = b.n;
+  auto vp = std::make_shared<VirtualOp>();
+  VirtualOp& v = *vp;
+  const int nn = b.nn, np = b.np, ns = b.ns;
+  if (nn > 32 || np > 32) throw Error(CG_ERR_UNSUPPORTED, "more than 32 m-states per species");
+  v.nn = nn;
+  v.np = np;
+  HostOp H = host_operator(sys, op);
+  int m2max = 0;
+  for (int i = 0; i < ns; ++i) m2max = std::max(m2max, std::abs(b.sp_m2[i]));
+  for (int i = 0; i < ns; ++i)
+    if ((b.sp_m2[i] - b.sp_m2[0]) & 1) throw Error(CG_ERR_UNSUPPORTED, "mixed integer / half-integer m");
+  // transition slot = (change of 2m, change of parity): (dm2 / 2 + m2max) * 2 + dpar.  A neutron
+  // transition in slot s pairs with proton transitions in slot nslot - 2 - (s & ~1) + (s & 1) (opposite
+  // 2m change, same parity change), so both species land in classes of the same block.
+  v.m2max = m2max;
+  v.ndm = 2 * (2 * m2max + 1);
+  v.dm0 = 2 * m2max;
+  const auto& par = b.sp_par;
+  auto dmi_of = [&](int from, int to) { return (((b.sp_m2[to] - b.sp_m2[from]) / 2 + m2max) << 1) | (par[to] ^ par[from]); };
+
+  const int nblocks = int(b.h_bstart.size());
+  const int nclasses = int(b.h_cstart.size()) - 1;
+  v.nblocks = nblocks;
+  v.nconf_p = b.h_cmasks.size();
+  std::vector<uint32_t> blen(nblocks), order(nblocks);
+  for (int i = 0; i < nblocks; ++i) {
+    uint32_t c = b.h_bclass[i];
+    blen[i] = b.h_cstart[c + 1] - b.h_cstart[c];
+    v.lmax = std::max<int>(v.lmax, int(blen[i]));
+  }
+  std::vector<int32_t> block_of(std::max<uint64_t>(b.neut.nconf, 1), -1);
+  for (int i = 0; i < nblocks; ++i) block_of[colex_host(b.h_bmask[i], b.h_binom)] = i;
+  std::vector<int32_t> pclass(std::max<uint64_t>(b.prot.nconf, 1), -1);
+  for (int c = 0; c < nclasses; ++c)
+    for (uint32_t g = b.h_cstart[c]; g < b.h_cstart[c + 1]; ++g) pclass[colex_host(b.h_cmasks[g], b.h_binom)] = c;
+  const uint64_t nall = nn == 64 ? ~0ull : ((1ull << nn) - 1);
+  const uint64_t pall_local = np == 64 ? ~0ull : ((1ull << np) - 1);
+  const auto& m2 = b.sp_m2;
+
+  // neutron transitions and NN2 per block
+  std::vector<uint32_t> nt_off(nblocks + 1, 0), nn_off(nblocks + 1, 0);
+  std::vector<NTrans> nt;
+  std::vector<VPair> nn2;
+  std::vector<double> En(nblocks, 0.0);
+  for (int beta = 0; beta < nblocks; ++beta) {
+    const uint64_t nu = b.h_bmask[beta];
+    const uint64_t holes = ~nu & nall;
+    double e = 0;
+    for (uint64_t t = nu; t; t &= t - 1) {
+      int a = __builtin_ctzll(t);
+      e += H.e1[a * ns + a];
+    }
+    for (uint64_t t = nu; t; t &= t - 1) {
+      int a = __builtin_ctzll(t);
+      for (uint64_t w = t & (t - 1); w; w &= w - 1) {
+        int c = __builtin_ctzll(w);
+        e += H.V(a, c, a, c);
+      }
+    }
+    En[beta] = e;
+    for (uint64_t t = nu; t; t &= t - 1) {
+      const int a = __builtin_ctzll(t);
+      for (uint64_t w = holes; w; w &= w - 1) {
+        const int c = __builtin_ctzll(w);
+        const uint64_t nu2 = nu ^ (1ull << a) ^ (1ull << c);
+        const int tb = block_of[colex_host(nu2, b.h_binom)];
+        if (tb < 0) continue;
+        NTrans tr{};
+        tr.target = uint32_t(tb);
+        tr.a = uint8_t(a);
+        tr.c = uint8_t(c);
+        tr.sign = int8_t(move_sign(nu, a, c));
+        tr.dmi = uint8_t(dmi_of(a, c));
+        tr.cn = 0.0;
+        if (tr.dmi == v.dm0) {
+          const int x = std::min(a, c), yy = std::max(a, c);
+          const uint64_t S0 = a < c ? nu : nu2;
+          double val = H.term1(S0, x, yy);
+          for (uint64_t q = nu & ~(1ull << a); q; q &= q - 1) {
+            const int sc = __builtin_ctzll(q);
+            val += H.term2(S0, std::min(x, sc), std::max(x, sc), std::min(yy, sc), std::max(yy, sc));
+          }
+          tr.cn = val;
+        }
+        nt.push_back(tr);
+      }
+    }
+    nt_off[beta + 1] = uint32_t(nt.size());
+    for (uint64_t t = nu; t; t &= t - 1) {
+      const int a = __builtin_ctzll(t);
+      for (uint64_t u = t & (t - 1); u; u &= u - 1) {
+        const int bb = __builtin_ctzll(u);
+        for (uint64_t w = holes; w; w &= w - 1) {
+          const int c = __builtin_ctzll(w);
+          for (uint64_t z = holes & ~below_h(c + 1); z; z &= z - 1) {
+            const int d = __builtin_ctzll(z);
+            if (m2[a] + m2[bb] != m2[c] + m2[d] || (par[a] ^ par[bb] ^ par[c] ^ par[d])) continue;
+            const uint64_t K = nu ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
+            const int tb = block_of[colex_host(K, b.h_binom)];
+            if (tb < 0) throw Error(CG_ERR_INTERNAL, "two-neutron move leaves the basis");
+            const bool fwd = (a < c) || (a == c && bb < d);
+            const double val = fwd ? H.term2(nu, a, bb, c, d) : H.term2(K, c, d, a, bb);
+            if (std::fabs(val) >= kDropV) nn2.push_back(VPair{uint32_t(tb), 0u, val});
+          }
+        }
+      }
+    }
+    nn_off[beta + 1] = uint32_t(nn2.size());
+  }
+
+  // proton transitions (grouped by 2m change) and PP2 per proton configuration
+  const uint64_t npc = b.h_cmasks.size();
+  std::vector<uint32_t> pt_off(npc * v.ndm + 1, 0), pp_off(npc + 1, 0);
+  std::vector<uint2> pt;
+  std::vector<double> pt_c, Ep(npc, 0.0);
+  std::vector<VPair> pp2;
+  std::vector<std::vector<std::pair<uint2, double>>> bydm(v.ndm);
+  for (uint64_t g = 0; g < npc; ++g) {
+    const uint64_t pi = b.h_cmasks[g];
+    const uint64_t holes = ~pi & pall_local;
+    const uint64_t P = pi << nn;  // global bits
+    double e = 0;
+    for (uint64_t t = pi; t; t &= t - 1) {
+      int q = nn + __builtin_ctzll(t);
+      e += H.e1[q * ns + q];
+    }
+    for (uint64_t t = pi; t; t &= t - 1) {
+      int q = nn + __builtin_ctzll(t);
+      for (uint64_t w = t & (t - 1); w; w &= w - 1) {
+        int r = nn + __builtin_ctzll(w);
+        e += H.V(q, r, q, r);
+      }
+    }
+    Ep[g] = e;
+    for (auto& l : bydm) l.clear();
+    for (uint64_t t = pi; t; t &= t - 1) {
+      const int bl = __builtin_ctzll(t);
+      for (uint64_t w = holes; w; w &= w - 1) {
+        const int dl = __builtin_ctzll(w);
+        const uint64_t pi2 = pi ^ (1ull << bl) ^ (1ull << dl);
+        const uint32_t rank = b.h_pcrank[colex_host(pi2, b.h_binom)];
+        const int bg = nn + bl, dg = nn + dl;
+        const int sign = move_sign(pi, bl, dl);
+        uint2 q;
+        q.x = rank;
+        q.y = uint32_t(bl) | (uint32_t(dl) << 8) | (uint32_t(sign) << 16);
+        double cp = 0.0;
+        if (dmi_of(bg, dg) == v.dm0) {
+          const int x = std::min(bg, dg), yy = std::max(bg, dg);
+          const uint64_t S0 = bl < dl ? P : (pi2 << nn);
+          cp = H.term1(S0, x, yy);
+          for (uint64_t z = P & ~(1ull << bg); z; z &= z - 1) {
+            const int sc = __builtin_ctzll(z);
+            cp += H.term2(S0, std::min(x, sc), std::max(x, sc), std::min(yy, sc), std::max(yy, sc));
+          }
+        }
+        bydm[dmi_of(bg, dg)].push_back({q, cp});
+      }
+    }
+    for (int k = 0; k < v.ndm; ++k) {
+      pt_off[g * v.ndm + k] = uint32_t(pt.size());
+      for (auto& qc : bydm[k]) {
+        pt.push_back(qc.first);
+        pt_c.push_back(qc.second);
+      }
+    }
+    for (uint64_t t = pi; t; t &= t - 1) {
+      const int a = nn + __builtin_ctzll(t);
+      for (uint64_t u = t & (t - 1); u; u &= u - 1) {
+        const int bb = nn + __builtin_ctzll(u);
+        for (uint64_t w = holes; w; w &= w - 1) {
+          const int c = nn + __builtin_ctzll(w);
+          for (uint64_t z = holes & ~below_h(c - nn + 1); z; z &= z - 1) {
+            const int d = nn + __builtin_ctzll(z);
+            if (m2[a] + m2[bb] != m2[c] + m2[d] || (par[a] ^ par[bb] ^ par[c] ^ par[d])) continue;
+            const uint64_t K = P ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
+            const bool fwd = (a < c) || (a == c && bb < d);
+            const double val = fwd ? H.term2(P, a, bb, c, d) : H.term2(K, c, d, a, bb);
+            const uint32_t rank = b.h_pcrank[colex_host(K >> nn, b.h_binom)];
+            if (std::fabs(val) >= kDropV) pp2.push_back(VPair{rank, 0u, val});
+          }
+        }
+      }
+    }
+    pp_off[g + 1] = uint32_t(pp2.size());
+  }
+  pt_off[npc * v.ndm] = uint32_t(pt.size());
+  if (pt.size() >= (1ull << 32) || nt.size() >= (1ull << 32) || pp2.size() >= (1ull << 32) ||
+      nn2.size() >= (1ull << 32))
+    throw Error(CG_ERR_UNSUPPORTED, "transition tables beyond 2^32 entries");
+
+  // lane-interleaved (32-row slice) copies of the per-configuration lists, per proton class
+  const int npp_i = np * np;
+  std::vector<uint32_t> cslice(nclasses + 1, 0);
+  for (int c = 0; c < nclasses; ++c) cslice[c + 1] = cslice[c] + (b.h_cstart[c + 1] - b.h_cstart[c] + 31) / 32;
+  const uint32_t nslices = cslice[nclasses];
+  std::vector<uint32_t> sl_off(size_t(nslices) * v.ndm + 1, 0), sl_e, pps_off(nslices + 1, 0), pp_rank;
+  std::vector<double> sl_c, pp_h;
+  for (int c = 0; c < nclasses; ++c) {
+    const uint32_t g0 = b.h_cstart[c], L = b.h_cstart[c + 1] - g0;
+    if (L > 0xffff) throw Error(CG_ERR_UNSUPPORTED, "proton class longer than 65535 configurations");
+    for (uint32_t sg = 0; sg < (L + 31) / 32; ++sg) {
+      const uint32_t sl = cslice[c] + sg;
+      for (int k = 0; k < v.ndm; ++k) {
+        sl_off[size_t(sl) * v.ndm + k] = uint32_t(sl_e.size());
+        uint32_t cnt = 0;
+        for (uint32_t l = 0; l < 32 && sg * 32 + l < L; ++l) {
+          const uint64_t g = g0 + sg * 32 + l;
+          cnt = std::max(cnt, pt_off[g * v.ndm + k + 1] - pt_off[g * v.ndm + k]);
+        }
+        for (uint32_t j = 0; j < cnt; ++j)
+          for (uint32_t l = 0; l < 32; ++l) {
+            const uint32_t r = sg * 32 + l;
+            uint32_t ent = uint32_t(npp_i) << 16;  // padding: weight slot npp holds 0
+            double cv = 0.0;
+            if (r < L) {
+              const uint64_t g = g0 + r;
+              const uint32_t e0 = pt_off[g * v.ndm + k];
+              if (j < pt_off[g * v.ndm + k + 1] - e0) {
+                const uint2 q = pt[e0 + j];
+                const uint32_t bl = q.y & 0xff, dl = (q.y >> 8) & 0xff, sg1 = (q.y >> 16) & 1;
+                ent = q.x | ((bl * np + dl) << 16) | (sg1 << 27);
+                cv = pt_c[e0 + j];
+              }
+            }
+            sl_e.push_back(ent);
+            sl_c.push_back(cv);
+          }
+      }
+      pps_off[sl] = uint32_t(pp_rank.size());
+      uint32_t cnt = 0;
+      for (uint32_t l = 0; l < 32 && sg * 32 + l < L; ++l) {
+        const uint64_t g = g0 + sg * 32 + l;
+        cnt = std::max(cnt, pp_off[g + 1] - pp_off[g]);
+      }
+      for (uint32_t j = 0; j < cnt; ++j)
+        for (uint32_t l = 0; l < 32; ++l) {
+          const uint32_t r = sg * 32 + l;
+          uint32_t rank = 0;
+          double hv = 0.0;
+          if (r < L && j < pp_off[g0 + r + 1] - pp_off[g0 + r]) {
+            rank = pp2[pp_off[g0 + r] + j].target;
+            hv = pp2[pp_off[g0 + r] + j].h;
+          }
+          pp_rank.push_back(rank);
+          pp_h.push_back(hv);
+        }
+    }
+  }
+  sl_off[size_t(nslices) * v.ndm] = uint32_t(sl_e.size());
+  pps_off[nslices] = uint32_t(pp_rank.size());
+  if (sl_e.size() >= (1ull << 32) || pp_rank.size() >= (1ull << 32))
+    throw Error(CG_ERR_UNSUPPORTED, "transition tables beyond 2^32 entries");
+
+  // interaction slices
+  const size_t npp = size_t(np) * np;
+  std::vector<double> W(size_t(nn) * nn * npp, 0.0), Un(size_t(nn) * nn * np, 0.0), Up(npp * nn, 0.0),
+      Vd(size_t(nn) * np, 0.0);
+  for (int an = 0; an < nn; ++an)
+    for (int cn = 0; cn < nn; ++cn) {
+      if (an == cn) continue;
+      for (int bl = 0; bl < np; ++bl)
+        for (int dl = 0; dl < np; ++dl) {
+          if (bl == dl) continue;
+          const int bg = nn + bl, dg = nn + dl;
+          W[((size_t(an) * nn + cn) * np + bl) * np + dl] = an < cn ? H.V(an, bg, cn, dg) : H.V(cn, dg, an, bg);
+        }
+      for (int q = 0; q < np; ++q)
+        Un[(size_t(an) * nn + cn) * np + q] = H.V(std::min(an, cn), nn + q, std::max(an, cn), nn + q);
+    }
+  for (int bl = 0; bl < np; ++bl)
+    for (int dl = 0; dl < np; ++dl) {
+      if (bl == dl) continue;
+      for (int q = 0; q < nn; ++q)
+        Up[(size_t(bl) * np + dl) * nn + q] = H.V(q, nn + std::min(bl, dl), q, nn + std::max(bl, dl));
+    }
+  for (int q = 0; q < nn; ++q)
+    for (int bl = 0; bl < np; ++bl) Vd[size_t(q) * np + bl] = H.V(q, nn + bl, q, nn + bl);
+
+  // generated elements per product and a largest-first block order
+  std::vector<uint64_t> cls_pp(nclasses, 0), cls_dm(size_t(nclasses) * v.ndm, 0);
+  for (int c = 0; c < nclasses; ++c)
+    for (uint32_t g = b.h_cstart[c]; g < b.h_cstart[c + 1]; ++g) {
+      cls_pp[c] += pp_off[g + 1] - pp_off[g] + pt_off[size_t(g) * v.ndm + v.dm0 + 1] - pt_off[size_t(g) * v.ndm + v.dm0];
+      for (int k = 0; k < v.ndm; ++k) cls_dm[size_t(c) * v.ndm + k] += pt_off[size_t(g) * v.ndm + k + 1] - pt_off[size_t(g) * v.ndm + k];
+    }
+  std::vector<uint64_t> work(nblocks, 0);
+  uint64_t conn = 0;
+  for (int beta = 0; beta < nblocks; ++beta) {
+    const uint32_t c = b.h_bclass[beta];
+    uint64_t w = uint64_t(blen[beta]) * (1 + (nn_off[beta + 1] - nn_off[beta])) + cls_pp[c];
+    for (uint32_t t = nt_off[beta]; t < nt_off[beta + 1]; ++t) {
+      w += cls_dm[size_t(c) * v.ndm + (v.ndm - 2 - (nt[t].dmi & ~1) + (nt[t].dmi & 1))];
+      if (nt[t].dmi == v.dm0) w += blen[beta];
+    }
+    work[beta] = w;
+    conn += w;
+  }
+  v.connections = conn;
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t p, uint32_t q) { return work[p] > work[q]; });
+
+  // upload
+  v.bstart.upload(b.h_bstart, s);
+  v.blen.upload(blen, s);
+  v.bclass.upload(b.h_bclass, s);
+  v.bmask.upload(b.h_bmask, s);
+  v.order.upload(order, s);
+  v.cstart.upload(b.h_cstart, s);
+  v.cmask.upload(b.h_cmasks, s);
+  v.nt_off.upload(nt_off, s);
+  v.nt.upload(nt, s);
+  v.nn_off.upload(nn_off, s);
+  v.nn2.upload(nn2, s);
+  v.cslice.upload(cslice, s);
+  v.sl_off.upload(sl_off, s);
+  v.sl_e.upload(sl_e, s);
+  v.sl_c.upload(sl_c, s);
+  v.pp_off.upload(pps_off, s);
+  v.pp_rank.upload(pp_rank, s);
+  v.pp_h.upload(pp_h, s);
+  std::vector<float> sl_cf(sl_c.begin(), sl_c.end()), pp_hf(pp_h.begin(), pp_h.end());
+  v.sl_cf.upload(sl_cf, s);
+  v.pp_hf.upload(pp_hf, s);
+  v.W.upload(W, s);
+  v.Un.upload(Un, s);
+  v.Up.upload(Up, s);
+  std::vector<float> Wf(W.begin(), W.end()), Unf(Un.begin(), Un.end()), Upf(Up.begin(), Up.end());
+  v.Wf.upload(Wf, s);
+  v.Unf.upload(Unf, s);
+  v.Upf.upload(Upf, s);
+  h.diag.alloc(std::max<uint64_t>(b.n, 1));
+  if (b.n) {
+    DBuf<double> dEn, dEp, dVd;
+    dEn.upload(En, s);
+    dEp.upload(Ep, s);
+    dVd.upload(Vd, s);
+    k_virtual_diag<<<unsigned((b.n + 255) / 256), 256, 0, s>>>(b.n, nblocks, v.bstart.p, v.bclass.p, v.bmask.p,
+                                                               v.cstart.p, v.cmask.p, dEn.p, dEp.p, dVd.p, np,
+                                                               h.diag.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    CG_CUDA(cudaStreamSynchronize(s));
+  }
+  CG_CUDA(cudaStreamSynchronize(s));
+  v.err.alloc(1);
+  h.virt = vp;
+  h.nnz = conn;
+  h.nnz_upper = 0;
+  h.max_row = 0;
+  h.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_begin).count();
+}
+
+}  // namespace cg

@@ -141,6 +141,18 @@ typedef struct {
 } cg_hamiltonian_info;
 
 cg_status cg_hamiltonian_build(const cg_problem* p, const cg_basis* b, int32_t precision, cg_hamiltonian** out);
+/* On-the-fly H + lambda * J-J+ (nothing stored), SM::PPMatrix
+ * (include/sm/PPMatrix.cxx:42-152) as used by DEXHVJT (davidson/DEXHVJT.cpp:36-78):
+ * the product regenerates every element per call from the basis bitstrings and
+ * the interaction, through per-species transition tables (neutron blocks x
+ * proton classes of the M-scheme basis).  The handle works with every product
+ * and Davidson call: CG_PREC_FP32 products compute in FP32, CG_PREC_FP64 and
+ * CG_PREC_REFINE products in FP64; precision only sets the default of
+ * cg_spmm calls.  info.nnz_full = elements generated per product and vector,
+ * info.nnz_upper = 0; cg_hamiltonian_upper_rows / write_hh are unsupported. */
+cg_status cg_hamiltonian_build_virtual(const cg_problem* p, const cg_basis* b, int32_t precision,
+                                       cg_hamiltonian** out);
+cg_status cg_hamiltonian_is_virtual(const cg_hamiltonian* h, int32_t* is_virtual);
 void cg_hamiltonian_destroy(cg_hamiltonian* h);
 cg_status cg_hamiltonian_get_info(const cg_hamiltonian* h, cg_hamiltonian_info* info);
 /* FP64 diagonal, host buffer of n (SparseMatrixCSB::ReadDiagonal, include/tav/csbmatrix.cxx:393). */
@@ -255,6 +267,27 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates);
  * vectors (Davidson::InitVectors, include/kdav/cdavidson.cpp:386). */
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
                       double* eig, double* de, double* resid, double* vecs, cg_davidson_stats* stats);
+
+/* ----------------------------------------------------- spin and isospin */
+/* <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nstates (1..16) vectors of
+ * the basis (host, state k at vecs + k*n, the .EE layout), the computation of
+ * XSHLJT (include/xsm/XSHLJT.cxx:94-126): PPMatrix::Sqr (include/sm/PPMatrix.cxx:
+ * 403-411) of the one-body J+ (SPJPlus) and T+ (SPTPlus, proton -> neutron),
+ * include/sm/spherical2sp.cxx:629-700.  Computed on the GPU in FP64. */
+cg_status cg_jt_expectations(const cg_basis* b, const double* vecs, int32_t nstates, double* jj, double* tt);
+/* 2J from <J-J+> and 2M (SM::JJSpin, include/sm/QN.cxx:40-60): -1 when J + M is
+ * not an integer within 0.1. */
+int32_t cg_jj_spin(double jj, int32_t two_m);
+/* XSHLJT (xmlshell/XSHLJT.cpp, include/xsm/XSHLJT.cxx:38-142): the first nstates
+ * (all when <= 0) eigenpairs of ee_path get 2J and 2T from <J-J+> / <T-T+>
+ * computed on the GPU, E minus lambda*(J-M)(J+M+2)/4 when the system's matrix
+ * carries JJ = lambda, and a <state J P T E dE name Ex><wavefunction Jz Tz file
+ * id/></state> node each in the system of xml_path (SM::AddState +
+ * SM::OrganizeStates, include/xsm/xState.cxx:113-236), written to xml_out (or
+ * in place when NULL).  2Tz is Nv - Zv.  n_added (may be NULL) receives the
+ * number of states recorded after the system's J / T filters. */
+cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* ee_path, int32_t nstates,
+                    const char* xml_out, int32_t* n_added);
 
 /* ------------------------------------------------------------ file I/O */
 /* .EE eigenpair file: uint32 count, then per state double E, dE, resid,

@@ -12,6 +12,9 @@ the GPU build must reproduce:
   sha256 of (rowptr u64 | cols u32) plus every 97th row with values
 * y = H x from the reference SpMM for small cases
 * eigenvalues, eigenvalue changes and residual norms of the reference Davidson
+* <J-J+> and <T-T+> of the reference's eigenvectors (oracle/_ref/ref_jt, the
+  XSHLJT computation) with those vectors for small cases, and the <state>
+  nodes the reference XSHLJT writes
 
 usage (needs the reference tree; the fixtures are committed):
     python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
@@ -23,6 +26,7 @@ import hashlib
 import json
 import os
 import shutil
+import re
 import subprocess
 import sys
 import tempfile
@@ -147,6 +151,39 @@ def dump_case(name: str, work: str, xml: str, full: bool, nstates: int, iters: i
     print(name, json.dumps({k: v for k, v in entry.items() if k not in ("ref_eig", "ref_resid")}))
 
 
+def jt_case(name: str, work: str, xml: str, nstates: int, manifest: dict, keep_vecs: bool) -> None:
+    """<J-J+>, <T-T+> of the reference's own eigenvectors (oracle/_ref/ref_jt, the
+    computation of XSHLJT, include/xsm/XSHLJT.cxx:94-126) and the <state> nodes
+    the reference XSHLJT writes into the system XML."""
+    txt = open(xml).read()
+    jj = re.search(r'<matrix JJ="([^"]*)"/>', txt)
+    lam = jj.group(1) if jj else "0"
+    node = f'<matrix name="{name}" format="pp" JJ="{lam}"/>'
+    txt = txt.replace(jj.group(0), node) if jj else txt.replace("</system>", node + "</system>")
+    xj = os.path.join(work, name + ".jt.xml")
+    open(xj, "w").write(txt)
+    ee = os.path.join(work, name + ".EE")
+    with open(os.path.join(work, name + ".jt.log"), "w") as log:
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_jt"), xj, ee, str(nstates), name], cwd=work,
+                       stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLJT"), xj, "-n", str(nstates)], cwd=work,
+                       stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+    t = np.loadtxt(os.path.join(work, name + ".jt.txt"), ndmin=2)
+    out = open(xj).read()
+    states = [dict(re.findall(r'(\w+)="([^"]*)"', m)) for m in re.findall(r"<state ([^>]*)>", out)]
+    manifest[name]["ref_jj"] = [float(v) for v in t[:, 3]]
+    manifest[name]["ref_tt"] = [float(v) for v in t[:, 4]]
+    manifest[name]["ref_twoJ"] = [int(v) for v in t[:, 5]]
+    manifest[name]["ref_xshljt_states"] = states
+    if keep_vecs:
+        n = manifest[name]["n"]
+        v = np.fromfile(os.path.join(work, name + ".vecs.bin"), np.float64).reshape(-1, n)
+        arrays = dict(np.load(os.path.join(HERE, name + ".npz")))
+        arrays["ref_vecs"] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    print(name, "jt", manifest[name]["ref_twoJ"])
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -165,6 +202,8 @@ def main() -> None:
             dump_case(name, work, xml, full, nst, it, manifest)
             manifest[name]["system"] = dict(space=sysd.space, nv=sysd.nv, zv=sysd.zv, twom=sysd.twom,
                                             parity=sysd.parity, jj=sysd.jj, seed=sysd.seed)
+            if nst and full:
+                jt_case(name, work, xml, nst, manifest, keep_vecs=full)
         for name, sysd in BASIS_CASES.items():
             if a.only and a.only != name:
                 continue
@@ -187,6 +226,7 @@ def main() -> None:
             open(xml, "w").write(txt)
             dump_case("mg24usdb", work, xml, False, 10, 0, manifest, keep_terms=True)
             manifest["mg24usdb"]["system"] = dict(space="sd-usdb", nv=4, zv=4, twom=0, parity="+", jj=None)
+            jt_case("mg24usdb", work, xml, 10, manifest, keep_vecs=False)
             # known answers printed in EXAMPLE-24Mg-usdb.md:29-38 (E, 4 decimals)
             manifest["mg24usdb"]["example_E"] = [-87.1044, -85.6021, -82.9883, -82.732, -82.0294, -81.2219,
                                                  -79.7662, -79.6227, -79.3076, -79.2863]
