@@ -249,6 +249,7 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - s0)
         h2d = int(p2.info.n_one_body) * 16 + int(p2.info.n_two_body) * 24
         d2h = r2.vecs.nbytes + 3 * 8 * NSTATES
+        mixed_vecs = r2.vecs
         del h2, b2, p2
     e2e = statistics.median(e2e_times)
 
@@ -269,19 +270,39 @@ def run_ours(args):
         H64 = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP64)
         torch.cuda.synchronize()
         s0 = time.perf_counter()
-        r64 = cg.davidson_diagonalization(H64, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64,
+        r64 = cg.davidson_diagonalization(H64, NSTATES, want_vectors=True, precision=cg.CG_PREC_FP64,
                                           tol_resid=TOL, maxiter=args.fp64_maxiter)
         torch.cuda.synchronize()
         fp64 = dict(seconds=time.perf_counter() - s0, iterations=int(r64.stats.iterations),
                     converged=int(r64.stats.converged), spmm_seconds=r64.stats.spmm_seconds,
                     max_abs_dE_vs_mixed=float(np.abs(r64.eig - last.eig).max()))
-        del H64
+        # per-state eigenvalue and <J-J+> error of the mixed solve against the FP64 one
+        # (states the FP64 reference algorithm converged)
+        jj_mixed, _ = cg.jt_expectations(basis, mixed_vecs)
+        jj64, _ = cg.jt_expectations(basis, r64.vecs)
+        ok = r64.resid <= TOL
+        fp64["per_state"] = [{"E_fp64": float(r64.eig[i]), "dE": float(last.eig[i] - r64.eig[i]),
+                              "JJ_fp64": float(jj64[i]), "dJJ": float(jj_mixed[i] - jj64[i]),
+                              "twoJ": cg.jj_spin(jj64[i], 0)} for i in range(NSTATES) if ok[i]]
+        fp64["max_abs_dJJ_vs_mixed"] = max((abs(x["dJJ"]) for x in fp64["per_state"]), default=None)
+        del H64, r64
 
     # CPU baseline: the reference algorithm restated in C (oracle), FP64 CSB, on
     # this host's cores, bounded sample scaled to a full solve
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline_from_gpu_matrix(H, fp64["iterations"] if fp64 else None, args.cpu_budget)
+
+    hinfo = {"n": int(H.n), "nnz_full": int(H.info.nnz_full), "nnz_upper": int(H.info.nnz_upper),
+             "build_seconds": H.info.build_seconds, "device_bytes": int(H.info.device_bytes)}
+    batched = None
+    virtual = None
+    if rank == 0 and not args.skip_batched:
+        batched = batched_subbench(cg)
+    if rank == 0 and not args.skip_virtual:
+        del H
+        torch.cuda.empty_cache()
+        virtual = virtual_subbench(cg, fp64["iterations"] if fp64 else None)
 
     if rank != 0:
         if dist:
@@ -307,16 +328,124 @@ def run_ours(args):
                   "matvecs": int(last.stats.matvecs), "converged": int(last.stats.converged),
                   "max_resid": float(last.resid.max()), "spmm_seconds": last.stats.spmm_seconds,
                   "eig": [round(float(x), 8) for x in last.eig]},
-        "hamiltonian": {"n": int(H.n), "nnz_full": int(H.info.nnz_full), "nnz_upper": int(H.info.nnz_upper),
-                        "build_seconds": H.info.build_seconds, "device_bytes": int(H.info.device_bytes)},
+        "hamiltonian": hinfo,
         "fp64_gpu_davidson": fp64,
         "cpu_baseline": cpu,
+        "batched_sd64": batched,
+        "virtual_fp55": virtual,
     }
     if fp64:
         line["speedup_vs_fp64_gpu"] = fp64["seconds"] / per_solve
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def batched_subbench(cg):
+    """64 independent sd-shell problems (dimensions 0..67,251), lowest 5
+    eigenpairs each to resid <= 1e-5: the batched lockstep solve (one CUDA graph
+    launch per iteration for all problems) against the same problems solved one
+    after another with the single-problem mixed solver."""
+    import torch
+    from cosmo_gb300.synthetic import batched_sd_systems, make_system
+    tmp = tempfile.mkdtemp(prefix="cg_batch_")
+    probs = [cg.Problem(make_system(tmp, s)[1]) for s in batched_sd_systems()]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = cg.Batch(probs)
+    build = time.perf_counter() - t0
+    dims = b.dims()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eig, res, nconv, st = b.solve(5)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    wanted = int(sum(min(5, int(d)) for d in dims))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in probs:
+        bb = cg.ManyBodyStates(p)
+        if bb.n <= 64:  # the batched path solves these exactly as well
+            continue
+        h = cg.Hamiltonian(p, bb, cg.CG_PREC_FP32)
+        cg.davidson_diagonalization(h, 5, want_vectors=False, precision=cg.CG_PREC_FP32, tol_resid=TOL,
+                                    block=5, lim=30)
+    torch.cuda.synchronize()
+    seq = time.perf_counter() - t0
+    return {"problems": len(probs), "rows": int(dims.sum()), "max_dim": int(dims.max()),
+            "build_seconds": build, "solve_seconds": min(times), "build_plus_solve_seconds": build + min(times),
+            "iterations_fp32": int(st.iterations_fp32), "iterations_fp64": int(st.iterations_fp64),
+            "graph_launches": int(st.graph_launches), "kernels_per_graph": int(st.graph_kernels),
+            "launches": int(st.launches), "states_converged": int(nconv.sum()), "states_wanted": wanted,
+            "max_resid": float(np.nanmax(res)),
+            "sequential_build_plus_solve_seconds": seq,
+            "speedup_vs_sequential": seq / (build + min(times))}
+
+
+def virtual_subbench(cg, fp64_iters):
+    """fp-shell 5p+5n M=0 (n = 18,600,516) with the on-the-fly product: the
+    products alone, the mixed solve (FP32 products, FP64 projection and
+    refinement) to 10 eigenpairs, and the plain FP64 on-the-fly Davidson (the
+    reference algorithm) timed over a bounded sample of iterations."""
+    import torch
+    from cosmo_gb300.synthetic import SyntheticSystem, make_system
+    tmp = tempfile.mkdtemp(prefix="cg_fp55_")
+    xml = make_system(tmp, SyntheticSystem("fp", 5, 5, 0, "+", 0.5, 8, name="fp55m0s8"))[1]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prob = cg.Problem(xml)
+    basis = cg.ManyBodyStates(prob)
+    hv = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP32, virtual=True)
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    n = hv.n
+    conn = int(hv.info.nnz_full)
+    st = torch.cuda.ExternalStream(hv.stream)
+
+    def product_ms(prec, vb, reps):
+        dt = torch.float32 if prec == cg.CG_PREC_FP32 else torch.float64
+        x = torch.randn(n, vb, dtype=dt, device="cuda")
+        y = torch.zeros(n, vb, dtype=dt, device="cuda")
+        torch.cuda.synchronize()
+        hv.spmm_device(x.data_ptr(), vb, y.data_ptr(), vb, vb, prec)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            hv.spmm_device(x.data_ptr(), vb, y.data_ptr(), vb, vb, prec)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms32 = product_ms(cg.CG_PREC_FP32, 8, 5)
+    ms64 = product_ms(cg.CG_PREC_FP64, 4, 2)
+    kw = dict(precision=cg.CG_PREC_FP32, tol_resid=TOL, **MIXED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = cg.davidson_diagonalization(hv, NSTATES, want_vectors=False, **kw)
+    torch.cuda.synchronize()
+    mixed = time.perf_counter() - t0
+    # plain FP64 on-the-fly Davidson: a bounded sample of iterations
+    t0 = time.perf_counter()
+    r64 = cg.davidson_diagonalization(hv, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64, maxiter=4)
+    torch.cuda.synchronize()
+    per_it = (time.perf_counter() - t0) / max(1, int(r64.stats.iterations))
+    its = fp64_iters or REF_ITERS_DEFAULT
+    return {"workload": "fp-shell 5p+5n M=0, lowest 10 eigenpairs, resid<=1e-5, on-the-fly product",
+            "n": int(n), "connections_per_product": conn, "table_bytes": int(hv.info.device_bytes),
+            "setup_seconds": setup, "fp32_product_ms_8vec": ms32, "fp64_product_ms_4vec": ms64,
+            "fp32_connection_vectors_per_s": conn * 8 / (ms32 * 1e-3),
+            "fp64_connection_vectors_per_s": conn * 4 / (ms64 * 1e-3),
+            "mixed_solve_seconds": mixed, "mixed_iterations": int(r.stats.iterations),
+            "mixed_refine_iterations": int(r.stats.refine_iterations), "mixed_converged": int(r.stats.converged),
+            "mixed_max_resid": float(r.resid.max()), "eig": [round(float(x), 8) for x in r.eig],
+            "fp64_seconds_per_iteration": per_it,
+            "fp64_estimated_seconds": per_it * its,
+            "fp64_sample": f"{int(r64.stats.iterations)} iterations of the reference algorithm (block 10, lim 30) "
+                           f"in FP64 on the on-the-fly product, scaled to {its} iterations",
+            "speedup_vs_fp64_estimate": per_it * its / mixed}
 
 
 def cpu_baseline_from_gpu_matrix(H, ref_iters, budget):
@@ -381,6 +510,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--fp64-maxiter", type=int, default=400)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-virtual", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--mode", default="solve", choices=["solve", "spmm"])
     ap.add_argument("--config", default="fp44", choices=sorted(CONFIGS))

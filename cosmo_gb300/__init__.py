@@ -65,6 +65,18 @@ class DavidsonParams(C.Structure):
                 ("keep", C.c_int32), ("precond", C.c_int32)]
 
 
+class BatchParams(C.Structure):
+    _fields_ = [("nstates", C.c_int32), ("block", C.c_int32), ("lim", C.c_int32), ("keep", C.c_int32),
+                ("maxiter", C.c_int32), ("tol_resid", C.c_double), ("switch_resid", C.c_double),
+                ("use_graph", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("iterations_fp32", C.c_int32), ("iterations_fp64", C.c_int32), ("graph_launches", C.c_uint64),
+                ("graph_kernels", C.c_int32), ("launches", C.c_uint64), ("seconds", C.c_double),
+                ("build_seconds", C.c_double)]
+
+
 class DavidsonStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refine_iterations", C.c_int32), ("matvecs", C.c_int64),
                 ("restarts", C.c_int32), ("converged", C.c_int32), ("ierr", C.c_int32), ("seconds", C.c_double),
@@ -105,7 +117,13 @@ _SIGS = {
     "cg_spmm_refine_static": (C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, C.c_int32]),
     "cg_spmm_refine_static_max_rows": (C.c_int32, [C.POINTER(C.c_uint64)]),
     "cg_hamiltonian_build_virtual": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(_P)]),
+    "cg_hamiltonian_read_hh": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(_P)]),
     "cg_hamiltonian_is_virtual": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
+    "cg_batch_create": (C.c_int32, [C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
+    "cg_batch_destroy": (None, [_P]),
+    "cg_batch_defaults": (C.c_int32, [C.POINTER(BatchParams)]),
+    "cg_batch_dims": (C.c_int32, [_P, _P]),
+    "cg_batch_solve": (C.c_int32, [_P, C.POINTER(BatchParams), _P, _P, _P, C.POINTER(BatchStats)]),
     "cg_jt_expectations": (C.c_int32, [_P, _P, C.c_int32, _P, _P]),
     "cg_jj_spin": (C.c_int32, [C.c_double, C.c_int32]),
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
@@ -153,6 +171,45 @@ def gather_ceiling(rows: int, share: int = 1) -> float:
     g = C.c_double()
     _check(lib().cg_gather_ceiling(rows, share, C.byref(g)))
     return float(g.value)
+
+
+class Batch:
+    """Many independent problems solved together on the GPU (lockstep block
+    Davidson under CUDA graphs; exact batched Jacobi for dimensions <= 64)."""
+
+    def __init__(self, problems: list):
+        arr = (_P * len(problems))(*[p._h for p in problems])
+        h = _P()
+        _check(lib().cg_batch_create(arr, len(problems), C.byref(h)))
+        self._h = h
+        self.count = len(problems)
+        self._problems = problems
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().cg_batch_destroy(self._h)
+            self._h = None
+
+    def dims(self) -> np.ndarray:
+        d = np.zeros(self.count, dtype=np.uint64)
+        _check(lib().cg_batch_dims(self._h, _ptr(d)))
+        return d
+
+    def solve(self, nstates: int = 5, **kw):
+        p = BatchParams()
+        _check(lib().cg_batch_defaults(C.byref(p)))
+        p.nstates = nstates
+        p.block = max(p.block, nstates)
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise TypeError(f"unknown batch parameter {k}")
+            setattr(p, k, v)
+        eig = np.zeros((self.count, nstates))
+        res = np.zeros((self.count, nstates))
+        nconv = np.zeros(self.count, dtype=np.int32)
+        st = BatchStats()
+        _check(lib().cg_batch_solve(self._h, C.byref(p), _ptr(eig), _ptr(res), _ptr(nconv), C.byref(st)))
+        return eig, res, nconv, st
 
 
 def jt_expectations(basis: "ManyBodyStates", vecs) -> tuple[np.ndarray, np.ndarray]:
@@ -291,6 +348,17 @@ class Hamiltonian:
         self._h = h
         self.virtual = bool(virtual)
         self.refresh_info()
+
+    @classmethod
+    def from_hh(cls, path: str, precision: int = CG_PREC_FP64) -> "Hamiltonian":
+        """Stored H read from a .HH file (the davidson_vfile input)."""
+        self = cls.__new__(cls)
+        h = _P()
+        _check(lib().cg_hamiltonian_read_hh(path.encode(), precision, C.byref(h)))
+        self._h = h
+        self.virtual = False
+        self.refresh_info()
+        return self
 
     def refresh_info(self):
         inf = HamiltonianInfo()

@@ -22,7 +22,7 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcosmo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp"]
+SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp"]
 
 
 def nvcc() -> str:
@@ -57,6 +57,9 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB)
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(ROOT, "include", "cosmo_gb300.h"),
                                                                 os.path.abspath(__file__)]
+    deps += [os.path.join(PKG, "cli", f) for f in os.listdir(os.path.join(PKG, "cli"))]
+    if not all(os.path.exists(os.path.join(PKG, "bin", c)) for c in ("cg_dexhvjt", "cg_xshljt")):
+        return True
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
@@ -73,9 +76,34 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
     if r.returncode != 0:
         raise RuntimeError(f"link failed\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+CLI_DIR = os.path.join(PKG, "cli")
+BIN_DIR = os.path.join(PKG, "bin")
+CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt"]
+
+
+def build_cli() -> list[str]:
+    """The command-line drop-ins (C++ over the C ABI) into cosmo_gb300/bin/."""
+    os.makedirs(BIN_DIR, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+
+    def one(name: str) -> str:
+        out = os.path.join(BIN_DIR, name)
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+               os.path.join(CLI_DIR, name + ".cpp"), "-o", out, "-L", PKG, "-lcosmo_gb300",
+               "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"cli build failed: {name}\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return out
+
+    with cf.ThreadPoolExecutor(max_workers=len(CLIS)) as ex:
+        return list(ex.map(one, CLIS))
 
 
 def main() -> None:

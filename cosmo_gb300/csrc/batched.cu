@@ -1,0 +1,902 @@
+// Batched solve of many independent CI problems (uneven dimensions) in lockstep.
+//
+// The reference solves one system per DEXHVJTcsb run (davidson/DEXHVJTcsb.cpp:
+// 36-77, DavidsonDiagonalization include/kdav/davidson.cxx:168-281).  Here a
+// whole set of problems is solved at once on one GPU:
+//   * every problem's basis and stored H (FP32 hi + lo) is built on the GPU and
+//     the matrices are concatenated into one block-diagonal CSR, so a single
+//     SpMM launch multiplies the blocks of all problems;
+//   * problems of dimension <= kDense are diagonalised exactly: their dense H
+//     (hi + lo summed in FP64) goes through the batched Jacobi eigensolver;
+//   * the others run one block Davidson in lockstep (same block size, basis
+//     limit and thick-restart length for all, each with its own vectors,
+//     projected matrix and Ritz pairs): tall-skinny products are segmented by
+//     problem (warp chunks never cross a problem boundary, per-problem partial
+//     sums reduced in a fixed order), the projected eigenproblems are solved on
+//     the device by a parallel cyclic Jacobi (one CTA per problem), and every
+//     iteration shape (basis size) is captured once into a CUDA graph and
+//     replayed, so an iteration is one graph launch for all problems;
+//   * FP32 vectors and products with FP64 projections until the residuals reach
+//     the switch threshold, then the same engine in FP64 with the FP64-accurate
+//     (hi + lo) product to the final tolerance.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <type_traits>
+
+#include "batched.h"
+#include "dense.h"
+
+namespace cg {
+
+namespace {
+
+constexpr int kDense = 64;     // problems up to this dimension are solved exactly
+constexpr int kJac = 64;       // largest matrix of the batched Jacobi
+constexpr int kChunk = 64;     // rows summed in the working precision before an FP64 add
+constexpr int kTile = 16 * kChunk;  // rows of one problem per CTA of the segmented products
+constexpr int kMaxB = 8;       // block size limit
+constexpr int kMaxLim = 40;    // basis limit
+
+// ------------------------------------------------------------ assembly
+__global__ void k_concat_rows(uint64_t n, const uint64_t* __restrict__ rp, uint64_t base, uint64_t row0,
+                              uint64_t* __restrict__ out) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < n) out[row0 + i] = base + rp[i];
+}
+__global__ void k_concat_cols(uint64_t nnz, const uint32_t* __restrict__ c, uint32_t off, uint32_t* __restrict__ out) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < nnz) out[i] = c[i] + off;
+}
+// dense FP64 matrix (n x n, row-major, ld kJac) of rows [r0, r0 + n) of a CSR whose columns start at r0
+__global__ void k_dense_fill(int n, uint64_t r0, const uint64_t* __restrict__ rp, const uint32_t* __restrict__ col,
+                             const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ A) {
+  const int i = blockIdx.x;
+  for (int j = threadIdx.x; j < kJac; j += blockDim.x) A[i * kJac + j] = 0.0;
+  __syncthreads();
+  for (uint64_t e = rp[r0 + i] + threadIdx.x; e < rp[r0 + i + 1]; e += blockDim.x)
+    A[i * kJac + int(col[e] - r0)] = double(hi[e]) + double(lo[e]);
+}
+
+// ------------------------------------------------ batched Jacobi eigensolver
+// One CTA per matrix: A (k x k, symmetric, FP64, ld kJac) -> eigenvalues
+// ascending w[0..k) and eigenvectors Z (column j of the k x k block, ld kJac).
+// Cyclic Jacobi with the round-robin ordering: each round applies k/2 disjoint
+// rotations at once; sweeps repeat until the off-diagonal norm falls below
+// 1e-15 of the Frobenius norm (at most 40 sweeps).
+constexpr size_t kJacSmem = (size_t(2) * kJac * (kJac + 1) + 256 + kJac) * sizeof(double) + (2 * kJac + 8) * sizeof(int);
+
+__global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain, const int* __restrict__ kdim,
+                                                 int kconst, double* __restrict__ w, double* __restrict__ Zout,
+                                                 const int* __restrict__ fz) {
+  if (fz && fz[blockIdx.x]) return;
+  extern __shared__ double jsm[];
+  double(*A)[kJac + 1] = reinterpret_cast<double(*)[kJac + 1]>(jsm);
+  double(*Z)[kJac + 1] = reinterpret_cast<double(*)[kJac + 1]>(jsm + kJac * (kJac + 1));
+  double* red = jsm + 2 * kJac * (kJac + 1);
+  double* rc = red + 256;
+  double* rs = rc + kJac / 2;
+  int* rp = reinterpret_cast<int*>(rs + kJac / 2);
+  int* rq = rp + kJac / 2;
+  int* order = rq + kJac / 2;
+  int& done = order[kJac];
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const int k = kdim ? kdim[b] : kconst;
+  const double* Ab = Ain + size_t(b) * kJac * kJac;
+  for (int i = tid; i < kJac * kJac; i += blockDim.x) {
+    const int r = i / kJac, c = i % kJac;
+    A[r][c] = (r < k && c < k) ? Ab[r * kJac + c] : 0.0;
+    Z[r][c] = r == c ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int kk = k + (k & 1);  // even player count; player k (if odd) is idle
+  for (int sweep = 0; sweep < 40 && k > 1; ++sweep) {
+    // convergence: off-diagonal vs total
+    double off = 0.0, tot = 0.0;
+    for (int i = tid; i < k * k; i += blockDim.x) {
+      const int r = i / k, c = i % k;
+      const double v = A[r][c] * A[r][c];
+      tot += v;
+      if (r != c) off += v;
+    }
+    red[tid] = off;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+      if (tid < s) red[tid] += red[tid + s];
+      __syncthreads();
+    }
+    const double offs = red[0];
+    __syncthreads();
+    red[tid] = tot;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+      if (tid < s) red[tid] += red[tid + s];
+      __syncthreads();
+    }
+    if (tid == 0) done = offs <= 1e-30 * red[0] || offs == 0.0;
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < kk - 1; ++round) {
+      // pairs of this round: player 0 fixed, the others rotate
+      if (tid < kk / 2) {
+        auto player = [&](int pos) { return pos == 0 ? 0 : 1 + (pos - 1 + round) % (kk - 1); };
+        int p = player(tid), q = player(kk - 1 - tid);
+        if (p > q) { int t = p; p = q; q = t; }
+        double c = 1.0, s = 0.0;
+        if (q < k) {
+          const double apq = A[p][q];
+          if (fabs(apq) > 1e-300) {
+            const double tau = (A[q][q] - A[p][p]) / (2.0 * apq);
+            const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        rp[tid] = p;
+        rq[tid] = q;
+        rc[tid] = c;
+        rs[tid] = s;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int i = tid; i < (kk / 2) * k; i += blockDim.x) {
+        const int pr = i / k, j = i % k;
+        const int p = rp[pr], q = rq[pr];
+        if (q < k) {
+          const double c = rc[pr], s = rs[pr];
+          const double ap = A[p][j], aq = A[q][j];
+          A[p][j] = c * ap - s * aq;
+          A[q][j] = s * ap + c * aq;
+        }
+      }
+      __syncthreads();
+      // columns: A <- A J, Z <- Z J
+      for (int i = tid; i < (kk / 2) * k; i += blockDim.x) {
+        const int pr = i / k, j = i % k;
+        const int p = rp[pr], q = rq[pr];
+        if (q < k) {
+          const double c = rc[pr], s = rs[pr];
+          const double ap = A[j][p], aq = A[j][q];
+          A[j][p] = c * ap - s * aq;
+          A[j][q] = s * ap + c * aq;
+          const double zp = Z[j][p], zq = Z[j][q];
+          Z[j][p] = c * zp - s * zq;
+          Z[j][q] = s * zp + c * zq;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // ascending order (ties by index)
+  for (int i = tid; i < k; i += blockDim.x) {
+    int rank = 0;
+    const double di = A[i][i];
+    for (int j = 0; j < k; ++j) {
+      const double dj = A[j][j];
+      rank += (dj < di) || (dj == di && j < i);
+    }
+    order[rank] = i;
+  }
+  __syncthreads();
+  double* wb = w + size_t(b) * kJac;
+  double* Zb = Zout + size_t(b) * kJac * kJac;
+  for (int i = tid; i < kJac; i += blockDim.x) wb[i] = i < k ? A[order[i]][order[i]] : 0.0;
+  for (int i = tid; i < kJac * kJac; i += blockDim.x) {
+    const int r = i / kJac, c = i % kJac;
+    Zb[r * kJac + c] = (r < k && c < k) ? Z[r][order[c]] : 0.0;
+  }
+}
+
+// ------------------------------------------------ segmented tall-skinny ops
+// Per-tile partials of G = X[:, xo:xo+K]^T Y[:, yo:yo+J]: one CTA per tile (rows
+// of one problem), warp w takes every 8th 64-row chunk of the tile, lane owns
+// columns lane and lane + 32 of X; products are summed in T over a 64-row chunk
+// and the chunks in FP64 (FP32 products with FP64 sums for the FP32 engine),
+// then the 8 warps are added in a fixed order.
+template <class T>
+__global__ void __launch_bounds__(256) k_bxty(const BatchChunk* __restrict__ tiles, const T* __restrict__ X, int ldx,
+                                              int xo, int K, const T* __restrict__ Y, int ldy, int yo, int J,
+                                              double* __restrict__ part, const int* __restrict__ fz) {
+  __shared__ double red[8][kMaxLim * kMaxB];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const BatchChunk tl = tiles[blockIdx.x];
+  if (fz[tl.prob]) return;
+  const bool two = K > 32;
+  double a0[kMaxB], a1[kMaxB];
+#pragma unroll
+  for (int j = 0; j < kMaxB; ++j) { a0[j] = 0.0; a1[j] = 0.0; }
+  for (uint32_t c0 = tl.row0 + uint32_t(w) * kChunk; c0 < tl.row1; c0 += 8u * kChunk) {
+    const uint32_t c1 = min(tl.row1, c0 + uint32_t(kChunk));
+    T s0[kMaxB], s1[kMaxB];
+#pragma unroll
+    for (int j = 0; j < kMaxB; ++j) { s0[j] = T(0); s1[j] = T(0); }
+    for (uint32_t r = c0; r < c1; ++r) {
+      const T x0 = lane < K ? X[size_t(r) * ldx + xo + lane] : T(0);
+      const T* yr = Y + size_t(r) * ldy + yo;
+      if (two) {
+        const T x1 = lane + 32 < K ? X[size_t(r) * ldx + xo + lane + 32] : T(0);
+#pragma unroll
+        for (int j = 0; j < kMaxB; ++j)
+          if (j < J) {
+            const T yv = yr[j];
+            s0[j] = fma(x0, yv, s0[j]);
+            s1[j] = fma(x1, yv, s1[j]);
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < kMaxB; ++j)
+          if (j < J) s0[j] = fma(x0, yr[j], s0[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxB; ++j) {
+      a0[j] += double(s0[j]);
+      if (two) a1[j] += double(s1[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kMaxB; ++j)
+    if (j < J) {
+      if (lane < K) red[w][lane * J + j] = a0[j];
+      if (lane + 32 < K) red[w][(lane + 32) * J + j] = a1[j];
+    }
+  __syncthreads();
+  for (int o = threadIdx.x; o < K * J; o += blockDim.x) {
+    double sum = 0.0;
+    for (int i = 0; i < 8; ++i) sum += red[i][o];
+    part[size_t(blockIdx.x) * (kMaxLim * kMaxB) + o] = sum;
+  }
+}
+
+// G[q][K x J] = sum of the partials of problem q's chunks, in chunk order
+__global__ void k_breduce(const uint32_t* __restrict__ pchunk, const double* __restrict__ part, int K, int J,
+                          double* __restrict__ G, const int* __restrict__ fz) {
+  const int q = blockIdx.x;
+  if (fz[q]) return;
+  for (int o = threadIdx.x; o < K * J; o += blockDim.x) {
+    double s = 0.0;
+    for (uint32_t c = pchunk[q]; c < pchunk[q + 1]; ++c) s += part[size_t(c) * (kMaxLim * kMaxB) + o];
+    G[size_t(q) * (kMaxLim * kMaxB) + o] = s;
+  }
+}
+
+// S[q][i][c0 + j] = S[q][c0 + j][i] = G[q][i * J + j] for i < K (K = c0 + J)
+__global__ void k_bset_proj(int K, int J, int c0, const double* __restrict__ G, double* __restrict__ S,
+                            const int* __restrict__ fz) {
+  const int q = blockIdx.x;
+  if (fz[q]) return;
+  double* Sq = S + size_t(q) * kJac * kJac;
+  const double* Gq = G + size_t(q) * (kMaxLim * kMaxB);
+  for (int o = threadIdx.x; o < K * J; o += blockDim.x) {
+    const int i = o / J, j = o % J;
+    const double v = Gq[o];
+    if (i >= c0 && i - c0 > j) continue;  // lower part of the new block comes from its mirror
+    Sq[i * kJac + c0 + j] = v;
+    Sq[(c0 + j) * kJac + i] = v;
+  }
+}
+
+// Y[r][yo + j] = beta * Y[r][yo + j] + alpha * sum_i X[r][xo + i] M[q][i][j]  (M ld mld, per problem),
+// computed in T.  One CTA per tile (rows of one problem, M staged in shared
+// memory), one thread per row: the row is read completely before it is
+// written (in-place safe).
+template <class T>
+__global__ void __launch_bounds__(256) k_bgemm(const BatchChunk* __restrict__ tiles, const T* X, int ldx, int xo,
+                                               int K, const double* __restrict__ M, size_t mstride, int mld, T* Y,
+                                               int ldy, int yo, int J, double alpha, double beta,
+                                               const int* __restrict__ fz) {
+  __shared__ T Ms[kMaxLim * kMaxLim];
+  const BatchChunk tl = tiles[blockIdx.x];
+  if (fz[tl.prob]) return;
+  const double* Mq = M + size_t(tl.prob) * mstride;
+  for (int i = threadIdx.x; i < K * J; i += blockDim.x) Ms[i] = T(Mq[(i / J) * mld + (i % J)]);
+  __syncthreads();
+  const T a = T(alpha), bt = T(beta);
+  for (uint32_t r = tl.row0 + threadIdx.x; r < tl.row1; r += blockDim.x) {
+    T acc[kMaxLim];
+#pragma unroll
+    for (int j = 0; j < kMaxLim; ++j) acc[j] = T(0);
+    const T* xr = X + size_t(r) * ldx + xo;
+    for (int i = 0; i < K; ++i) {
+      const T xv = xr[i];
+#pragma unroll
+      for (int j = 0; j < kMaxLim; ++j)
+        if (j < J) acc[j] = fma(xv, Ms[i * J + j], acc[j]);
+    }
+    T* yr = Y + size_t(r) * ldy + yo;
+#pragma unroll
+    for (int j = 0; j < kMaxLim; ++j)
+      if (j < J) yr[j] = beta == 0.0 ? a * acc[j] : bt * yr[j] + a * acc[j];
+  }
+}
+
+// R[r][j] = sum_i (AV[r][i] - theta[q][j] V[r][i]) Z[q][i][j], j < b  (computed in T;
+// one CTA per tile with Z[:, 0:b] and theta staged in shared memory)
+template <class T>
+__global__ void __launch_bounds__(256) k_bresid(const BatchChunk* __restrict__ tiles, const T* __restrict__ V,
+                                                const T* __restrict__ AV, int ld, int K, const double* __restrict__ w,
+                                                const double* __restrict__ Z, T* __restrict__ R, int ldr, int b,
+                                                const int* __restrict__ fz) {
+  __shared__ T Zs[kMaxLim * kMaxB];
+  __shared__ T th[kMaxB];
+  const BatchChunk tl = tiles[blockIdx.x];
+  if (fz[tl.prob]) return;
+  const double* Zq = Z + size_t(tl.prob) * kJac * kJac;
+  for (int i = threadIdx.x; i < K * b; i += blockDim.x) Zs[i] = T(Zq[(i / b) * kJac + (i % b)]);
+  if (threadIdx.x < b) th[threadIdx.x] = T(w[size_t(tl.prob) * kJac + threadIdx.x]);
+  __syncthreads();
+  for (uint32_t r = tl.row0 + threadIdx.x; r < tl.row1; r += blockDim.x) {
+    T acc[kMaxB];
+#pragma unroll
+    for (int j = 0; j < kMaxB; ++j) acc[j] = T(0);
+    for (int i = 0; i < K; ++i) {
+      const T v = V[size_t(r) * ld + i], av = AV[size_t(r) * ld + i];
+#pragma unroll
+      for (int j = 0; j < kMaxB; ++j)
+        if (j < b) acc[j] = fma(av - th[j] * v, Zs[i * b + j], acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxB; ++j)
+      if (j < b) R[size_t(r) * ldr + j] = acc[j];
+  }
+}
+
+// V[r][c0 + j] = R[r][j] / (theta[q][j] - diag[r]) with the reference's 1e-13 floor
+template <class T>
+__global__ void k_bprecond(uint32_t nrows, const uint32_t* __restrict__ rowprob, const T* __restrict__ R, int ldr,
+                           const double* __restrict__ w, const double* __restrict__ diag, T* __restrict__ V, int ld,
+                           int c0, int b, const int* __restrict__ fz) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows || fz[rowprob[r]]) return;
+  const double* wq = w + size_t(rowprob[r]) * kJac;
+  for (int j = 0; j < b; ++j) {
+    double den = wq[j] - diag[r];
+    if (fabs(den) < 1e-13) den = den < 0 ? -1e-13 : 1e-13;
+    V[size_t(r) * ld + c0 + j] = T(double(R[size_t(r) * ldr + j]) / den);
+  }
+}
+
+// per problem: residual norms of the b Ritz pairs from diag(G) (G = R^T R); a
+// problem whose first nev residuals are all <= tol is frozen (every later kernel
+// of the engine skips it, so its basis, Ritz values and vectors stay those of
+// this iteration; kfreeze records the basis size).  nconv = frozen problems.
+__global__ void k_bconv(int Q, int nev, int b, const double* __restrict__ G, double tol, double* __restrict__ rnorm,
+                        int* __restrict__ fz, int* __restrict__ kfreeze, int k, int* __restrict__ nconv) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  for (int q = threadIdx.x; q < Q; q += blockDim.x) {
+    if (!fz[q]) {
+      bool ok = true;
+      for (int j = 0; j < b; ++j) {
+        const double r = sqrt(fmax(G[size_t(q) * (kMaxLim * kMaxB) + j * b + j], 0.0));
+        rnorm[q * kMaxB + j] = r;
+        if (j < nev) ok = ok && r <= tol;
+      }
+      if (ok) {
+        fz[q] = 1;
+        kfreeze[q] = k;
+      }
+    }
+    if (fz[q]) atomicAdd(&cnt, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *nconv = cnt;
+}
+
+// Cholesky of each problem's b x b Gram matrix G = T^T T; writes M = L^{-T}
+// (upper triangular, ld kMaxB) so that T M has orthonormal columns.  A pivot
+// below 1e-24 of the largest diagonal marks the column for replacement.
+__global__ void k_bchol(int Q, int b, const double* __restrict__ G, double* __restrict__ M, int* __restrict__ bad,
+                        const int* __restrict__ fz) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Q) return;
+  if (fz[q]) {
+    bad[q] = 0;
+    return;
+  }
+  double L[kMaxB][kMaxB], Li[kMaxB][kMaxB];
+  const double* g = G + size_t(q) * (kMaxLim * kMaxB);
+  double dmax = 0.0;
+  for (int i = 0; i < b; ++i) dmax = fmax(dmax, g[i * b + i]);
+  int badmask = 0;
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double s = g[i * b + j];
+      for (int t = 0; t < j; ++t) s -= L[i][t] * L[j][t];
+      if (i == j) {
+        if (s <= 1e-24 * dmax || !(s > 0.0)) {
+          badmask |= 1 << i;
+          L[i][i] = 1.0;
+          for (int t = 0; t < i; ++t) L[i][t] = 0.0;
+        } else {
+          L[i][i] = sqrt(s);
+        }
+      } else {
+        L[i][j] = (badmask >> i & 1) ? 0.0 : s / L[j][j];
+      }
+    }
+  // Li = L^{-1} (lower)
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) Li[i][j] = 0.0;
+  for (int j = 0; j < b; ++j) {
+    Li[j][j] = 1.0 / L[j][j];
+    for (int i = j + 1; i < b; ++i) {
+      double s = 0.0;
+      for (int t = j; t < i; ++t) s += L[i][t] * Li[t][j];
+      Li[i][j] = -s / L[i][i];
+    }
+  }
+  double* m = M + size_t(q) * (kMaxLim * kMaxB);
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) m[i * kMaxB + j] = Li[j][i];  // (L^{-1})^T
+  bad[q] = badmask;
+}
+
+// replace marked columns by a fixed pseudo-random vector (hash of row and column)
+template <class T>
+__global__ void k_bfill(uint32_t nrows, const uint32_t* __restrict__ rowprob, const int* __restrict__ bad, T* V,
+                        int ld, int c0, int b, uint32_t salt, const int* __restrict__ fz) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows || fz[rowprob[r]]) return;
+  const int m = bad[rowprob[r]];
+  if (!m) return;
+  for (int j = 0; j < b; ++j)
+    if (m >> j & 1) {
+      uint32_t h = r * 0x9E3779B1u ^ (uint32_t(j + 1) * 0x85EBCA77u) ^ salt;
+      h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+      V[size_t(r) * ld + c0 + j] = T(double(h) * (1.0 / 4294967296.0) - 0.5);
+    }
+}
+
+// S[q] = diag(w[q][0..keep)), rest zero
+__global__ void k_bset_diag(int keep, const double* __restrict__ w, double* __restrict__ S,
+                            const int* __restrict__ fz) {
+  const int q = blockIdx.x;
+  if (fz[q]) return;
+  double* Sq = S + size_t(q) * kJac * kJac;
+  for (int i = threadIdx.x; i < kJac * kJac; i += blockDim.x) {
+    const int r = i / kJac, c = i % kJac;
+    Sq[i] = (r == c && r < keep) ? w[size_t(q) * kJac + r] : 0.0;
+  }
+}
+
+// M[q][i][j] = diag(1 / sqrt(G[q][j][j])) for normalisation (ld kMaxB)
+__global__ void k_bnorm_mat(int Q, int b, const double* __restrict__ G, double* __restrict__ M,
+                            const int* __restrict__ fz) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Q || fz[q]) return;
+  double* m = M + size_t(q) * (kMaxLim * kMaxB);
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) {
+      double g = G[size_t(q) * (kMaxLim * kMaxB) + j * b + j];
+      m[i * kMaxB + j] = (i == j) ? (g > 0.0 ? 1.0 / sqrt(g) : 1.0) : 0.0;
+    }
+}
+
+template <class T>
+__global__ void k_bpack(uint32_t nrows, const T* __restrict__ V, int ld, int c0, int b, T* __restrict__ W, int ldw) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= uint64_t(nrows) * ldw) return;
+  const uint64_t r = i / ldw;
+  const int j = int(i - r * ldw);
+  W[i] = j < b ? V[r * ld + c0 + j] : T(0);
+}
+
+__global__ void k_bunits(int Q, const uint32_t* __restrict__ rows, int b, float* V32, double* V64, int ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Q * b) return;
+  const int j = i % b;
+  if (V32) V32[size_t(rows[i]) * ld + j] = 1.f;
+  if (V64) V64[size_t(rows[i]) * ld + j] = 1.0;
+}
+
+template <class S, class D>
+__global__ void k_bconvert(uint64_t n, const S* __restrict__ a, int lda, D* __restrict__ b, int ldb, int cols) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= n * cols) return;
+  const uint64_t r = i / cols;
+  const int j = int(i - r * cols);
+  b[r * ldb + j] = D(a[r * lda + j]);
+}
+
+// X[r][0:b] = Ritz vectors of the problem of tile: V[:, 0:K] Z[:, 0:b] with K the
+// freeze-time basis size for frozen problems; otherwise the last iteration's
+// (V[:, 0:b] when that iteration restarted, V[:, 0:last_k] Z otherwise)
+template <class T, class D>
+__global__ void __launch_bounds__(256) k_britz(const BatchChunk* __restrict__ tiles, const T* __restrict__ V, int ld,
+                                               const double* __restrict__ Z, const int* __restrict__ fz,
+                                               const int* __restrict__ kfreeze, int last_k, int last_restarted,
+                                               D* __restrict__ X, int ldx, int b) {
+  __shared__ double Zs[kMaxLim * kMaxB];
+  const BatchChunk tl = tiles[blockIdx.x];
+  const bool frozen = fz[tl.prob] != 0;
+  const bool copy = !frozen && last_restarted;
+  const int K = frozen ? kfreeze[tl.prob] : last_k;
+  const double* Zq = Z + size_t(tl.prob) * kJac * kJac;
+  for (int i = threadIdx.x; i < K * b; i += blockDim.x) Zs[i] = Zq[(i / b) * kJac + (i % b)];
+  __syncthreads();
+  for (uint32_t r = tl.row0 + threadIdx.x; r < tl.row1; r += blockDim.x) {
+    const T* vr = V + size_t(r) * ld;
+    for (int j = 0; j < b; ++j) {
+      double a = 0.0;
+      if (copy) {
+        a = double(vr[j]);
+      } else {
+        for (int i = 0; i < K; ++i) a += double(vr[i]) * Zs[i * b + j];
+      }
+      X[size_t(r) * ldx + j] = D(a);
+    }
+  }
+}
+
+inline unsigned nblk(uint64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
+
+// ---------------------------------------------------------------- engine
+template <class T>
+struct BEngine {
+  BatchSet& bs;
+  cudaStream_t s;
+  int Q, nev, b, lim, keep;
+  uint32_t N;
+  DBuf<T> V, AV, R, W;        // N x lim, N x lim, N x 8, N x 8 (SpMM staging, FP32 engine)
+  DBuf<double> S, Z, w, G, M, part, rnorm;
+  DBuf<float> dfstage;        // N x 16 (FP64 engine: double-float staging)
+  DBuf<int> fz, kfreeze, nconv, bad;
+  int* h_nconv = nullptr;     // pinned
+  std::vector<cudaGraphExec_t> graphs;  // per basis size
+  std::vector<int> graph_kernels;
+  int kernels_per_graph = 0;
+  uint64_t graph_launches = 0, graph_kernel_launches = 0;
+  double iter_s = 0;
+  int last_k = 0;
+
+  BEngine(BatchSet& b_, int nev0, int b0, int lim0, int keep0)
+      : bs(b_), s(b_.stream), Q(b_.nq), nev(nev0), b(b0), lim(lim0), keep(keep0), N(uint32_t(b_.H.n)) {
+    V.alloc(size_t(N) * lim);
+    AV.alloc(size_t(N) * lim);
+    R.alloc(size_t(N) * 8);
+    W.alloc(size_t(N) * 8);
+    if (sizeof(T) == 8) dfstage.alloc(size_t(N) * 16);
+    S.alloc(size_t(Q) * kJac * kJac);
+    Z.alloc(size_t(Q) * kJac * kJac);
+    w.alloc(size_t(Q) * kJac);
+    G.alloc(size_t(Q) * kMaxLim * kMaxB);
+    M.alloc(size_t(Q) * kMaxLim * kMaxB);
+    part.alloc(size_t(bs.nchunks) * kMaxLim * kMaxB);
+    rnorm.alloc(size_t(Q) * kMaxB);
+    fz.alloc(Q);
+    kfreeze.alloc(Q);
+    nconv.alloc(1);
+    bad.alloc(Q);
+    CG_CUDA(cudaMallocHost(&h_nconv, sizeof(int)));
+    CG_CUDA(cudaMemsetAsync(V.p, 0, V.bytes(), s));
+    CG_CUDA(cudaMemsetAsync(AV.p, 0, AV.bytes(), s));
+    CG_CUDA(cudaMemsetAsync(S.p, 0, S.bytes(), s));
+    CG_CUDA(cudaMemsetAsync(fz.p, 0, fz.bytes(), s));
+    CG_CUDA(cudaMemsetAsync(kfreeze.p, 0, kfreeze.bytes(), s));
+    CG_CUDA(cudaMemsetAsync(bad.p, 0, bad.bytes(), s));
+    graphs.assign(lim + 1, nullptr);
+    graph_kernels.assign(lim + 1, 0);
+  }
+  ~BEngine() {
+    for (auto g : graphs)
+      if (g) cudaGraphExecDestroy(g);
+    if (h_nconv) cudaFreeHost(h_nconv);
+  }
+
+  // G[q] = X[:, xo:xo+K]^T Y[:, yo:yo+J] per (unfrozen) problem
+  void xty(const T* X, int ldx, int xo, int K, const T* Y, int ldy, int yo, int J) {
+    k_bxty<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, X, ldx, xo, K, Y, ldy, yo, J, part.p, fz.p);
+    k_breduce<<<Q, 128, 0, s>>>(bs.pchunk.p, part.p, K, J, G.p, fz.p);
+  }
+  void gemm(const T* X, int ldx, int xo, int K, const double* Mm, size_t mstride, int mld, T* Y, int ldy, int yo,
+            int J, double alpha, double beta) {
+    k_bgemm<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, X, ldx, xo, K, Mm, mstride, mld, Y, ldy, yo, J,
+                                                     alpha, beta, fz.p);
+  }
+  void spmm(int c0) {
+    if constexpr (sizeof(T) == 4) {
+      k_bpack<float><<<nblk(uint64_t(N) * 8), 256, 0, s>>>(N, V.p, lim, c0, b, W.p, 8);
+      spmm_f32_padded(bs.H, W.p, 8, AV.p + c0, lim, b, s);
+    } else {
+      spmm_refine_df(bs.H, V.p + c0, lim, AV.p + c0, lim, b, dfstage.p, s);
+    }
+  }
+  // orthonormalise V[:, c0:c0+b] against V[:, 0:c0] and within the block
+  void orthonormalise(int c0) {
+    const size_t ms = kMaxLim * kMaxB;
+    xty(V.p, lim, c0, b, V.p, lim, c0, b);
+    k_bnorm_mat<<<nblk(Q, 64), 64, 0, s>>>(Q, b, G.p, M.p, fz.p);
+    gemm(V.p, lim, c0, b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
+    for (int pass = 0; pass < 2; ++pass) {
+      if (c0 > 0) {
+        for (int rep = 0; rep < 2; ++rep) {
+          xty(V.p, lim, 0, c0, V.p, lim, c0, b);  // G = V^T T (c0 x b)
+          gemm(V.p, lim, 0, c0, G.p, ms, b, V.p, lim, c0, b, -1.0, 1.0);
+        }
+      }
+      xty(V.p, lim, c0, b, V.p, lim, c0, b);
+      k_bchol<<<nblk(Q, 64), 64, 0, s>>>(Q, b, G.p, M.p, bad.p, fz.p);
+      gemm(V.p, lim, c0, b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
+      k_bfill<T><<<nblk(N), 256, 0, s>>>(N, bs.rowprob.p, bad.p, V.p, lim, c0, b, 0x1234567u + pass, fz.p);
+    }
+  }
+  // one iteration with current basis size k (the newest b columns not yet multiplied)
+  void enqueue_step(int k, double tol) {
+    spmm(k - b);
+    xty(V.p, lim, 0, k, AV.p, lim, k - b, b);
+    k_bset_proj<<<Q, 128, 0, s>>>(k, b, k - b, G.p, S.p, fz.p);
+    k_bjacobi<<<Q, 256, kJacSmem, s>>>(S.p, nullptr, k, w.p, Z.p, fz.p);
+    k_bresid<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, V.p, AV.p, lim, k, w.p, Z.p, R.p, 8, b, fz.p);
+    xty(R.p, 8, 0, b, R.p, 8, 0, b);
+    k_bconv<<<1, 256, 0, s>>>(Q, nev, b, G.p, tol, rnorm.p, fz.p, kfreeze.p, k, nconv.p);
+    CG_CUDA(cudaMemcpyAsync(h_nconv, nconv.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int c0 = k;
+    if (k + b > lim) {  // thick restart to the `keep` lowest Ritz vectors
+      const size_t zs = size_t(kJac) * kJac;
+      gemm(V.p, lim, 0, k, Z.p, zs, kJac, V.p, lim, 0, keep, 1.0, 0.0);
+      gemm(AV.p, lim, 0, k, Z.p, zs, kJac, AV.p, lim, 0, keep, 1.0, 0.0);
+      k_bset_diag<<<Q, 256, 0, s>>>(keep, w.p, S.p, fz.p);
+      c0 = keep;
+    }
+    k_bprecond<T><<<nblk(N, 128), 128, 0, s>>>(N, bs.rowprob.p, R.p, 8, w.p, bs.diag.p, V.p, lim, c0, b, fz.p);
+    orthonormalise(c0);
+  }
+  int next_k(int k) const { return (k + b > lim ? keep : k) + b; }
+
+  // run until every problem's first nev residuals are <= tol or maxiter; returns iterations
+  int run(double tol, int maxiter, bool use_graph) {
+    int k = b;
+    int it = 0;
+    for (; it < maxiter; ++it) {
+      last_k = k;
+      auto t0 = std::chrono::steady_clock::now();
+      if (use_graph) {
+        if (!graphs[k]) {
+          cudaGraph_t g;
+          CG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+          enqueue_step(k, tol);
+          CG_CUDA(cudaStreamEndCapture(s, &g));
+          size_t nn = 0;
+          CG_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+          std::vector<cudaGraphNode_t> nodes(nn);
+          CG_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+          int nk = 0;
+          for (auto nd : nodes) {
+            cudaGraphNodeType ty;
+            CG_CUDA(cudaGraphNodeGetType(nd, &ty));
+            nk += ty == cudaGraphNodeTypeKernel;
+          }
+          graph_kernels[k] = nk;
+          kernels_per_graph = std::max(kernels_per_graph, nk);
+          CG_CUDA(cudaGraphInstantiate(&graphs[k], g, 0));
+          CG_CUDA(cudaGraphDestroy(g));
+        }
+        CG_CUDA(cudaGraphLaunch(graphs[k], s));
+        ++graph_launches;
+        graph_kernel_launches += uint64_t(graph_kernels[k]);
+      } else {
+        enqueue_step(k, tol);
+      }
+      CG_CUDA(cudaStreamSynchronize(s));
+      iter_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (*h_nconv == Q) {
+        ++it;
+        break;
+      }
+      k = next_k(k);
+    }
+    return it;
+  }
+  // Ritz vectors (b per problem) into X (N x b, ld ldx)
+  template <class D>
+  void ritz_vectors(D* X, int ldx) {
+    k_britz<T, D><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, V.p, lim, Z.p, fz.p, kfreeze.p, last_k,
+                                                        last_k + b > lim ? 1 : 0, X, ldx, b);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+  }
+};
+
+}  // namespace
+
+BatchSet::~BatchSet() {
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void batch_build(const std::vector<const System*>& sys, const std::vector<const Operator*>& ops, BatchSet& bs) {
+  CG_CUDA(cudaGetDevice(&bs.device));
+  if (!bs.stream) CG_CUDA(cudaStreamCreateWithFlags(&bs.stream, cudaStreamNonBlocking));
+  cudaStream_t s = bs.stream;
+  const int P = int(sys.size());
+  bs.np = P;
+  bs.dims.assign(P, 0);
+  bs.kind.assign(P, 0);
+  bs.slot.assign(P, -1);
+  std::vector<std::unique_ptr<Hamiltonian>> hs(P);
+  auto t0 = std::chrono::steady_clock::now();
+  uint64_t ntot = 0, nnz = 0;
+  int nq = 0, nd = 0;
+  for (int p = 0; p < P; ++p) {
+    Basis b;
+    basis_build(*sys[p], b);
+    bs.dims[p] = b.n;
+    if (b.n == 0) continue;
+    hs[p] = std::make_unique<Hamiltonian>();
+    hamiltonian_build(*sys[p], *ops[p], b, CG_PREC_FP32, *hs[p]);
+    if (b.n <= uint64_t(kDense)) {
+      bs.kind[p] = 1;
+      bs.slot[p] = nd++;
+    } else {
+      bs.kind[p] = 2;
+      bs.slot[p] = nq++;
+      ntot += b.n;
+      nnz += hs[p]->nnz;
+    }
+  }
+  if (ntot >= (1ull << 32)) throw Error(CG_ERR_UNSUPPORTED, "batched rows beyond 2^32");
+  bs.nq = nq;
+  bs.nd = nd;
+  // block-diagonal FP32 (hi + lo) matrix of the Davidson problems
+  Hamiltonian& H = bs.H;
+  H.device = bs.device;
+  H.precision = CG_PREC_FP32;
+  H.n = ntot;
+  H.nnz = nnz;
+  H.rowptr.alloc(ntot + 1);
+  H.col.alloc(std::max<uint64_t>(nnz, 1));
+  H.hi.alloc(std::max<uint64_t>(nnz, 1));
+  H.lo.alloc(std::max<uint64_t>(nnz, 1));
+  H.diag.alloc(std::max<uint64_t>(ntot, 1));
+  std::vector<uint32_t> rowprob(ntot), pchunk(nq + 1, 0);
+  std::vector<BatchChunk> chunks;
+  bs.qrow0.assign(nq + 1, 0);
+  bs.qprob.assign(nq, 0);
+  uint64_t row = 0, e = 0;
+  for (int p = 0; p < P; ++p) {
+    if (bs.kind[p] != 2) continue;
+    const Hamiltonian& h = *hs[p];
+    const int q = bs.slot[p];
+    bs.qprob[q] = p;
+    bs.qrow0[q] = row;
+    k_concat_rows<<<nblk(h.n), 256, 0, s>>>(h.n, h.rowptr.p, e, row, H.rowptr.p);
+    k_concat_cols<<<nblk(h.nnz), 256, 0, s>>>(h.nnz, h.col.p, uint32_t(row), H.col.p + e);
+    CG_CUDA(cudaMemcpyAsync(H.hi.p + e, h.hi.p, h.nnz * 4, cudaMemcpyDeviceToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(H.lo.p + e, h.lo.p, h.nnz * 4, cudaMemcpyDeviceToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(H.diag.p + row, h.diag.p, h.n * 8, cudaMemcpyDeviceToDevice, s));
+    count_launch(2);
+    pchunk[q] = uint32_t(chunks.size());
+    for (uint64_t r0 = 0; r0 < h.n; r0 += kTile)
+      chunks.push_back(BatchChunk{uint32_t(q), uint32_t(row + r0), uint32_t(row + std::min<uint64_t>(h.n, r0 + kTile))});
+    for (uint64_t i = 0; i < h.n; ++i) rowprob[row + i] = uint32_t(q);
+    row += h.n;
+    e += h.nnz;
+    CG_CUDA(cudaStreamSynchronize(s));  // h is released after its copy
+  }
+  pchunk[nq] = uint32_t(chunks.size());
+  bs.qrow0[nq] = row;
+  CG_CUDA(cudaMemcpyAsync(H.rowptr.p + ntot, &e, 8, cudaMemcpyHostToDevice, s));
+  bs.nchunks = int(chunks.size());
+  bs.chunks.upload(chunks, s);
+  bs.pchunk.upload(pchunk, s);
+  bs.rowprob.upload(rowprob, s);
+  bs.diag.alloc(std::max<uint64_t>(ntot, 1));
+  CG_CUDA(cudaMemcpyAsync(bs.diag.p, H.diag.p, ntot * 8, cudaMemcpyDeviceToDevice, s));
+  // host diagonal for the starting vectors
+  bs.h_diag.resize(ntot);
+  CG_CUDA(cudaMemcpyAsync(bs.h_diag.data(), H.diag.p, ntot * 8, cudaMemcpyDeviceToHost, s));
+  // dense matrices of the small problems
+  bs.dense.alloc(std::max<size_t>(size_t(nd) * kJac * kJac, 1));
+  bs.ddim.assign(nd, 0);
+  for (int p = 0; p < P; ++p) {
+    if (bs.kind[p] != 1) continue;
+    const Hamiltonian& h = *hs[p];
+    const int d = bs.slot[p];
+    bs.ddim[d] = int(h.n);
+    k_dense_fill<<<unsigned(h.n), 64, 0, s>>>(int(h.n), 0, h.rowptr.p, h.col.p, h.hi.p, h.lo.p,
+                                               bs.dense.p + size_t(d) * kJac * kJac);
+    count_launch();
+    CG_CUDA(cudaStreamSynchronize(s));
+  }
+  CG_CUDA(cudaGetLastError());
+  CG_CUDA(cudaStreamSynchronize(s));
+  bs.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
+  CG_CUDA(cudaFuncSetAttribute(k_bjacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kJacSmem)));
+  if (prm.nev < 1 || prm.nev > kMaxB) throw Error(CG_ERR_ARG, "batched solve: nstates must be in 1..8");
+  if (prm.block < prm.nev || prm.block > kMaxB) throw Error(CG_ERR_ARG, "batched solve: block must be in nstates..8");
+  if (prm.lim > kMaxLim || prm.keep < prm.block || prm.keep + prm.block > prm.lim)
+    throw Error(CG_ERR_ARG, "batched solve: need block <= keep, keep + block <= lim <= 40");
+  cudaStream_t s = bs.stream;
+  const int P = bs.np, nev = prm.nev;
+  res.eig.assign(size_t(P) * nev, std::nan(""));
+  res.resid.assign(size_t(P) * nev, std::nan(""));
+  res.nconv.assign(P, 0);
+  res.found.assign(P, 0);
+  auto t0 = std::chrono::steady_clock::now();
+  const uint64_t l0 = launch_counter();
+  // exact solves of the small problems (one launch)
+  std::vector<double> dw, dz;
+  if (bs.nd > 0) {
+    DBuf<double> w(size_t(bs.nd) * kJac), Z(size_t(bs.nd) * kJac * kJac);
+    DBuf<int> kd;
+    kd.upload(bs.ddim, s);
+    k_bjacobi<<<bs.nd, 256, kJacSmem, s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    dw.resize(size_t(bs.nd) * kJac);
+    CG_CUDA(cudaMemcpyAsync(dw.data(), w.p, dw.size() * 8, cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+  }
+  for (int p = 0; p < P; ++p) {
+    if (bs.kind[p] != 1) continue;
+    const int d = bs.slot[p], k = bs.ddim[d], m = std::min(k, nev);
+    for (int j = 0; j < m; ++j) {
+      res.eig[size_t(p) * nev + j] = dw[size_t(d) * kJac + j];
+      res.resid[size_t(p) * nev + j] = 0.0;
+    }
+    res.nconv[p] = m;
+    res.found[p] = m;
+  }
+  // lockstep Davidson of the others
+  if (bs.nq > 0) {
+    const int Q = bs.nq;
+    const int blk = prm.block;
+    BEngine<float> e32(bs, nev, blk, prm.lim, prm.keep);
+    // starting vectors: unit vectors at the nev lowest diagonal entries of each problem
+    std::vector<uint32_t> urows(size_t(Q) * blk);
+    for (int q = 0; q < Q; ++q) {
+      const uint64_t r0 = bs.qrow0[q], r1 = bs.qrow0[q + 1];
+      std::vector<uint32_t> idx(r1 - r0);
+      std::iota(idx.begin(), idx.end(), 0u);
+      std::partial_sort(idx.begin(), idx.begin() + blk, idx.end(), [&](uint32_t a, uint32_t c) {
+        return bs.h_diag[r0 + a] < bs.h_diag[r0 + c] || (bs.h_diag[r0 + a] == bs.h_diag[r0 + c] && a < c);
+      });
+      for (int j = 0; j < blk; ++j) urows[size_t(q) * blk + j] = uint32_t(r0 + idx[j]);
+    }
+    DBuf<uint32_t> du;
+    du.upload(urows, s);
+    k_bunits<<<nblk(size_t(Q) * blk), 256, 0, s>>>(Q, du.p, blk, e32.V.p, nullptr, prm.lim);
+    count_launch();
+    const double sw = std::max(prm.switch_resid, prm.tol_resid);
+    res.iterations32 = e32.run(sw, prm.maxiter, prm.use_graph);
+    res.graph_launches += e32.graph_launches;
+    res.graph_kernels = std::max(res.graph_kernels, e32.kernels_per_graph);
+    res.graph_kernel_launches += e32.graph_kernel_launches;
+    // FP64 phase from the FP32 Ritz vectors
+    BEngine<double> e64(bs, nev, blk, prm.lim, prm.keep);
+    e32.ritz_vectors(e64.V.p, prm.lim);  // FP32 Ritz vectors, widened, start the FP64 phase
+    e64.orthonormalise(0);
+    res.iterations64 = e64.run(prm.tol_resid, prm.maxiter, prm.use_graph);
+    res.graph_launches += e64.graph_launches;
+    res.graph_kernels = std::max(res.graph_kernels, e64.kernels_per_graph);
+    res.graph_kernel_launches += e64.graph_kernel_launches;
+    std::vector<double> w(size_t(Q) * kJac), rn(size_t(Q) * kMaxB);
+    std::vector<int> cv(Q);
+    CG_CUDA(cudaMemcpyAsync(w.data(), e64.w.p, w.size() * 8, cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaMemcpyAsync(rn.data(), e64.rnorm.p, rn.size() * 8, cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    for (int q = 0; q < Q; ++q) {
+      const int p = bs.qprob[q];
+      int c = 0;
+      for (int j = 0; j < nev; ++j) {
+        res.eig[size_t(p) * nev + j] = w[size_t(q) * kJac + j];
+        res.resid[size_t(p) * nev + j] = rn[size_t(q) * kMaxB + j];
+        c += rn[size_t(q) * kMaxB + j] <= prm.tol_resid;
+      }
+      res.nconv[p] = c;
+      res.found[p] = nev;
+    }
+    res.spmm_seconds = e32.iter_s + e64.iter_s;
+  }
+  res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  res.launches = launch_counter() - l0 + res.graph_kernel_launches;
+  count_launch(res.graph_kernel_launches);
+}
+
+}  // namespace cg

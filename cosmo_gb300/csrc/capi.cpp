@@ -15,6 +15,7 @@
 #include "davidson.h"
 #include "device.h"
 #include "model.h"
+#include "batched.h"
 #include "virtual.h"
 #include "xshljt.h"
 
@@ -28,6 +29,9 @@ struct cg_basis {
 };
 struct cg_hamiltonian {
   cg::Hamiltonian h;
+};
+struct cg_batch {
+  cg::BatchSet bs;
 };
 
 namespace {
@@ -380,6 +384,18 @@ cg_status cg_hamiltonian_write_hh(const cg_hamiltonian* h, const char* path) {
   });
 }
 
+cg_status cg_hamiltonian_read_hh(const char* path, int32_t precision, cg_hamiltonian** out) {
+  return guard([&] {
+    CG_NOT_NULL(path);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    require_device();
+    auto h = std::make_unique<cg_hamiltonian>();
+    cg::hamiltonian_read_hh(path, precision, h->h);
+    *out = h.release();
+  });
+}
+
 void* cg_hamiltonian_stream(const cg_hamiltonian* h) { return h ? static_cast<void*>(h->h.stream) : nullptr; }
 
 // ------------------------------------------------------------------ SpMM
@@ -438,6 +454,88 @@ cg_status cg_spmm_refine_static_max_rows(uint64_t* rows) {
   return guard([&] {
     CG_NOT_NULL(rows);
     *rows = cg::spmm_refine_static_max_rows();
+  });
+}
+
+cg_status cg_batch_create(const cg_problem* const* problems, int32_t count, cg_batch** out) {
+  return guard([&] {
+    CG_NOT_NULL(problems);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    if (count < 1) throw cg::Error(CG_ERR_ARG, "count must be >= 1");
+    require_device();
+    std::vector<const cg::System*> sys;
+    std::vector<const cg::Operator*> ops;
+    for (int i = 0; i < count; ++i) {
+      CG_NOT_NULL(problems[i]);
+      sys.push_back(&problems[i]->sys);
+      ops.push_back(&problems[i]->op);
+    }
+    auto b = std::make_unique<cg_batch>();
+    cg::batch_build(sys, ops, b->bs);
+    *out = b.release();
+  });
+}
+
+void cg_batch_destroy(cg_batch* b) { delete b; }
+
+cg_status cg_batch_defaults(cg_batch_params* prm) {
+  return guard([&] {
+    CG_NOT_NULL(prm);
+    cg::BatchParams d;
+    prm->nstates = d.nev;
+    prm->block = d.block;
+    prm->lim = d.lim;
+    prm->keep = d.keep;
+    prm->maxiter = d.maxiter;
+    prm->tol_resid = d.tol_resid;
+    prm->switch_resid = d.switch_resid;
+    prm->use_graph = d.use_graph ? 1 : 0;
+  });
+}
+
+cg_status cg_batch_dims(const cg_batch* b, uint64_t* dims) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(dims);
+    for (int p = 0; p < b->bs.np; ++p) dims[p] = b->bs.dims[p];
+  });
+}
+
+cg_status cg_batch_solve(cg_batch* b, const cg_batch_params* prm, double* eig, double* resid, int32_t* nconv,
+                         cg_batch_stats* stats) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(prm);
+    CG_NOT_NULL(eig);
+    same_device(b->bs.device);
+    cg::BatchParams p;
+    p.nev = prm->nstates;
+    p.block = prm->block;
+    p.lim = prm->lim;
+    p.keep = prm->keep;
+    p.maxiter = prm->maxiter;
+    p.tol_resid = prm->tol_resid;
+    p.switch_resid = prm->switch_resid;
+    p.use_graph = prm->use_graph != 0;
+    cg::BatchResult r;
+    cg::batch_solve(b->bs, p, r);
+    const int P = b->bs.np;
+    for (size_t i = 0; i < size_t(P) * p.nev; ++i) {
+      eig[i] = r.eig[i];
+      if (resid) resid[i] = r.resid[i];
+    }
+    if (nconv)
+      for (int i = 0; i < P; ++i) nconv[i] = r.nconv[i];
+    if (stats) {
+      stats->iterations_fp32 = r.iterations32;
+      stats->iterations_fp64 = r.iterations64;
+      stats->graph_launches = r.graph_launches;
+      stats->graph_kernels = r.graph_kernels;
+      stats->launches = r.launches;
+      stats->seconds = r.seconds;
+      stats->build_seconds = b->bs.build_seconds;
+    }
   });
 }
 

@@ -159,6 +159,8 @@ struct Hamiltonian {
 void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h);
 void hamiltonian_upper_rows(const Hamiltonian& h, uint64_t row0, uint64_t nrows, uint64_t* rowptr, uint32_t* cols,
                             double* vals);
+// stored H from a .HH file (both triangles rebuilt from the stored upper rows)
+void hamiltonian_read_hh(const std::string& path, int precision, Hamiltonian& h);
 
 // ------------------------------------------------------------------ SpMM
 // Row-interleaved operands: element (i, k) at x[i*ldx + k].

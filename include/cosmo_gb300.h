@@ -166,6 +166,10 @@ cg_status cg_hamiltonian_upper_rows(const cg_hamiltonian* h, uint64_t row0, uint
 /* .HH row-sparse file: uint64 n, then per row uint32 nz, uint64 ind[nz], double
  * elem[nz] (upper triangle incl. diagonal), PPMatrix::Write (include/sm/PPMatrix.cxx:413-465). */
 cg_status cg_hamiltonian_write_hh(const cg_hamiltonian* h, const char* path);
+/* A stored Hamiltonian from a .HH file (the davidson_vfile input: SparseMatrix::Read,
+ * include/tav/sparse.cxx:402-445; each off-diagonal pair stored once, applied to
+ * both triangles as SparseMatrix::TimesMatrix does, :274-291). */
+cg_status cg_hamiltonian_read_hh(const char* path, int32_t precision, cg_hamiltonian** out);
 /* Stream used by this handle's kernels (cudaStream_t), for event timing. */
 void* cg_hamiltonian_stream(const cg_hamiltonian* h);
 
@@ -267,6 +271,44 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates);
  * vectors (Davidson::InitVectors, include/kdav/cdavidson.cpp:386). */
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
                       double* eig, double* de, double* resid, double* vecs, cg_davidson_stats* stats);
+
+/* ------------------------------------------------------------- batches */
+/* Many independent problems solved together (no counterpart in the reference,
+ * which runs one system per DEXHVJTcsb call, davidson/DEXHVJTcsb.cpp:36-77):
+ * every basis and stored FP32 (hi + lo) H is built on the GPU and concatenated
+ * block-diagonally; problems of dimension <= 64 are diagonalised exactly by a
+ * batched Jacobi kernel, the others run one lockstep block Davidson (FP32
+ * vectors and products with FP64 projections to switch_resid, then FP64 with
+ * the hi + lo product to tol_resid) whose iterations are CUDA graphs covering
+ * all problems; a problem whose nstates residuals are below the tolerance is
+ * frozen (skipped by every later kernel) until the slowest one finishes. */
+typedef struct cg_batch cg_batch;
+typedef struct {
+  int32_t nstates;      /* eigenpairs per problem, 1..8 (default 5) */
+  int32_t block;        /* vectors added per iteration, nstates..8 (default 8) */
+  int32_t lim;          /* basis limit <= 40 (default 40) */
+  int32_t keep;         /* Ritz vectors kept at a restart, >= block (default 16) */
+  int32_t maxiter;      /* per precision phase (default 300) */
+  double tol_resid;     /* default 1e-5 */
+  double switch_resid;  /* default 1e-4 */
+  int32_t use_graph;    /* 1: replay captured CUDA graphs (default) */
+} cg_batch_params;
+typedef struct {
+  int32_t iterations_fp32, iterations_fp64;
+  uint64_t graph_launches;   /* iterations replayed as one graph launch each */
+  int32_t graph_kernels;     /* kernels in the largest iteration graph */
+  uint64_t launches;         /* kernel launches of the solve, graph replays included */
+  double seconds, build_seconds;
+} cg_batch_stats;
+cg_status cg_batch_create(const cg_problem* const* problems, int32_t count, cg_batch** out);
+void cg_batch_destroy(cg_batch* b);
+cg_status cg_batch_defaults(cg_batch_params* prm);
+/* dimension of each problem (count values) */
+cg_status cg_batch_dims(const cg_batch* b, uint64_t* dims);
+/* eig, resid: count * nstates (NaN where a problem has fewer states); nconv:
+ * per problem, states with resid <= tol_resid; stats may be NULL. */
+cg_status cg_batch_solve(cg_batch* b, const cg_batch_params* prm, double* eig, double* resid, int32_t* nconv,
+                         cg_batch_stats* stats);
 
 /* ----------------------------------------------------- spin and isospin */
 /* <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nstates (1..16) vectors of

@@ -12,6 +12,7 @@ the GPU build must reproduce:
   sha256 of (rowptr u64 | cols u32) plus every 97th row with values
 * y = H x from the reference SpMM for small cases
 * eigenvalues, eigenvalue changes and residual norms of the reference Davidson
+* the reference's .HH file (XHH+JJ): sha256 for small cases, bytes for one
 * <J-J+> and <T-T+> of the reference's eigenvectors (oracle/_ref/ref_jt, the
   XSHLJT computation) with those vectors for small cases, and the <state>
   nodes the reference XSHLJT writes
@@ -184,6 +185,22 @@ def jt_case(name: str, work: str, xml: str, nstates: int, manifest: dict, keep_v
     print(name, "jt", manifest[name]["ref_twoJ"])
 
 
+def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) -> None:
+    """The reference's .HH file (XHH+JJ, PPMatrix::Write): sha256, and the bytes
+    for one small case so the .HH reader can be pinned on the GPU machine."""
+    with open(os.path.join(work, name + ".hh.log"), "w") as log:
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XHH+JJ"), xml], cwd=work, stdin=subprocess.DEVNULL,
+                       stdout=log, stderr=subprocess.STDOUT, check=True)
+    hh = os.path.join(work, name + ".HH")
+    manifest[name]["ref_hh_sha256"] = sha(hh)
+    manifest[name]["ref_hh_bytes"] = os.path.getsize(hh)
+    if keep_bytes:
+        arrays = dict(np.load(os.path.join(HERE, name + ".npz")))
+        arrays["ref_hh"] = np.fromfile(hh, np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    print(name, "hh", manifest[name]["ref_hh_bytes"])
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -204,6 +221,8 @@ def main() -> None:
                                             parity=sysd.parity, jj=sysd.jj, seed=sysd.seed)
             if nst and full:
                 jt_case(name, work, xml, nst, manifest, keep_vecs=full)
+            if full:
+                hh_case(name, work, xml, manifest, keep_bytes=(name == "sd22m0s1"))
         for name, sysd in BASIS_CASES.items():
             if a.only and a.only != name:
                 continue
