@@ -155,6 +155,10 @@ __global__ void __launch_bounds__(256) k_xty_w(uint64_t n, const T* __restrict__
                                                double* __restrict__ part, uint64_t rows_per_warp) {
   const int lane = threadIdx.x & 31;
   const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  // Y rows as float4 when every row start is 16-byte aligned; the columns past
+  // J in the last float4 are zero-weighted below (yv beyond J only meets c0/c1
+  // of columns j >= J, which are never written out)
+  const bool vec_y = (reinterpret_cast<uintptr_t>(Y + yo) % 16 == 0) && (ldy % 4 == 0) && (J % 4 == 0);
   const uint64_t r0 = gw * rows_per_warp;
   const uint64_t r1 = min(n, r0 + rows_per_warp);
   const bool a0 = lane < K, a1 = lane + 32 < K;
@@ -172,6 +176,20 @@ __global__ void __launch_bounds__(256) k_xty_w(uint64_t n, const T* __restrict__
       x0[u] = (ok && a0) ? xr[lane] : T(0);
       x1[u] = (ok && a1) ? xr[lane + 32] : T(0);
       const T* yr = Y + (r + u) * ldy + yo;
+      if constexpr (sizeof(T) == 4 && JMAX % 4 == 0) {
+        if (vec_y) {  // J values of the row as 16-byte loads (broadcast across the warp)
+#pragma unroll
+          for (int j4 = 0; j4 < JMAX / 4; ++j4) {
+            const float4 v = (ok && 4 * j4 < J) ? __ldg(reinterpret_cast<const float4*>(yr) + j4)
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+            yv[u][4 * j4] = v.x;
+            yv[u][4 * j4 + 1] = v.y;
+            yv[u][4 * j4 + 2] = v.z;
+            yv[u][4 * j4 + 3] = v.w;
+          }
+          continue;
+        }
+      }
 #pragma unroll
       for (int j = 0; j < JMAX; ++j) yv[u][j] = (ok && j < J) ? __ldg(yr + j) : T(0);
     }
@@ -235,6 +253,51 @@ __global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx,
     __syncwarp();
     if (ok) Y[r * ldy + yo + j] = (beta == 0.0) ? t : fma(tb, old, t);
     __syncwarp();
+  }
+}
+
+// Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G, one thread per row, all J
+// outputs of the row in registers, G (alpha folded in) in shared memory read
+// as broadcast; X rows read 4 values at a time when 16-byte aligned.  A row is
+// read completely before it is written, so X and Y may alias.
+template <class T, int JMAX>
+__global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx, int xo, int K,
+                                                const double* __restrict__ G, T* Y, int ldy, int yo, int J,
+                                                double alpha, double beta, bool vec_x) {
+  __shared__ __align__(16) T gs[64 * JMAX];
+  for (int i = threadIdx.x; i < 64 * JMAX; i += blockDim.x) {
+    const int k = i / JMAX, j = i % JMAX;
+    gs[i] = (k < K && j < J) ? T(alpha * G[k * J + j]) : T(0);
+  }
+  __syncthreads();
+  const T tb = T(beta);
+  for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
+    T acc[JMAX];
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) acc[j] = T(0);
+    const T* xr = X + r * ldx + xo;
+    int k = 0;
+    if constexpr (sizeof(T) == 4) {
+      if (vec_x) {
+        for (; k + 4 <= K; k += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(xr + k);
+          const float xv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int j = 0; j < JMAX; ++j) acc[j] = fma(xv[u], gs[(k + u) * JMAX + j], acc[j]);
+        }
+      }
+    }
+    for (; k < K; ++k) {
+      const T xv = xr[k];
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) acc[j] = fma(xv, gs[k * JMAX + j], acc[j]);
+    }
+    T* yr = Y + r * ldy + yo;
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j)
+      if (j < J) yr[j] = (beta == 0.0) ? acc[j] : fma(tb, yr[j], acc[j]);
   }
 }
 
@@ -557,10 +620,17 @@ struct Engine {
   // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
-    int JP = 1;
-    while (JP < J) JP <<= 1;
-    unsigned grid = unsigned(std::min<uint64_t>((n * JP + 255) / 256, uint64_t(nsm_) * 8));
-    k_gemm_s<T><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, JP, alpha, beta);
+    const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 16 == 0 && L % 4 == 0;
+    const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
+    if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
+    else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
+    else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
+    else {
+      int JP = 1;
+      while (JP < J) JP <<= 1;
+      unsigned g2 = unsigned(std::min<uint64_t>((n * JP + 255) / 256, uint64_t(nsm_) * 8));
+      k_gemm_s<T><<<g2, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, JP, alpha, beta);
+    }
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));  // G's staging buffer is reused by the next call
