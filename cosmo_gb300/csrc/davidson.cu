@@ -256,6 +256,145 @@ __global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx,
   }
 }
 
+// X^T Y with the Y sub-block of each 64-row chunk staged in shared memory:
+// the warp first copies the chunk's J columns of Y (coalesced: lane groups of
+// J read consecutive rows), then lane l owns columns l and l + 32 of X and
+// reads the J values of a row as shared-memory broadcasts.  FP32 products are
+// summed over the chunk and the chunks in FP64; per-warp partials go to
+// part[warp][k * J + j].  Any column offset yo (no alignment needed).
+template <class T, int JMAX>
+__global__ void __launch_bounds__(256) k_xty_t(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
+                                               const T* __restrict__ Y, int ldy, int yo, int J,
+                                               double* __restrict__ part, uint64_t rows_per_warp) {
+  constexpr int CH = 64;
+  __shared__ __align__(16) T ys[8][CH * JMAX];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t r0 = gw * rows_per_warp;
+  const uint64_t r1 = min(n, r0 + rows_per_warp);
+  const bool a0 = lane < K, a1 = lane + 32 < K;
+  T* yw = ys[wl];
+  double d0[JMAX], d1[JMAX];
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) { d0[j] = 0.0; d1[j] = 0.0; }
+  for (uint64_t c0 = r0; c0 < r1; c0 += CH) {
+    const int rows = int(min(uint64_t(CH), r1 - c0));
+    __syncwarp();
+    for (int i = lane; i < CH * JMAX; i += 32) {
+      const int rr = i / JMAX, j = i - rr * JMAX;
+      yw[i] = (rr < rows && j < J) ? Y[(c0 + rr) * ldy + yo + j] : T(0);
+    }
+    __syncwarp();
+    T c0v[JMAX], c1v[JMAX];
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) { c0v[j] = T(0); c1v[j] = T(0); }
+    for (int rr = 0; rr < rows; rr += 2) {
+      const T* xr0 = X + (c0 + rr) * ldx + xo;
+      const bool ok1 = rr + 1 < rows;
+      const T xa0 = a0 ? xr0[lane] : T(0);
+      const T xb0 = (a0 && ok1) ? xr0[ldx + lane] : T(0);
+      T xa1 = T(0), xb1 = T(0);
+      if (a1) {
+        xa1 = xr0[lane + 32];
+        xb1 = ok1 ? xr0[ldx + lane + 32] : T(0);
+      }
+      const T* ya = yw + rr * JMAX;
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) {
+        const T va = ya[j], vb = ya[JMAX + j];
+        c0v[j] = fma(xa0, va, fma(xb0, vb, c0v[j]));
+        c1v[j] = fma(xa1, va, fma(xb1, vb, c1v[j]));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) { d0[j] += double(c0v[j]); d1[j] += double(c1v[j]); }
+  }
+  double* out = part + gw * uint64_t(K * J);
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) {
+    if (j < J) {
+      if (a0) out[lane * J + j] = d0[j];
+      if (a1) out[(lane + 32) * J + j] = d1[j];
+    }
+  }
+}
+
+// R[:, c] = AB s_c - lam_c B s_c for C candidates, one thread per row with the
+// row read 4 values at a time, s in shared memory; per-CTA partial |R[:, c]|^2
+// (FP32 over a thread's rows, FP64 across threads, fixed order).
+template <class T, int CMAX>
+__global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
+                                                 int ld, int K, const double* __restrict__ Sc,
+                                                 const double* __restrict__ lam, int C, T* __restrict__ R, int ldr,
+                                                 double* __restrict__ part, bool vec) {
+  __shared__ __align__(16) T ss[64 * CMAX];
+  __shared__ T ls[CMAX];
+  __shared__ double red[8][CMAX];
+  for (int i = threadIdx.x; i < 64 * CMAX; i += blockDim.x) {
+    const int k = i / CMAX, c = i % CMAX;
+    ss[i] = (k < K && c < C) ? T(Sc[k * C + c]) : T(0);
+  }
+  for (int i = threadIdx.x; i < CMAX; i += blockDim.x) ls[i] = i < C ? T(lam[i]) : T(0);
+  __syncthreads();
+  T nrm[CMAX];
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) nrm[c] = T(0);
+  for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
+    T a[CMAX], b[CMAX];
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c) { a[c] = T(0); b[c] = T(0); }
+    const T* br = B + r * ld;
+    const T* abr = AB + r * ld;
+    int k = 0;
+    if constexpr (sizeof(T) == 4) {
+      if (vec) {
+        for (; k + 4 <= K; k += 4) {
+          const float4 bv = *reinterpret_cast<const float4*>(br + k);
+          const float4 av = *reinterpret_cast<const float4*>(abr + k);
+          const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, aa[4] = {av.x, av.y, av.z, av.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int c = 0; c < CMAX; ++c) {
+              const T sv = ss[(k + u) * CMAX + c];
+              a[c] = fma(aa[u], sv, a[c]);
+              b[c] = fma(bb[u], sv, b[c]);
+            }
+        }
+      }
+    }
+    for (; k < K; ++k) {
+      const T bv = br[k], av = abr[k];
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) {
+        a[c] = fma(av, ss[k * CMAX + c], a[c]);
+        b[c] = fma(bv, ss[k * CMAX + c], b[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c)
+      if (c < C) {
+        const T res = a[c] - ls[c] * b[c];
+        R[r * ldr + c] = res;
+        nrm[c] = fma(res, res, nrm[c]);
+      }
+  }
+  // CTA partials: warp shuffles then the 8 warps in order
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    double v = double(nrm[c]);
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+    if (lane == 0) red[w][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < C) {
+    double v = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) v += red[i][threadIdx.x];
+    part[uint64_t(blockIdx.x) * C + threadIdx.x] = v;
+  }
+}
+
 // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G, one thread per row, all J
 // outputs of the row in registers, G (alpha folded in) in shared memory read
 // as broadcast; X rows read 4 values at a time when 16-byte aligned.  A row is
@@ -579,7 +718,7 @@ struct Engine {
     xrows_ = (xrows_ + 3) / 4 * 4;
     xwarps_ = std::max<uint64_t>(8, (n + xrows_ - 1) / xrows_);
     xwarps_ = (xwarps_ + 7) / 8 * 8;
-    part.alloc(std::max<size_t>(std::max<size_t>(size_t(nparts) * kMaxK * kMaxJ, size_t(nsm * 4) * kMaxC),
+    part.alloc(std::max<size_t>(std::max<size_t>(size_t(nparts) * kMaxK * kMaxJ, size_t(nsm * 8) * kMaxC),
                                 size_t(xwarps_) * 64 * 16));
     small.alloc(kMaxK * kMaxK);
     small2.alloc(kMaxK * kMaxK);
@@ -605,8 +744,8 @@ struct Engine {
     if (K == 0 || J == 0) { G.assign(size_t(K) * J, 0.0); return; }
     if (J > 16 || K > 64) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
     const unsigned blocks = unsigned(xwarps_ / 8);
-    if (J <= 4) k_xty_w<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
-    else if (J <= 8) k_xty_w<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    if (J <= 4) k_xty_t<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    else if (J <= 8) k_xty_t<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     else k_xty_w<T, 16><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     CG_CUDA(cudaGetLastError());
     count_launch();
@@ -732,9 +871,12 @@ struct Engine {
     }
     CG_CUDA(cudaMemcpyAsync(small2.p, Sc.data(), sizeof(double) * Sc.size(), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s));
-    const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 4));
-    if (C <= 8) k_resid_s<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
-    else k_resid_s<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+    const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
+    const bool vec = L % 4 == 0;
+    if (C <= 8)
+      k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
+    else
+      k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
     CG_CUDA(cudaGetLastError());
     count_launch();
     k_reduce_parts<<<C, 128, 0, s>>>(part.p, int(rgrid), C, small.p);
