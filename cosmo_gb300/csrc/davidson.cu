@@ -288,22 +288,25 @@ __global__ void __launch_bounds__(256) k_xty_t(uint64_t n, const T* __restrict__
     T c0v[JMAX], c1v[JMAX];
 #pragma unroll
     for (int j = 0; j < JMAX; ++j) { c0v[j] = T(0); c1v[j] = T(0); }
-    for (int rr = 0; rr < rows; rr += 2) {
+    constexpr int U = 4;  // rows of X loads in flight per lane
+    for (int rr = 0; rr < rows; rr += U) {
       const T* xr0 = X + (c0 + rr) * ldx + xo;
-      const bool ok1 = rr + 1 < rows;
-      const T xa0 = a0 ? xr0[lane] : T(0);
-      const T xb0 = (a0 && ok1) ? xr0[ldx + lane] : T(0);
-      T xa1 = T(0), xb1 = T(0);
-      if (a1) {
-        xa1 = xr0[lane + 32];
-        xb1 = ok1 ? xr0[ldx + lane + 32] : T(0);
-      }
-      const T* ya = yw + rr * JMAX;
+      T xa[U], xb[U];
 #pragma unroll
-      for (int j = 0; j < JMAX; ++j) {
-        const T va = ya[j], vb = ya[JMAX + j];
-        c0v[j] = fma(xa0, va, fma(xb0, vb, c0v[j]));
-        c1v[j] = fma(xa1, va, fma(xb1, vb, c1v[j]));
+      for (int u = 0; u < U; ++u) {
+        const bool ok = rr + u < rows;
+        xa[u] = (a0 && ok) ? xr0[u * ldx + lane] : T(0);
+        xb[u] = (a1 && ok) ? xr0[u * ldx + lane + 32] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const T* ya = yw + (rr + u) * JMAX;
+#pragma unroll
+        for (int j = 0; j < JMAX; ++j) {
+          const T v = ya[j];
+          c0v[j] = fma(xa[u], v, c0v[j]);
+          c1v[j] = fma(xb[u], v, c1v[j]);
+        }
       }
     }
 #pragma unroll
@@ -592,9 +595,11 @@ __global__ void k_precond_copy(uint64_t n, const T* __restrict__ R, int ldr, con
   if (idx >= n * A) return;
   uint64_t i = idx / A;
   int a = int(idx - i * A);
-  double g = lam[a] - diag[i];
-  if (!(fabs(g) > 1e-13)) g = 1e-13;
-  B[i * ld + bo + a] = T(double(R[i * ldr + sel[a]]) / g);
+  // the difference in FP64 (theta and diag agree to many digits near
+  // convergence), the division in the vectors' precision
+  T g = T(lam[a] - diag[i]);
+  if (!(fabs(g) > T(1e-13))) g = T(1e-13);
+  B[i * ld + bo + a] = R[i * ldr + sel[a]] / g;
 }
 
 template <class T>
@@ -603,7 +608,7 @@ __global__ void k_scale_cols(uint64_t n, T* __restrict__ B, int ld, int bo, int 
   if (idx >= n * J) return;
   uint64_t i = idx / J;
   int j = int(idx - i * J);
-  B[i * ld + bo + j] = T(double(B[i * ld + bo + j]) * sc[j]);
+  B[i * ld + bo + j] = B[i * ld + bo + j] * T(sc[j]);
 }
 
 template <class T>
