@@ -62,7 +62,8 @@ class DavidsonParams(C.Structure):
                 ("crite", C.c_double), ("critc", C.c_double), ("critr", C.c_double), ("ortho", C.c_double),
                 ("tol_resid", C.c_double), ("switch_resid", C.c_double), ("precision", C.c_int32),
                 ("verbose", C.c_int32), ("ortho_block", C.c_int32), ("algorithm", C.c_int32),
-                ("keep", C.c_int32), ("precond", C.c_int32)]
+                ("keep", C.c_int32), ("precond", C.c_int32), ("refine_lim", C.c_int32),
+                ("refine_keep", C.c_int32)]
 
 
 class BatchParams(C.Structure):
@@ -470,7 +471,7 @@ def davidson_diagonalization(h: Hamiltonian, nstates: int = 10, want_vectors: bo
 
     Keyword arguments set :class:`DavidsonParams` fields (block, lim, maxiter,
     crite, critc, critr, ortho, tol_resid, switch_resid, precision, verbose,
-    ortho_block, algorithm, keep, precond).  precision defaults to the matrix
+    ortho_block, algorithm, keep, precond, refine_lim, refine_keep).  precision defaults to the matrix
     precision."""
     kw.setdefault("precision", h.precision)
     p = davidson_params(nstates, **kw)

@@ -627,6 +627,8 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   prm->algorithm = -1;
   prm->keep = 0;
   prm->precond = 1;
+  prm->refine_lim = 0;
+  prm->refine_keep = 0;
 }
 
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
@@ -681,6 +683,13 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
       rq.phase1 = c1;
       cg::DavConfig c2 = c;
       c2.spmm_prec = CG_PREC_REFINE;
+      if (prm->refine_lim > 0) {
+        if (prm->refine_lim <= nume || prm->refine_lim > 64)
+          throw cg::Error(CG_ERR_ARG, "refine_lim must be in nstates+1..64");
+        c2.lim = prm->refine_lim;
+      }
+      if (prm->refine_keep > 0) c2.keep = prm->refine_keep;
+      if (c2.keep + c2.block > c2.lim) c2.keep = std::max(nume, c2.lim - c2.block);
 
       rq.phase2 = c2;
       rq.refine = true;

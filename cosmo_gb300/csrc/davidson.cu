@@ -266,7 +266,7 @@ template <class T, int JMAX>
 __global__ void __launch_bounds__(256) k_xty_t(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
                                                const T* __restrict__ Y, int ldy, int yo, int J,
                                                double* __restrict__ part, uint64_t rows_per_warp) {
-  constexpr int CH = 64;
+  constexpr int CH = JMAX * sizeof(T) > 32 ? 32 : 64;  // staged rows per chunk (<= 32 KB per CTA)
   __shared__ __align__(16) T ys[8][CH * JMAX];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -769,6 +769,7 @@ struct Engine {
     if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
+    else if (J <= 32) k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else {
       int JP = 1;
       while (JP < J) JP <<= 1;

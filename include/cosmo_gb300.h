@@ -252,6 +252,8 @@ typedef struct {
                         re-checked each iteration, restarts keep `keep` Ritz vectors */
   int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates) */
   int32_t precond;   /* algorithm 1: 1 = diagonal preconditioner (lambda - H_ii), 0 = none */
+  int32_t refine_lim;   /* mixed solve: basis limit of the FP64 refinement phase (0: lim) */
+  int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep) */
 } cg_davidson_params;
 
 typedef struct {
