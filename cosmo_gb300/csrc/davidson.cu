@@ -256,6 +256,179 @@ __global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx,
   }
 }
 
+// ---- double-float arithmetic for the FP64 engine --------------------------
+// GB300 runs FP64 at ~1/64 of the FP32 rate, so the FP64 engine's tall-skinny
+// products split every FP64 operand once into an FP32 pair (hi + lo) and
+// multiply-accumulate in double-float (products exact to 2^-48 via fma, sums
+// with a compensation term), which keeps ~44 bits and runs on the FP32 pipe.
+__device__ __forceinline__ void df_split(double d, float& h, float& l) {
+  h = __double2float_rn(d);
+  l = __double2float_rn(d - double(h));
+}
+// (sh, sl) += (ah + al) * (bh + bl), the al * bl term dropped
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  const float t = sh + p;
+  const float bb = t - sh;
+  float err = (sh - (t - bb)) + (p - bb);
+  err += sl + e;
+  sh = t + err;
+  sl = err - (sh - t);
+}
+
+// X^T Y of the FP64 engine in double-float: as k_xty_t, with the staged Y chunk
+// held as FP32 pairs and 32-row chunks summed in double-float, then in FP64.
+template <int JMAX>
+__global__ void __launch_bounds__(256) k_xty_df(uint64_t n, const double* __restrict__ X, int ldx, int xo, int K,
+                                                const double* __restrict__ Y, int ldy, int yo, int J,
+                                                double* __restrict__ part, uint64_t rows_per_warp) {
+  constexpr int CH = 32;
+  __shared__ __align__(16) float yh[8][CH * JMAX], yl[8][CH * JMAX];
+  __shared__ double dsh[8][2 * JMAX][32];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t r0 = gw * rows_per_warp;
+  const uint64_t r1 = min(n, r0 + rows_per_warp);
+  const bool a0 = lane < K, a1 = lane + 32 < K;
+#pragma unroll
+  for (int j = 0; j < 2 * JMAX; ++j) dsh[wl][j][lane] = 0.0;
+  for (uint64_t c0 = r0; c0 < r1; c0 += CH) {
+    const int rows = int(min(uint64_t(CH), r1 - c0));
+    __syncwarp();
+    for (int i = lane; i < CH * JMAX; i += 32) {
+      const int rr = i / JMAX, j = i - rr * JMAX;
+      const double v = (rr < rows && j < J) ? Y[(c0 + rr) * ldy + yo + j] : 0.0;
+      df_split(v, yh[wl][i], yl[wl][i]);
+    }
+    __syncwarp();
+    float c0h[JMAX], c0l[JMAX], c1h[JMAX], c1l[JMAX];
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) { c0h[j] = c0l[j] = c1h[j] = c1l[j] = 0.f; }
+    for (int rr = 0; rr < rows; ++rr) {
+      const double* xr = X + (c0 + rr) * ldx + xo;
+      float xah = 0.f, xal = 0.f, xbh = 0.f, xbl = 0.f;
+      if (a0) df_split(xr[lane], xah, xal);
+      if (a1) df_split(xr[lane + 32], xbh, xbl);
+      const float* yhr = yh[wl] + rr * JMAX;
+      const float* ylr = yl[wl] + rr * JMAX;
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) {
+        df_mac(c0h[j], c0l[j], xah, xal, yhr[j], ylr[j]);
+        if (a1) df_mac(c1h[j], c1l[j], xbh, xbl, yhr[j], ylr[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) {
+      dsh[wl][j][lane] += double(c0h[j]) + double(c0l[j]);
+      dsh[wl][JMAX + j][lane] += double(c1h[j]) + double(c1l[j]);
+    }
+  }
+  double* out = part + gw * uint64_t(K * J);
+#pragma unroll
+  for (int j = 0; j < JMAX; ++j) {
+    if (j < J) {
+      if (a0) out[lane * J + j] = dsh[wl][j][lane];
+      if (a1) out[(lane + 32) * J + j] = dsh[wl][JMAX + j][lane];
+    }
+  }
+}
+
+// R = AB s_c - lam_c B s_c of the FP64 engine in double-float, one thread per
+// row; s and lam as FP32 pairs in shared memory; R and the norms in FP64.
+template <int CMAX>
+__global__ void __launch_bounds__(256) k_resid_df(uint64_t n, const double* __restrict__ B,
+                                                  const double* __restrict__ AB, int ld, int K,
+                                                  const double* __restrict__ Sc, const double* __restrict__ lam, int C,
+                                                  double* __restrict__ R, int ldr, double* __restrict__ part) {
+  __shared__ float sh_[64 * CMAX], sl_[64 * CMAX];
+  __shared__ double ls[CMAX];
+  __shared__ double red[8][CMAX];
+  for (int i = threadIdx.x; i < 64 * CMAX; i += blockDim.x) {
+    const int k = i / CMAX, c = i % CMAX;
+    df_split((k < K && c < C) ? Sc[k * C + c] : 0.0, sh_[i], sl_[i]);
+  }
+  for (int i = threadIdx.x; i < CMAX; i += blockDim.x) ls[i] = i < C ? lam[i] : 0.0;
+  __syncthreads();
+  double nrm[CMAX];
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) nrm[c] = 0.0;
+  for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
+    float ah[CMAX], al[CMAX], bh[CMAX], bl[CMAX];
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c) { ah[c] = al[c] = bh[c] = bl[c] = 0.f; }
+    const double* br = B + r * ld;
+    const double* abr = AB + r * ld;
+    for (int k = 0; k < K; ++k) {
+      float xbh, xbl, xah, xal;
+      df_split(br[k], xbh, xbl);
+      df_split(abr[k], xah, xal);
+#pragma unroll
+      for (int c = 0; c < CMAX; ++c) {
+        const float s0 = sh_[k * CMAX + c], s1 = sl_[k * CMAX + c];
+        df_mac(ah[c], al[c], xah, xal, s0, s1);
+        df_mac(bh[c], bl[c], xbh, xbl, s0, s1);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c)
+      if (c < C) {
+        const double res = (double(ah[c]) + double(al[c])) - ls[c] * (double(bh[c]) + double(bl[c]));
+        R[r * ldr + c] = res;
+        nrm[c] += res * res;
+      }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < CMAX; ++c) {
+    double v = nrm[c];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+    if (lane == 0) red[w][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < C) {
+    double v = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) v += red[i][threadIdx.x];
+    part[uint64_t(blockIdx.x) * C + threadIdx.x] = v;
+  }
+}
+
+// Y = beta Y + alpha X G of the FP64 engine in double-float: one thread per
+// row, alpha G as FP32 pairs in shared memory, outputs combined in FP64.  A row
+// is read completely before it is written (X and Y may alias).
+template <int JMAX>
+__global__ void __launch_bounds__(256) k_gemm_df(uint64_t n, const double* X, int ldx, int xo, int K,
+                                                 const double* __restrict__ G, double* Y, int ldy, int yo, int J,
+                                                 double alpha, double beta) {
+  __shared__ float gh[64 * JMAX], gl[64 * JMAX];
+  for (int i = threadIdx.x; i < 64 * JMAX; i += blockDim.x) {
+    const int k = i / JMAX, j = i % JMAX;
+    df_split((k < K && j < J) ? alpha * G[k * J + j] : 0.0, gh[i], gl[i]);
+  }
+  __syncthreads();
+  for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
+    float ah[JMAX], al[JMAX];
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j) { ah[j] = 0.f; al[j] = 0.f; }
+    const double* xr = X + r * ldx + xo;
+    for (int k = 0; k < K; ++k) {
+      float xh, xl;
+      df_split(xr[k], xh, xl);
+#pragma unroll
+      for (int j = 0; j < JMAX; ++j) df_mac(ah[j], al[j], xh, xl, gh[k * JMAX + j], gl[k * JMAX + j]);
+    }
+    double* yr = Y + r * ldy + yo;
+#pragma unroll
+    for (int j = 0; j < JMAX; ++j)
+      if (j < J) {
+        const double v = double(ah[j]) + double(al[j]);
+        yr[j] = beta == 0.0 ? v : fma(beta, yr[j], v);
+      }
+  }
+}
+
 // X^T Y with the Y sub-block of each 64-row chunk staged in shared memory:
 // the warp first copies the chunk's J columns of Y (coalesced: lane groups of
 // J read consecutive rows), then lane l owns columns l and l + 32 of X and
@@ -263,20 +436,21 @@ __global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx,
 // summed over the chunk and the chunks in FP64; per-warp partials go to
 // part[warp][k * J + j].  Any column offset yo (no alignment needed).
 template <class T, int JMAX>
-__global__ void __launch_bounds__(256) k_xty_t(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
+__global__ void __launch_bounds__(256, 4) k_xty_t(uint64_t n, const T* __restrict__ X, int ldx, int xo, int K,
                                                const T* __restrict__ Y, int ldy, int yo, int J,
                                                double* __restrict__ part, uint64_t rows_per_warp) {
   constexpr int CH = JMAX * sizeof(T) > 32 ? 32 : 64;  // staged rows per chunk (<= 32 KB per CTA)
   __shared__ __align__(16) T ys[8][CH * JMAX];
+  // FP64 chunk sums of lane l, column j at dsh[warp][j][l] (x0) and [JMAX + j][l] (x1)
+  __shared__ double dsh[8][2 * JMAX][32];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t r0 = gw * rows_per_warp;
   const uint64_t r1 = min(n, r0 + rows_per_warp);
   const bool a0 = lane < K, a1 = lane + 32 < K;
   T* yw = ys[wl];
-  double d0[JMAX], d1[JMAX];
 #pragma unroll
-  for (int j = 0; j < JMAX; ++j) { d0[j] = 0.0; d1[j] = 0.0; }
+  for (int j = 0; j < 2 * JMAX; ++j) dsh[wl][j][lane] = 0.0;
   for (uint64_t c0 = r0; c0 < r1; c0 += CH) {
     const int rows = int(min(uint64_t(CH), r1 - c0));
     __syncwarp();
@@ -310,14 +484,17 @@ __global__ void __launch_bounds__(256) k_xty_t(uint64_t n, const T* __restrict__
       }
     }
 #pragma unroll
-    for (int j = 0; j < JMAX; ++j) { d0[j] += double(c0v[j]); d1[j] += double(c1v[j]); }
+    for (int j = 0; j < JMAX; ++j) {
+      dsh[wl][j][lane] += double(c0v[j]);
+      dsh[wl][JMAX + j][lane] += double(c1v[j]);
+    }
   }
   double* out = part + gw * uint64_t(K * J);
 #pragma unroll
   for (int j = 0; j < JMAX; ++j) {
     if (j < J) {
-      if (a0) out[lane * J + j] = d0[j];
-      if (a1) out[(lane + 32) * J + j] = d1[j];
+      if (a0) out[lane * J + j] = dsh[wl][j][lane];
+      if (a1) out[(lane + 32) * J + j] = dsh[wl][JMAX + j][lane];
     }
   }
 }
@@ -749,7 +926,11 @@ struct Engine {
     if (K == 0 || J == 0) { G.assign(size_t(K) * J, 0.0); return; }
     if (J > 16 || K > 64) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
     const unsigned blocks = unsigned(xwarps_ / 8);
-    if (J <= 4) k_xty_t<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    if constexpr (sizeof(T) == 8) {
+      if (J <= 4) k_xty_df<4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      else if (J <= 8) k_xty_df<8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      else k_xty_w<T, 16><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+    } else if (J <= 4) k_xty_t<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     else if (J <= 8) k_xty_t<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     else k_xty_w<T, 16><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     CG_CUDA(cudaGetLastError());
@@ -766,6 +947,19 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 16 == 0 && L % 4 == 0;
     const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
+    if constexpr (sizeof(T) == 8) {
+      if (J <= 32) {
+        const double* Xd = reinterpret_cast<const double*>(Xp);
+        double* Yd = reinterpret_cast<double*>(Yp);
+        if (J <= 8) k_gemm_df<8><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
+        else if (J <= 16) k_gemm_df<16><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
+        else k_gemm_df<32><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
+        CG_CUDA(cudaGetLastError());
+        count_launch();
+        CG_CUDA(cudaStreamSynchronize(s));
+        return;
+      }
+    }
     if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
@@ -879,7 +1073,12 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s));
     const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     const bool vec = L % 4 == 0;
-    if (C <= 8)
+    if constexpr (sizeof(T) == 8) {
+      if (C <= 8)
+        k_resid_df<8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+      else
+        k_resid_df<16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+    } else if (C <= 8)
       k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
     else
       k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
