@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "batched.h"
+#include "dfloat.h"
 #include "dense.h"
 
 namespace cg {
@@ -191,56 +192,84 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
 
 // ------------------------------------------------ segmented tall-skinny ops
 // Per-tile partials of G = X[:, xo:xo+K]^T Y[:, yo:yo+J]: one CTA per tile (rows
-// of one problem), warp w takes every 8th 64-row chunk of the tile, lane owns
-// columns lane and lane + 32 of X; products are summed in T over a 64-row chunk
-// and the chunks in FP64 (FP32 products with FP64 sums for the FP32 engine),
-// then the 8 warps are added in a fixed order.
+// of one problem), warp w takes every 8th chunk of the tile; the chunk's J
+// columns of Y are staged in shared memory, lane l owns columns l and l + 32 of
+// X with four rows of loads in flight.  FP32 engine: FP32 products summed over
+// a 64-row chunk, chunks in FP64.  FP64 engine: double-float products (FP64
+// operands split once into FP32 pairs) summed over a 32-row chunk, chunks in
+// FP64.  The 8 warps are added in a fixed order.
 template <class T>
 __global__ void __launch_bounds__(256) k_bxty(const BatchChunk* __restrict__ tiles, const T* __restrict__ X, int ldx,
                                               int xo, int K, const T* __restrict__ Y, int ldy, int yo, int J,
                                               double* __restrict__ part, const int* __restrict__ fz) {
+  constexpr bool DF = sizeof(T) == 8;
+  constexpr int CH = DF ? 32 : kChunk;
   __shared__ double red[8][kMaxLim * kMaxB];
+  __shared__ __align__(16) float yh[8][CH * kMaxB];
+  __shared__ __align__(16) float yl[8][DF ? CH * kMaxB : 1];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const BatchChunk tl = tiles[blockIdx.x];
   if (fz[tl.prob]) return;
-  const bool two = K > 32;
-  double a0[kMaxB], a1[kMaxB];
+  const bool a0 = lane < K, a1 = lane + 32 < K;
+  double d0[kMaxB], d1[kMaxB];
 #pragma unroll
-  for (int j = 0; j < kMaxB; ++j) { a0[j] = 0.0; a1[j] = 0.0; }
-  for (uint32_t c0 = tl.row0 + uint32_t(w) * kChunk; c0 < tl.row1; c0 += 8u * kChunk) {
-    const uint32_t c1 = min(tl.row1, c0 + uint32_t(kChunk));
-    T s0[kMaxB], s1[kMaxB];
+  for (int j = 0; j < kMaxB; ++j) { d0[j] = 0.0; d1[j] = 0.0; }
+  for (uint32_t c0 = tl.row0 + uint32_t(w) * CH; c0 < tl.row1; c0 += 8u * CH) {
+    const int rows = int(min(tl.row1 - c0, uint32_t(CH)));
+    __syncwarp();
+    for (int i = lane; i < CH * kMaxB; i += 32) {
+      const int rr = i / kMaxB, j = i - rr * kMaxB;
+      const T v = (rr < rows && j < J) ? Y[size_t(c0 + rr) * ldy + yo + j] : T(0);
+      if constexpr (DF) df_split(double(v), yh[w][i], yl[w][i]);
+      else yh[w][i] = float(v);
+    }
+    __syncwarp();
+    float sh0[kMaxB], sh1[kMaxB], sl0[kMaxB], sl1[kMaxB];
 #pragma unroll
-    for (int j = 0; j < kMaxB; ++j) { s0[j] = T(0); s1[j] = T(0); }
-    for (uint32_t r = c0; r < c1; ++r) {
-      const T x0 = lane < K ? X[size_t(r) * ldx + xo + lane] : T(0);
-      const T* yr = Y + size_t(r) * ldy + yo;
-      if (two) {
-        const T x1 = lane + 32 < K ? X[size_t(r) * ldx + xo + lane + 32] : T(0);
+    for (int j = 0; j < kMaxB; ++j) { sh0[j] = sh1[j] = sl0[j] = sl1[j] = 0.f; }
+    for (int rr = 0; rr < rows; rr += 4) {
+      T xa[4], xb[4];
 #pragma unroll
-        for (int j = 0; j < kMaxB; ++j)
-          if (j < J) {
-            const T yv = yr[j];
-            s0[j] = fma(x0, yv, s0[j]);
-            s1[j] = fma(x1, yv, s1[j]);
+      for (int u = 0; u < 4; ++u) {
+        const bool ok = rr + u < rows;
+        const T* xr = X + size_t(c0 + rr + u) * ldx + xo;
+        xa[u] = (ok && a0) ? xr[lane] : T(0);
+        xb[u] = (ok && a1) ? xr[lane + 32] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float* yr = yh[w] + (rr + u) * kMaxB;
+        if constexpr (DF) {
+          const float* ylr = yl[w] + (rr + u) * kMaxB;
+          float ah, al, bh, bl;
+          df_split(double(xa[u]), ah, al);
+          df_split(double(xb[u]), bh, bl);
+#pragma unroll
+          for (int j = 0; j < kMaxB; ++j)
+            if (j < J) {
+              df_mac(sh0[j], sl0[j], ah, al, yr[j], ylr[j]);
+              if (a1) df_mac(sh1[j], sl1[j], bh, bl, yr[j], ylr[j]);
+            }
+        } else {
+#pragma unroll
+          for (int j = 0; j < kMaxB; ++j) {
+            sh0[j] = fmaf(float(xa[u]), yr[j], sh0[j]);
+            sh1[j] = fmaf(float(xb[u]), yr[j], sh1[j]);
           }
-      } else {
-#pragma unroll
-        for (int j = 0; j < kMaxB; ++j)
-          if (j < J) s0[j] = fma(x0, yr[j], s0[j]);
+        }
       }
     }
 #pragma unroll
     for (int j = 0; j < kMaxB; ++j) {
-      a0[j] += double(s0[j]);
-      if (two) a1[j] += double(s1[j]);
+      d0[j] += double(sh0[j]) + double(sl0[j]);
+      d1[j] += double(sh1[j]) + double(sl1[j]);
     }
   }
 #pragma unroll
   for (int j = 0; j < kMaxB; ++j)
     if (j < J) {
-      if (lane < K) red[w][lane * J + j] = a0[j];
-      if (lane + 32 < K) red[w][(lane + 32) * J + j] = a1[j];
+      if (a0) red[w][lane * J + j] = d0[j];
+      if (a1) red[w][(lane + 32) * J + j] = d1[j];
     }
   __syncthreads();
   for (int o = threadIdx.x; o < K * J; o += blockDim.x) {
@@ -287,28 +316,44 @@ __global__ void __launch_bounds__(256) k_bgemm(const BatchChunk* __restrict__ ti
                                                int K, const double* __restrict__ M, size_t mstride, int mld, T* Y,
                                                int ldy, int yo, int J, double alpha, double beta,
                                                const int* __restrict__ fz) {
-  __shared__ T Ms[kMaxLim * kMaxLim];
+  constexpr bool DF = sizeof(T) == 8;  // FP64 engine: double-float arithmetic
+  __shared__ float Mh[kMaxLim * kMaxLim];
+  __shared__ float Ml[DF ? kMaxLim * kMaxLim : 1];
   const BatchChunk tl = tiles[blockIdx.x];
   if (fz[tl.prob]) return;
   const double* Mq = M + size_t(tl.prob) * mstride;
-  for (int i = threadIdx.x; i < K * J; i += blockDim.x) Ms[i] = T(Mq[(i / J) * mld + (i % J)]);
+  for (int i = threadIdx.x; i < K * J; i += blockDim.x) {
+    const double v = alpha * Mq[(i / J) * mld + (i % J)];
+    if constexpr (DF) df_split(v, Mh[i], Ml[i]);
+    else Mh[i] = float(v);
+  }
   __syncthreads();
-  const T a = T(alpha), bt = T(beta);
   for (uint32_t r = tl.row0 + threadIdx.x; r < tl.row1; r += blockDim.x) {
-    T acc[kMaxLim];
+    float ah[kMaxLim], al[kMaxLim];
 #pragma unroll
-    for (int j = 0; j < kMaxLim; ++j) acc[j] = T(0);
+    for (int j = 0; j < kMaxLim; ++j) { ah[j] = 0.f; al[j] = 0.f; }
     const T* xr = X + size_t(r) * ldx + xo;
     for (int i = 0; i < K; ++i) {
-      const T xv = xr[i];
+      if constexpr (DF) {
+        float xh, xl;
+        df_split(double(xr[i]), xh, xl);
 #pragma unroll
-      for (int j = 0; j < kMaxLim; ++j)
-        if (j < J) acc[j] = fma(xv, Ms[i * J + j], acc[j]);
+        for (int j = 0; j < kMaxLim; ++j)
+          if (j < J) df_mac(ah[j], al[j], xh, xl, Mh[i * J + j], Ml[i * J + j]);
+      } else {
+        const float xv = float(xr[i]);
+#pragma unroll
+        for (int j = 0; j < kMaxLim; ++j)
+          if (j < J) ah[j] = fmaf(xv, Mh[i * J + j], ah[j]);
+      }
     }
     T* yr = Y + size_t(r) * ldy + yo;
 #pragma unroll
     for (int j = 0; j < kMaxLim; ++j)
-      if (j < J) yr[j] = beta == 0.0 ? a * acc[j] : bt * yr[j] + a * acc[j];
+      if (j < J) {
+        const T v = DF ? T(double(ah[j]) + double(al[j])) : T(ah[j]);
+        yr[j] = beta == 0.0 ? v : T(beta) * yr[j] + v;
+      }
   }
 }
 
@@ -319,27 +364,54 @@ __global__ void __launch_bounds__(256) k_bresid(const BatchChunk* __restrict__ t
                                                 const T* __restrict__ AV, int ld, int K, const double* __restrict__ w,
                                                 const double* __restrict__ Z, T* __restrict__ R, int ldr, int b,
                                                 const int* __restrict__ fz) {
-  __shared__ T Zs[kMaxLim * kMaxB];
-  __shared__ T th[kMaxB];
+  constexpr bool DF = sizeof(T) == 8;  // FP64 engine: double-float arithmetic
+  __shared__ float Zh[kMaxLim * kMaxB];
+  __shared__ float Zl[DF ? kMaxLim * kMaxB : 1];
+  __shared__ double th[kMaxB];
   const BatchChunk tl = tiles[blockIdx.x];
   if (fz[tl.prob]) return;
   const double* Zq = Z + size_t(tl.prob) * kJac * kJac;
-  for (int i = threadIdx.x; i < K * b; i += blockDim.x) Zs[i] = T(Zq[(i / b) * kJac + (i % b)]);
-  if (threadIdx.x < b) th[threadIdx.x] = T(w[size_t(tl.prob) * kJac + threadIdx.x]);
+  for (int i = threadIdx.x; i < K * b; i += blockDim.x) {
+    const double v = Zq[(i / b) * kJac + (i % b)];
+    if constexpr (DF) df_split(v, Zh[i], Zl[i]);
+    else Zh[i] = float(v);
+  }
+  if (threadIdx.x < b) th[threadIdx.x] = w[size_t(tl.prob) * kJac + threadIdx.x];
   __syncthreads();
   for (uint32_t r = tl.row0 + threadIdx.x; r < tl.row1; r += blockDim.x) {
-    T acc[kMaxB];
+    // AV z_j and V z_j separately, then R = AV z - theta V z
+    float ah[kMaxB], al[kMaxB], bh[kMaxB], bl[kMaxB];
 #pragma unroll
-    for (int j = 0; j < kMaxB; ++j) acc[j] = T(0);
+    for (int j = 0; j < kMaxB; ++j) { ah[j] = al[j] = bh[j] = bl[j] = 0.f; }
     for (int i = 0; i < K; ++i) {
       const T v = V[size_t(r) * ld + i], av = AV[size_t(r) * ld + i];
+      if constexpr (DF) {
+        float vh, vl, ach, acl;
+        df_split(double(v), vh, vl);
+        df_split(double(av), ach, acl);
 #pragma unroll
-      for (int j = 0; j < kMaxB; ++j)
-        if (j < b) acc[j] = fma(av - th[j] * v, Zs[i * b + j], acc[j]);
+        for (int j = 0; j < kMaxB; ++j)
+          if (j < b) {
+            df_mac(ah[j], al[j], ach, acl, Zh[i * b + j], Zl[i * b + j]);
+            df_mac(bh[j], bl[j], vh, vl, Zh[i * b + j], Zl[i * b + j]);
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < kMaxB; ++j)
+          if (j < b) {
+            ah[j] = fmaf(float(av), Zh[i * b + j], ah[j]);
+            bh[j] = fmaf(float(v), Zh[i * b + j], bh[j]);
+          }
+      }
     }
 #pragma unroll
     for (int j = 0; j < kMaxB; ++j)
-      if (j < b) R[size_t(r) * ldr + j] = acc[j];
+      if (j < b) {
+        if constexpr (DF)
+          R[size_t(r) * ldr + j] = T((double(ah[j]) + double(al[j])) - th[j] * (double(bh[j]) + double(bl[j])));
+        else
+          R[size_t(r) * ldr + j] = T(ah[j] - float(th[j]) * bh[j]);
+      }
   }
 }
 

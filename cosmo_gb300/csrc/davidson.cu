@@ -26,6 +26,7 @@
 #include <numeric>
 
 #include "davidson.h"
+#include "dfloat.h"
 #include "virtual.h"
 #include "dense.h"
 #include "device.h"
@@ -256,28 +257,7 @@ __global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx,
   }
 }
 
-// ---- double-float arithmetic for the FP64 engine --------------------------
-// GB300 runs FP64 at ~1/64 of the FP32 rate, so the FP64 engine's tall-skinny
-// products split every FP64 operand once into an FP32 pair (hi + lo) and
-// multiply-accumulate in double-float (products exact to 2^-48 via fma, sums
-// with a compensation term), which keeps ~44 bits and runs on the FP32 pipe.
-__device__ __forceinline__ void df_split(double d, float& h, float& l) {
-  h = __double2float_rn(d);
-  l = __double2float_rn(d - double(h));
-}
-// (sh, sl) += (ah + al) * (bh + bl), the al * bl term dropped
-__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
-  const float p = ah * bh;
-  float e = fmaf(ah, bh, -p);
-  e = fmaf(ah, bl, e);
-  e = fmaf(al, bh, e);
-  const float t = sh + p;
-  const float bb = t - sh;
-  float err = (sh - (t - bb)) + (p - bb);
-  err += sl + e;
-  sh = t + err;
-  sl = err - (sh - t);
-}
+// ---- double-float arithmetic for the FP64 engine (dfloat.h) ----------------
 
 // X^T Y of the FP64 engine in double-float: as k_xty_t, with the staged Y chunk
 // held as FP32 pairs and 32-row chunks summed in double-float, then in FP64.
@@ -926,9 +906,14 @@ struct Engine {
     if (K == 0 || J == 0) { G.assign(size_t(K) * J, 0.0); return; }
     if (J > 16 || K > 64) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
     const unsigned blocks = unsigned(xwarps_ / 8);
+    // the refinement phase of the mixed solve multiplies in double-float; the
+    // plain FP64 solve (and any product of fewer than 3 columns) stays FP64
+    const bool df = sizeof(T) == 8 && cfg.spmm_prec == CG_PREC_REFINE && J >= 3;
     if constexpr (sizeof(T) == 8) {
-      if (J <= 4) k_xty_df<4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
-      else if (J <= 8) k_xty_df<8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      if (df && J <= 4) k_xty_df<4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      else if (df && J <= 8) k_xty_df<8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      else if (J <= 4) k_xty_t<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
+      else if (J <= 8) k_xty_t<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
       else k_xty_w<T, 16><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     } else if (J <= 4) k_xty_t<T, 4><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
     else if (J <= 8) k_xty_t<T, 8><<<blocks, 256, 0, s>>>(n, X, L, xo, K, Y, L, yo, J, part.p, xrows_);
@@ -948,7 +933,7 @@ struct Engine {
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 16 == 0 && L % 4 == 0;
     const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     if constexpr (sizeof(T) == 8) {
-      if (J <= 32) {
+      if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
         const double* Xd = reinterpret_cast<const double*>(Xp);
         double* Yd = reinterpret_cast<double*>(Yp);
         if (J <= 8) k_gemm_df<8><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
@@ -1073,15 +1058,22 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s));
     const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     const bool vec = L % 4 == 0;
+    bool done = false;
     if constexpr (sizeof(T) == 8) {
+      if (cfg.spmm_prec == CG_PREC_REFINE) {
+        if (C <= 8)
+          k_resid_df<8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+        else
+          k_resid_df<16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+        done = true;
+      }
+    }
+    if (!done) {
       if (C <= 8)
-        k_resid_df<8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+        k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
       else
-        k_resid_df<16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
-    } else if (C <= 8)
-      k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
-    else
-      k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
+        k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
+    }
     CG_CUDA(cudaGetLastError());
     count_launch();
     k_reduce_parts<<<C, 128, 0, s>>>(part.p, int(rgrid), C, small.p);
