@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(_HERE, "libcosmo_gb300.so")
 CG_OK = 0
 CG_ERR_ARG = -1
 CG_PREC_FP64, CG_PREC_FP32, CG_PREC_REFINE = 0, 1, 2
+CG_FORMAT_ROWS, CG_FORMAT_TILED = 0, 1
 STATUS_NAMES = {0: "CG_OK", -1: "CG_ERR_ARG", -2: "CG_ERR_IO", -3: "CG_ERR_PARSE", -4: "CG_ERR_CUDA",
                 -5: "CG_ERR_NOMEM", -6: "CG_ERR_UNSUPPORTED", -7: "CG_ERR_NOT_CONVERGED",
                 -8: "CG_ERR_TIMEOUT", -9: "CG_ERR_NO_DEVICE", -10: "CG_ERR_INTERNAL"}
@@ -130,6 +131,8 @@ _SIGS = {
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "cg_spmm_set_format": (C.c_int32, [_P, C.c_int32]),
+    "cg_spmm_get_format": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
     "cg_davidson": (C.c_int32, [_P, C.POINTER(DavidsonParams), _P, C.c_int32, _P, _P, _P, _P,
                                 C.POINTER(DavidsonStats)]),
@@ -420,7 +423,12 @@ class Hamiltonian:
             if key in db:
                 w, c = db[key]["warps"], db[key]["ctas_per_sm"]
                 _check(lib().cg_spmm_set_tuning(self._h, w, c))
-                return {"warps": w, "ctas_per_sm": c, "cached": True}
+                fmt = db[key].get("format", CG_FORMAT_ROWS)
+                if fmt == CG_FORMAT_TILED and not self.format()[1]:
+                    fmt = CG_FORMAT_ROWS
+                if self.format()[1]:
+                    self.set_format(fmt)
+                return {"warps": w, "ctas_per_sm": c, "format": fmt, "cached": True}
         cap = C.c_int32(64)
         w = np.zeros(64, dtype=np.int32)
         c = np.zeros(64, dtype=np.int32)
@@ -428,14 +436,15 @@ class Hamiltonian:
         _check(lib().cg_spmm_autotune(self._h, nvec, reps, C.byref(cap), _ptr(w), _ptr(c), _ptr(ms)))
         k = int(cap.value)
         bw, bc, _ = self.tuning()
-        res = {"warps": bw, "ctas_per_sm": bc, "cached": False,
+        fmt = self.format()[0]
+        res = {"warps": bw, "ctas_per_sm": bc, "format": fmt, "cached": False,
                "candidates": [(int(w[i]), int(c[i]), float(ms[i])) for i in range(k)]}
         if cache:
             db = {}
             if os.path.exists(cache):
                 with open(cache) as f:
                     db = json.load(f)
-            db[key] = {"warps": bw, "ctas_per_sm": bc, "ms": float(min(ms[:k]))}
+            db[key] = {"warps": bw, "ctas_per_sm": bc, "format": fmt, "ms": float(min(ms[:k]))}
             with open(cache, "w") as f:
                 json.dump(db, f, indent=1, sort_keys=True)
         return res
@@ -444,6 +453,17 @@ class Hamiltonian:
         w, c, t = C.c_int32(), C.c_int32(), C.c_int32()
         _check(lib().cg_spmm_get_tuning(self._h, C.byref(w), C.byref(c), C.byref(t)))
         return int(w.value), int(c.value), bool(t.value)
+
+    def set_format(self, fmt: int) -> None:
+        """Storage the FP32 product of up to 8 vectors reads: CG_FORMAT_ROWS
+        (row-wise) or CG_FORMAT_TILED (neutron-block tiles)."""
+        _check(lib().cg_spmm_set_format(self._h, fmt))
+
+    def format(self):
+        """(format in use, tiled copy present, tiled entries incl. padding)."""
+        f, a, e = C.c_int32(), C.c_int32(), C.c_uint64()
+        _check(lib().cg_spmm_get_format(self._h, C.byref(f), C.byref(a), C.byref(e)))
+        return int(f.value), bool(a.value), int(e.value)
 
 
 @dataclass

@@ -16,6 +16,7 @@
 #include "device.h"
 #include "model.h"
 #include "batched.h"
+#include "tiled.h"
 #include "virtual.h"
 #include "xshljt.h"
 
@@ -604,6 +605,27 @@ cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* c
     if (warps) *warps = h->h.tuning.warps;
     if (ctas_per_sm) *ctas_per_sm = h->h.tuning.ctas_per_sm;
     if (tuned) *tuned = h->h.tuning.tuned;
+  });
+}
+
+cg_status cg_spmm_set_format(cg_hamiltonian* h, int32_t format) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    if (format != CG_FORMAT_ROWS && format != CG_FORMAT_TILED) throw cg::Error(CG_ERR_ARG, "unknown SpMM format");
+    if (format == CG_FORMAT_TILED && !h->h.tiled)
+      throw cg::Error(CG_ERR_UNSUPPORTED, "no block-tiled copy (FP32 matrix built from a basis, blocks <= 2048 rows)");
+    h->h.use_tiled = format == CG_FORMAT_TILED;
+  });
+}
+
+cg_status cg_spmm_get_format(const cg_hamiltonian* h, int32_t* format, int32_t* tiled_available,
+                             uint64_t* tiled_entries) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    const bool t = h->h.tiled != nullptr;
+    if (format) *format = t && h->h.use_tiled ? CG_FORMAT_TILED : CG_FORMAT_ROWS;
+    if (tiled_available) *tiled_available = t;
+    if (tiled_entries) *tiled_entries = t ? h->h.tiled->entries : 0;
   });
 }
 

@@ -138,6 +138,7 @@ struct SpmmCandidate {
 };
 
 struct VirtualOp;
+struct TiledOp;
 struct Hamiltonian {
   int device = 0;
   int precision = CG_PREC_FP64;
@@ -151,6 +152,8 @@ struct Hamiltonian {
   DBuf<double> diag;      // n
   SpmmTuning tuning;
   std::shared_ptr<VirtualOp> virt;  // set for the on-the-fly product (nothing stored)
+  std::shared_ptr<TiledOp> tiled;   // block-tiled copy of the FP32 values (8-vector product)
+  bool use_tiled = true;            // route 8-vector FP32 products through `tiled` when present
   cudaStream_t stream = nullptr;
   ~Hamiltonian();
   uint64_t device_bytes() const;  // HBM held by the matrix (or the on-the-fly tables)

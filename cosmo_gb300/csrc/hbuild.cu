@@ -25,6 +25,7 @@
 #include <chrono>
 
 #include "device.h"
+#include "tiled.h"
 
 namespace cg {
 
@@ -486,6 +487,14 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   h.build_seconds = ms * 1e-3;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (precision == CG_PREC_FP32) {
+    // block-tiled copy for the 8-vector product, blocks = neutron blocks
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<uint64_t> bs = b.h_bstart;
+    bs.push_back(b.n);
+    tiled_build(h, bs);
+    h.build_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
 }
 
 void hamiltonian_upper_rows(const Hamiltonian& h, uint64_t row0, uint64_t nrows, uint64_t* rowptr, uint32_t* cols,

@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "device.h"
+#include "tiled.h"
 #include "virtual.h"
 
 namespace cg {
@@ -484,9 +485,11 @@ void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, 
   else spmm_host_t<double>(h, precision, x, y, m);
 }
 
-// Autotuner: time every candidate launch shape of the FP32 product on this
-// matrix (CUDA events on the handle's stream, median of `reps`) and keep the
-// fastest in h.tuning.  Returns the per-candidate times.
+// Autotuner: time every candidate launch shape of the row-wise FP32 product on
+// this matrix and, for up to 8 vectors, the block-tiled product (CUDA events
+// on the handle's stream, median of `reps`); keep the fastest in h.tuning /
+// h.use_tiled.  Returns the per-candidate times (the tiled candidate carries
+// ctas_per_sm = 0).
 std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   if (h.virt) throw Error(CG_ERR_UNSUPPORTED, "launch-shape tuning applies to stored matrices");
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "autotuning applies to FP32 matrices");
@@ -497,33 +500,59 @@ std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   cudaEvent_t e0, e1;
   CG_CUDA(cudaEventCreate(&e0));
   CG_CUDA(cudaEventCreate(&e1));
+  auto time_once = [&]() {
+    spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);  // warm
+    std::vector<float> ts;
+    for (int r = 0; r < reps; ++r) {
+      CG_CUDA(cudaEventRecord(e0, s));
+      spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);
+      CG_CUDA(cudaEventRecord(e1, s));
+      CG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      ts.push_back(ms);
+    }
+    std::sort(ts.begin(), ts.end());
+    return ts[ts.size() / 2];
+  };
   std::vector<SpmmCandidate> out;
   const SpmmTuning keep = h.tuning;
   float best = 1e30f;
   SpmmTuning bt = keep;
+  bool tiled_best = false;
+  h.use_tiled = false;
   for (int w : {4, 8, 16, 32})
     for (int c : {1, 2, 4, 8}) {
       if (w * c > 64) continue;  // at most 64 resident warps per SM
       h.tuning.warps = w;
       h.tuning.ctas_per_sm = c;
-      spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);  // warm
-      std::vector<float> ts;
-      for (int r = 0; r < reps; ++r) {
-        CG_CUDA(cudaEventRecord(e0, s));
-        spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);
-        CG_CUDA(cudaEventRecord(e1, s));
-        CG_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        ts.push_back(ms);
-      }
-      std::sort(ts.begin(), ts.end());
-      float med = ts[ts.size() / 2];
+      const float med = time_once();
       out.push_back({w, c, med});
       if (med < best) { best = med; bt = h.tuning; }
     }
+  if (h.tiled && m <= 8) {
+    // tiled launch shapes: warps per CTA x ring slots
+    TiledOp& t = *h.tiled;
+    int bw = t.warps, bst = t.stages;
+    float tbest = 1e30f;
+    h.use_tiled = true;
+    for (int w : {8, 16})
+      for (int st : {2, 3, 4, 6}) {
+        if ((t.smax + w - 1) / w > 4) continue;  // at most 4 slices per warp
+        if (kTiledHeadBytes + size_t(st) * t.lmax * 32 > 227 * 1024) continue;
+        t.warps = w;
+        t.stages = st;
+        const float med = time_once();
+        if (med < tbest) { tbest = med; bw = w; bst = st; }
+      }
+    t.warps = bw;
+    t.stages = bst;
+    out.push_back({bw, 0, tbest});
+    if (tbest < best) { best = tbest; tiled_best = true; }
+  }
   h.tuning = bt;
   h.tuning.tuned = true;
+  h.use_tiled = tiled_best;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return out;
@@ -679,6 +708,7 @@ void spmm_f32_padded(const Hamiltonian& h, const float* x, int ldx, float* y, in
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "FP32 product needs an FP32 matrix");
   if (m < 1 || m > 16) throw Error(CG_ERR_ARG, "padded FP32 SpMM takes 1..16 vectors");
   if (reinterpret_cast<uintptr_t>(x) % 32 || ldx % 8) throw Error(CG_ERR_ARG, "padded FP32 SpMM needs 32-byte rows");
+  if (m <= 8 && ldx == 8 && h.tiled && h.use_tiled) return tiled_product(h, x, y, ldy, m, s);
   if (m <= 8) {
     if (ldx < 8) throw Error(CG_ERR_ARG, "ldx < 8");
     run_wide<8>(h, x, ldx, y, ldy, m, s);
@@ -700,6 +730,8 @@ void spmm_launch(const Hamiltonian& h, int precision, const void* x, int ldx, vo
       break;
     case CG_PREC_FP32:
       if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "FP32 product needs an FP32 matrix");
+      if (m <= 8 && ldx == 8 && h.tiled && h.use_tiled && reinterpret_cast<uintptr_t>(x) % 16 == 0)
+        return tiled_product(h, static_cast<const float*>(x), static_cast<float*>(y), ldy, m, s);
       dispatch_nv<CG_PREC_FP32>(m, h, h.hi.p, x, ldx, y, ldy, s);
       break;
     case CG_PREC_REFINE:

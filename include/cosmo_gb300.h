@@ -220,6 +220,19 @@ cg_status cg_gather_ceiling(uint64_t rows, int32_t share, double* gathers_per_se
 /* Set (e.g. from a cached tuning) or read the launch shape of the FP32 product. */
 cg_status cg_spmm_set_tuning(cg_hamiltonian* h, int32_t warps, int32_t ctas_per_sm);
 cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* ctas_per_sm, int32_t* tuned);
+/* Storage the FP32 product of up to 8 vectors reads.  An FP32 matrix built
+ * from a basis also holds a block-tiled copy: tiles = (neutron block, neutron
+ * block) pairs, 16-bit in-tile columns, x of the column block staged in shared
+ * memory per tile.  The reference's counterpart is its fixed CSB blocking
+ * (PPMatrix2CSBBlk, include/sm/PPMatrix.cxx:571-656); the choice of format has
+ * no counterpart there.  cg_spmm_autotune picks the faster format (its tiled
+ * candidate is reported with ctas_per_sm = 0); tiled_entries counts stored
+ * entries including the slice padding. */
+#define CG_FORMAT_ROWS 0
+#define CG_FORMAT_TILED 1
+cg_status cg_spmm_set_format(cg_hamiltonian* h, int32_t format);
+cg_status cg_spmm_get_format(const cg_hamiltonian* h, int32_t* format, int32_t* tiled_available,
+                             uint64_t* tiled_entries);
 
 /* -------------------------------------------------------------- Davidson */
 /* Block Davidson for the lowest eigenpairs (Davidson-Liu with diagonal
