@@ -40,6 +40,14 @@ class CosmoError(RuntimeError):
         self.status = status
 
 
+class SpmmFormatInfo(C.Structure):
+    _fields_ = [("format", C.c_int32), ("tiled_available", C.c_int32), ("warps", C.c_int32),
+                ("stages", C.c_int32), ("slices_per_warp", C.c_int32), ("reserved", C.c_int32),
+                ("entries", C.c_uint64), ("units", C.c_uint64),
+                ("meta_bytes", C.c_uint64), ("device_bytes", C.c_uint64), ("ident_tiles", C.c_uint64),
+                ("ident_entries", C.c_uint64)]
+
+
 class ProblemInfo(C.Structure):
     _fields_ = [("n_sps", C.c_int32), ("n_neutron_sps", C.c_int32), ("nv", C.c_int32), ("zv", C.c_int32),
                 ("twom", C.c_int32), ("parity", C.c_int32), ("has_jj", C.c_int32), ("jj", C.c_double),
@@ -132,7 +140,8 @@ _SIGS = {
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_spmm_set_format": (C.c_int32, [_P, C.c_int32]),
-    "cg_spmm_get_format": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
+    "cg_spmm_get_format": (C.c_int32, [_P, _P]),
+    "cg_spmm_set_tiled_shape": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "cg_davidson_defaults": (None, [C.POINTER(DavidsonParams), C.c_int32]),
     "cg_davidson": (C.c_int32, [_P, C.POINTER(DavidsonParams), _P, C.c_int32, _P, _P, _P, _P,
                                 C.POINTER(DavidsonStats)]),
@@ -428,6 +437,8 @@ class Hamiltonian:
                     fmt = CG_FORMAT_ROWS
                 if self.format()[1]:
                     self.set_format(fmt)
+                    if "tiled_shape" in db[key]:
+                        self.set_tiled_shape(*db[key]["tiled_shape"])
                 return {"warps": w, "ctas_per_sm": c, "format": fmt, "cached": True}
         cap = C.c_int32(64)
         w = np.zeros(64, dtype=np.int32)
@@ -445,6 +456,9 @@ class Hamiltonian:
                 with open(cache) as f:
                     db = json.load(f)
             db[key] = {"warps": bw, "ctas_per_sm": bc, "format": fmt, "ms": float(min(ms[:k]))}
+            fi = self.format_info()
+            if fi["tiled_available"]:
+                db[key]["tiled_shape"] = [fi["slices_per_warp"], fi["stages"]]
             with open(cache, "w") as f:
                 json.dump(db, f, indent=1, sort_keys=True)
         return res
@@ -461,9 +475,19 @@ class Hamiltonian:
 
     def format(self):
         """(format in use, tiled copy present, tiled entries incl. padding)."""
-        f, a, e = C.c_int32(), C.c_int32(), C.c_uint64()
-        _check(lib().cg_spmm_get_format(self._h, C.byref(f), C.byref(a), C.byref(e)))
-        return int(f.value), bool(a.value), int(e.value)
+        i = self.format_info()
+        return i["format"], i["tiled_available"], i["entries"]
+
+    def set_tiled_shape(self, slices_per_warp: int, stages: int) -> None:
+        """Launch shape of the tiled product: slices per consumer warp, ring slots."""
+        _check(lib().cg_spmm_set_tiled_shape(self._h, slices_per_warp, stages))
+
+    def format_info(self) -> dict:
+        i = SpmmFormatInfo()
+        _check(lib().cg_spmm_get_format(self._h, C.byref(i)))
+        d = {k: getattr(i, k) for k, _ in SpmmFormatInfo._fields_}
+        d["tiled_available"] = bool(d["tiled_available"])
+        return d
 
 
 @dataclass

@@ -618,14 +618,41 @@ cg_status cg_spmm_set_format(cg_hamiltonian* h, int32_t format) {
   });
 }
 
-cg_status cg_spmm_get_format(const cg_hamiltonian* h, int32_t* format, int32_t* tiled_available,
-                             uint64_t* tiled_entries) {
+cg_status cg_spmm_set_tiled_shape(cg_hamiltonian* h, int32_t slices_per_warp, int32_t stages) {
   return guard([&] {
     CG_NOT_NULL(h);
-    const bool t = h->h.tiled != nullptr;
-    if (format) *format = t && h->h.use_tiled ? CG_FORMAT_TILED : CG_FORMAT_ROWS;
-    if (tiled_available) *tiled_available = t;
-    if (tiled_entries) *tiled_entries = t ? h->h.tiled->entries : 0;
+    cg::TiledOp* t = h->h.tiled.get();
+    if (!t) throw cg::Error(CG_ERR_UNSUPPORTED, "no block-tiled copy");
+    if (slices_per_warp < 1 || slices_per_warp > 4) throw cg::Error(CG_ERR_ARG, "slices per warp must be 1..4");
+    const int warps = (t->smax + slices_per_warp - 1) / slices_per_warp;
+    if (warps > 31) throw cg::Error(CG_ERR_ARG, "more than 31 consumer warps; take more slices per warp");
+    if (stages < 2 || stages > 7 || cg::tiled_smem(*t, stages) > 227 * 1024)
+      throw cg::Error(CG_ERR_ARG, "ring slots out of range (2..7 within 227 KB of shared memory)");
+    t->rps = slices_per_warp;
+    t->warps = warps;
+    t->stages = stages;
+  });
+}
+
+cg_status cg_spmm_get_format(const cg_hamiltonian* h, cg_spmm_format_info* info) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(info);
+    *info = cg_spmm_format_info{};
+    const cg::TiledOp* t = h->h.tiled.get();
+    info->format = t && h->h.use_tiled ? CG_FORMAT_TILED : CG_FORMAT_ROWS;
+    info->tiled_available = t != nullptr;
+    if (t) {
+      info->warps = t->warps;
+      info->stages = t->stages;
+      info->slices_per_warp = t->rps;
+      info->entries = t->entries;
+      info->units = t->nitems;
+      info->meta_bytes = t->items.bytes() + t->rcopy.bytes() + t->iden.bytes();
+      info->device_bytes = t->bytes();
+      info->ident_tiles = t->ident_tiles;
+      info->ident_entries = t->ident_nnz;
+    }
   });
 }
 

@@ -531,22 +531,25 @@ std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
       if (med < best) { best = med; bt = h.tuning; }
     }
   if (h.tiled && m <= 8) {
-    // tiled launch shapes: warps per CTA x ring slots
+    // tiled launch shapes: slices per consumer warp x ring slots
     TiledOp& t = *h.tiled;
-    int bw = t.warps, bst = t.stages;
+    int brps = t.rps, bst = t.stages;
     float tbest = 1e30f;
     h.use_tiled = true;
-    for (int w : {8, 16})
+    for (int rps : {1, 2, 3})
       for (int st : {2, 3, 4, 6}) {
-        if ((t.smax + w - 1) / w > 4) continue;  // at most 4 slices per warp
-        if (kTiledHeadBytes + size_t(st) * t.lmax * 32 > 227 * 1024) continue;
-        t.warps = w;
+        if ((t.smax + rps - 1) / rps > 31) continue;  // at most 31 consumer warps
+        if (tiled_smem(t, st) > 227 * 1024) continue;
+        t.rps = rps;
+        t.warps = (t.smax + rps - 1) / rps;
         t.stages = st;
         const float med = time_once();
-        if (med < tbest) { tbest = med; bw = w; bst = st; }
+        if (med < tbest) { tbest = med; brps = rps; bst = st; }
       }
-    t.warps = bw;
+    t.rps = brps;
+    t.warps = (t.smax + brps - 1) / brps;
     t.stages = bst;
+    const int bw = t.warps;
     out.push_back({bw, 0, tbest});
     if (tbest < best) { best = tbest; tiled_best = true; }
   }

@@ -1,15 +1,18 @@
 // Block-tiled 8-vector FP32 product (layout described in tiled.h).
 //
-// Product kernel: one CTA per row block b (longest first), warp w owning the
-// 32-row slices w, w + NW, ... of b and the 8 accumulators of each of its
-// rows in registers for the whole CTA.  The CTA walks the tiles of b in
-// ascending column block; thread 0 keeps `stages` tiles in flight, each x[c]
-// brought into a shared-memory ring slot by one cp.async.bulk whose completion
-// is counted on that slot's `full` mbarrier, and a slot is refilled once every
-// warp has arrived on its `empty` mbarrier.  Warps therefore run up to
-// stages - 1 tiles apart and never meet at a CTA-wide barrier inside the loop.
-// Each stored entry costs one 2-byte column, one FP32 value (both streamed,
-// coalesced) and one 32-byte row read from shared memory.
+// Product kernel: one CTA per row block b (longest first) with NW consumer
+// warps (the longest block's slices / RPS) and one producer warp.  Consumer warp w owns the 32-row slices
+// w, w + NW, ... of b and keeps the 8 accumulators of each of its rows in
+// registers for the whole CTA.  The CTA walks the tiles of b in ascending
+// column block, in staged units (tile, range of 32-entry groups): lane 0 of
+// the producer warp fills a ring of `stages` shared-memory slots, each unit
+// brought in by three cp.async.bulk copies (x of the column block, the
+// unit's 16-bit columns, its FP32 values) counted on the slot's `full`
+// mbarrier, and refills a slot once every consumer warp has arrived on its
+// `empty` mbarrier.  Consumers therefore never touch global memory in the
+// inner loop and never meet at a CTA-wide barrier inside it: per stored entry
+// one 2-byte and one 4-byte shared load (coalesced) and one 32-byte row read
+// of the staged x.
 //
 // The reference's blocked format is PPMatrix2CSBBlk (include/sm/PPMatrix.cxx:
 // 571-656, square blocks of floor(sqrt(n)) + 1 rows, 16-bit in-block indices)
@@ -117,17 +120,102 @@ __global__ void k_tfill(uint64_t n, const uint64_t* __restrict__ rowptr, const u
   }
 }
 
+// Reorder each row's entries inside its run so that, step by step, the 32
+// lanes' row reads of x spread over the shared-memory bank groups: lane l at
+// step j reads its first 16 bytes from group (2 col + (l & 1)) mod 8, and a
+// step costs as many wavefronts as its most used group.  Lane l aims at step j
+// for group 2 ((l / 2 + j) mod 4) + (l & 1), which puts four lanes on every
+// group, and takes the first entry of its next 8 with that group (else a
+// padding entry, which issues no read, else the next entry).  One warp per
+// run, each lane reordering its own entries; only a row's summation order
+// changes.
+__global__ void k_tbalance(uint64_t nruns, const uint32_t* __restrict__ roff, uint16_t* __restrict__ col,
+                           float* __restrict__ val) {
+  const int lane = threadIdx.x & 31, p = lane & 1;
+  const uint64_t w0 = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t nw = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t r = w0; r < nruns; r += nw) {
+    const uint64_t g0 = roff[r];
+    const uint32_t w = roff[r + 1] - roff[r];
+    for (uint32_t j = 0; j + 1 < w; ++j) {
+      const uint32_t target = 2 * (((lane >> 1) + j) & 3) + p;
+      const uint32_t jw = min(w, j + 8);
+      uint32_t hit = jw, pad = jw;
+      for (uint32_t q = j; q < jw && hit == jw; ++q) {
+        const uint64_t e = (g0 + q) * 32 + lane;
+        if (val[e] == 0.f) {
+          if (pad == jw) pad = q;
+        } else if (((2u * col[e] + p) & 7u) == target) {
+          hit = q;
+        }
+      }
+      const uint32_t best = hit < jw ? hit : (pad < jw ? pad : j);
+      if (best != j) {
+        const uint64_t ej = (g0 + j) * 32 + lane, eb = (g0 + best) * 32 + lane;
+        const uint16_t tc = col[ej]; col[ej] = col[eb]; col[eb] = tc;
+        const float tv = val[ej]; val[ej] = val[eb]; val[eb] = tv;
+      }
+    }
+  }
+}
+
+// Scaled-identity tiles: every row of the block holds exactly one entry, at
+// its own position in the column block, and all values are bitwise equal (a
+// two-neutron move with the protons as spectators).  One warp per tile.
+__global__ void k_tident(uint64_t ntiles, const uint32_t* __restrict__ tblock, const uint64_t* __restrict__ bstart,
+                         const uint32_t* __restrict__ tptr, const uint32_t* __restrict__ runbase,
+                         const uint32_t* __restrict__ roff, const uint16_t* __restrict__ col,
+                         const float* __restrict__ val, uint32_t* __restrict__ ident) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w0 = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t nw = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t t = w0; t < ntiles; t += nw) {
+    const uint32_t b = tblock[t];
+    const uint32_t L = uint32_t(bstart[b + 1] - bstart[b]), sl = (L + 31) / 32;
+    const uint32_t q0 = runbase[b] + (uint32_t(t) - tptr[b]) * sl;
+    const float v0 = val[uint64_t(roff[q0]) * 32];
+    bool ok = v0 != 0.f;
+    for (uint32_t s = 0; s < sl && ok; ++s) {
+      const uint32_t g = roff[q0 + s];
+      bool good = roff[q0 + s + 1] - g == 1;
+      const uint32_t r = s * 32 + lane;
+      if (good && r < L) {
+        const uint64_t e = uint64_t(g) * 32 + lane;
+        good = col[e] == r && __float_as_uint(val[e]) == __float_as_uint(v0);
+      }
+      ok = __all_sync(0xffffffffu, good);
+    }
+    if (lane == 0) ident[t] = ok ? __float_as_uint(v0) : 0u;
+  }
+}
+
+// One staged unit: x of one column block and the entry groups [g0, g1) of one
+// tile, plus the tile's run offsets (roff of its slices 0..slices, a 16-byte
+// aligned copy in TiledOp::rcopy).  32 bytes.
+struct __align__(16) TItem {
+  uint32_t xrow, xrows;  // first row and row count of the column block
+  uint32_t g0, g1;       // entry groups of this unit
+  uint32_t rc, rcbytes;  // run-offset copy: first u32 in rcopy, bytes (multiple of 16)
+  uint32_t pad0, pad1;
+};
+
 struct TArgs {
   const uint64_t* bstart;
   const uint32_t* order;
-  const uint32_t* tptr;
-  const uint32_t* tcb;
-  const uint32_t* runbase;
-  const uint32_t* roff;
+  const uint32_t* iptr;
+  const TItem* items;
+  const uint32_t* rcopy;
   const uint16_t* col;
   const float* val;
-  int lmax, stages;
+  const uint32_t* dptr;  // nb + 1: first scaled-identity tile of each block
+  const uint2* iden;     // per scaled-identity tile: first x row, value bits
+  int lmax, gmax, stages;
 };
+
+__device__ __forceinline__ void row8g(const float* p, int sw, float (&v)[8]) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p) + sw), b = __ldg(reinterpret_cast<const float4*>(p) + (sw ^ 1));
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
 
 // Row read of 8 floats as two 16-byte halves, odd lanes second half first (the
 // first load of a warp then covers all eight 16-byte bank groups); the halves
@@ -137,26 +225,29 @@ __device__ __forceinline__ void row8(const float* p, int sw, float (&v)[8]) {
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
-template <int NW, int RPS>
-__global__ void __launch_bounds__(NW * 32) k_tiled(TArgs a, const float* __restrict__ x, float* __restrict__ y,
-                                                   int ldy, int m, int* __restrict__ err) {
-  constexpr int U = 4;  // entry steps whose loads are in flight together
+template <int RPS>
+__global__ void __launch_bounds__(1024) k_tiled(TArgs a, const float* __restrict__ x, float* __restrict__ y,
+                                                int ldy, int m, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int NW = int(blockDim.x >> 5) - 1;  // consumer warps; the last warp produces
   const int S = a.stages;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
   uint64_t* empty = full + S;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(empty + S);
-  float* ring = reinterpret_cast<float*>(smem_raw + kTiledHead);
-  const size_t slot_floats = size_t(a.lmax) * 8;
+  unsigned char* ring = smem_raw + kTiledHead;
+  // slot: header (g0, g1, pad; run offsets of the tile's slices, up to
+  // kTiledSlotHead - 16 bytes) | x block (lmax rows x 32 B) | columns (gmax
+  // groups x 64 B) | values (gmax groups x 128 B)
+  const uint32_t xbytes = uint32_t(a.lmax) * 32u, cbytes = uint32_t(a.gmax) * 64u;
+  const uint32_t slot = kTiledSlotHead + xbytes + 3u * cbytes;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, sw = lane & 1;
   const uint32_t b = a.order[blockIdx.x];
   const uint64_t start = a.bstart[b];
   const int L = int(a.bstart[b + 1] - start);
   const int slices = (L + 31) >> 5;
-  const uint32_t t0 = a.tptr[b];
-  const int T = int(a.tptr[b + 1] - t0);
-  const uint32_t rb = a.runbase[b];
+  const uint32_t i0 = a.iptr[b];
+  const int I = int(a.iptr[b + 1] - i0);
 
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
@@ -167,15 +258,56 @@ __global__ void __launch_bounds__(NW * 32) k_tiled(TArgs a, const float* __restr
     bulk::fence_mbar_init();
   }
   __syncthreads();
-  auto issue = [&](int t) {
-    const uint32_t cb = a.tcb[t0 + t];
-    const uint64_t cs = a.bstart[cb];
-    const uint32_t bytes = uint32_t(a.bstart[cb + 1] - cs) * 32u;
-    bulk::bulk_load(ring + size_t(t % S) * slot_floats, x + cs * 8, bytes, &full[t % S]);
-  };
-  int issued = 0;
-  if (tid == 0)
-    for (; issued < S && issued < T; ++issued) issue(issued);
+
+  if (warp == NW) {
+    // producer warp: the lanes fetch the descriptors of 32 units at a time;
+    // lane 0 refills slot i % S once every consumer warp has released the unit
+    // S before, writes the unit's bounds and starts its four copies
+    int issued = 0;
+    bool stop = false;
+    for (int base = 0; base < I && !stop; base += 32) {
+      TItem d{};
+      if (base + lane < I) d = a.items[i0 + base + lane];
+      const int nb = min(32, I - base);
+      for (int k = 0; k < nb; ++k) {
+        const uint32_t xrow = __shfl_sync(0xffffffffu, d.xrow, k), xrows = __shfl_sync(0xffffffffu, d.xrows, k);
+        const uint32_t g0 = __shfl_sync(0xffffffffu, d.g0, k), g1 = __shfl_sync(0xffffffffu, d.g1, k);
+        const uint32_t rc = __shfl_sync(0xffffffffu, d.rc, k), rcb = __shfl_sync(0xffffffffu, d.rcbytes, k);
+        int bad = 0;
+        if (lane == 0) {
+          const int i = base + k;
+          if (i >= S && !bulk::mbar_wait(&empty[i % S], ((i / S) - 1) & 1)) {
+            *abort_flag = 1;
+            atomicOr(err, 1);
+            bad = 1;
+          } else if (*abort_flag) {
+            bad = 1;
+          } else {
+            unsigned char* st = ring + size_t(i % S) * slot;
+            uint32_t* hd = reinterpret_cast<uint32_t*>(st);
+            hd[0] = g0;
+            hd[1] = g1;
+            uint64_t* bar = &full[i % S];
+            const uint32_t ng = g1 - g0, xb = xrows * 32u;
+            bulk::expect_tx(bar, rcb + xb + ng * 192u);
+            bulk::copy(st + 16, a.rcopy + rc, rcb, bar);
+            bulk::copy(st + kTiledSlotHead, x + uint64_t(xrow) * 8, xb, bar);
+            bulk::copy(st + kTiledSlotHead + xbytes, a.col + uint64_t(g0) * 32, ng * 64u, bar);
+            bulk::copy(st + kTiledSlotHead + xbytes + cbytes, a.val + uint64_t(g0) * 32, ng * 128u, bar);
+            issued = i + 1;
+          }
+        }
+        if (__shfl_sync(0xffffffffu, bad, 0)) {
+          stop = true;
+          break;
+        }
+      }
+    }
+    if (lane == 0 && *abort_flag)  // let the copies still in flight land before the CTA's shared memory goes
+      for (int i = issued > S ? issued - S : 0; i < issued; ++i) bulk::mbar_wait(&full[i % S], (i / S) & 1);
+    __syncthreads();
+    return;
+  }
 
   float acc[RPS][8];
 #pragma unroll
@@ -183,86 +315,91 @@ __global__ void __launch_bounds__(NW * 32) k_tiled(TArgs a, const float* __restr
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[k][j] = 0.f;
 
-  // run offsets of this warp's slices, one tile ahead
-  uint32_t nx0[RPS], nx1[RPS];
+  // scaled-identity tiles straight from global memory (consecutive rows,
+  // coalesced) while the first units stream in
+  {
+    const uint32_t d0 = a.dptr[b], d1 = a.dptr[b + 1];
+    uint32_t d = d0;
+    for (; d + 2 <= d1; d += 2) {
+      const uint2 e0 = a.iden[d], e1 = a.iden[d + 1];
 #pragma unroll
-  for (int k = 0; k < RPS; ++k) {
-    const int s = warp + k * NW;
-    nx0[k] = nx1[k] = 0;
-    if (s < slices && T > 0) {
-      nx0[k] = a.roff[rb + s];
-      nx1[k] = a.roff[rb + s + 1];
+      for (int k = 0; k < RPS; ++k) {
+        const int r = (warp + k * NW) * 32 + lane;
+        if (r < L) {
+          float x0[8], x1[8];
+          row8g(x + (uint64_t(e0.x) + r) * 8, sw, x0);
+          row8g(x + (uint64_t(e1.x) + r) * 8, sw, x1);
+          const float v0 = __uint_as_float(e0.y), v1 = __uint_as_float(e1.y);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[k][u] = fmaf(v1, x1[u], fmaf(v0, x0[u], acc[k][u]));
+        }
+      }
+    }
+    if (d < d1) {
+      const uint2 e0 = a.iden[d];
+#pragma unroll
+      for (int k = 0; k < RPS; ++k) {
+        const int r = (warp + k * NW) * 32 + lane;
+        if (r < L) {
+          float x0[8];
+          row8g(x + (uint64_t(e0.x) + r) * 8, sw, x0);
+          const float v0 = __uint_as_float(e0.y);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[k][u] = fmaf(v0, x0[u], acc[k][u]);
+        }
+      }
     }
   }
-  for (int t = 0; t < T; ++t) {
-    // refill the slot of the previous tile once every warp has released it
-    if (tid == 0 && t >= 1 && issued < T) {
-      const int p = t - 1;
-      if (bulk::mbar_wait(&empty[p % S], (p / S) & 1)) {
-        issue(issued);
-        ++issued;
-      } else {
-        *abort_flag = 1;
-        atomicOr(err, 1);
-      }
-    }
-    if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
-    uint32_t o0[RPS], o1[RPS];
-#pragma unroll
-    for (int k = 0; k < RPS; ++k) {
-      o0[k] = nx0[k];
-      o1[k] = nx1[k];
-      const int s = warp + k * NW;
-      if (s < slices && t + 1 < T) {
-        const uint32_t q = rb + uint32_t(t + 1) * slices + s;
-        nx0[k] = a.roff[q];
-        nx1[k] = a.roff[q + 1];
-      }
-    }
-    const bool ok = bulk::mbar_wait(&full[t % S], (t / S) & 1);
-    if (!__all_sync(0xffffffffu, ok)) {
+
+  for (int i = 0; i < I; ++i) {
+    const bool ok = bulk::mbar_wait(&full[i % S], (i / S) & 1);
+    if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) {
       if (lane == 0) {
         *abort_flag = 1;
         atomicOr(err, 1);
       }
       break;
     }
-    const float* buf = ring + size_t(t % S) * slot_floats;
+    const unsigned char* st = ring + size_t(i % S) * slot;
+    const uint32_t* hd = reinterpret_cast<const uint32_t*>(st);
+    const uint32_t g0 = hd[0], g1 = hd[1];
+    const uint32_t* ro = hd + 4;  // run offsets of the tile's slices
+    const float* xs = reinterpret_cast<const float*>(st + kTiledSlotHead);
+    const uint16_t* sc = reinterpret_cast<const uint16_t*>(st + kTiledSlotHead + xbytes) + lane;
+    const float* sv = reinterpret_cast<const float*>(st + kTiledSlotHead + xbytes + cbytes) + lane;
 #pragma unroll
     for (int k = 0; k < RPS; ++k) {
-      for (uint32_t j = o0[k]; j < o1[k]; j += U) {
-        uint32_t c[U];
-        float v[U];
+      const int s = warp + k * NW;
+      if (s < slices) {
+        const uint32_t lo = max(ro[s], g0), hi = min(ro[s + 1], g1);
+        uint32_t j = lo;
+        // two steps per pass, all shared loads issued before the FMAs; padding
+        // (value 0, column 0) reads row 0 of the staged block and adds 0
+        for (; j + 2 <= hi; j += 2) {
+          const uint32_t q = (j - g0) * 32;
+          const float v0 = sv[q], v1 = sv[q + 32];
+          const uint32_t c0 = sc[q], c1 = sc[q + 32];
+          float x0[8], x1[8];
+          row8(xs + c0 * 8, sw, x0);
+          row8(xs + c1 * 8, sw, x1);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          c[u] = 0;
-          v[u] = 0.f;
-          if (j + u < o1[k]) {
-            const uint64_t e = uint64_t(j + u) * 32 + lane;
-            c[u] = __ldcs(a.col + e);
-            v[u] = __ldcs(a.val + e);
-          }
+          for (int u = 0; u < 8; ++u) acc[k][u] = fmaf(v1, x1[u], fmaf(v0, x0[u], acc[k][u]));
         }
+        if (j < hi) {
+          const uint32_t q = (j - g0) * 32;
+          const float v0 = sv[q];
+          float x0[8];
+          row8(xs + uint32_t(sc[q]) * 8, sw, x0);
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-          if (j + u < o1[k]) {
-            float xr[8];
-            row8(buf + size_t(c[u]) * 8, sw, xr);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) acc[k][q] = fmaf(v[u], xr[q], acc[k][q]);
-          }
+          for (int u = 0; u < 8; ++u) acc[k][u] = fmaf(v0, x0[u], acc[k][u]);
+        }
       }
     }
     __syncwarp();
-    if (lane == 0) bulk::mbar_arrive(&empty[t % S]);
+    if (lane == 0) bulk::mbar_arrive(&empty[i % S]);
   }
   __syncthreads();
-  if (*abort_flag) {
-    // let the copies still in flight land before the CTA's shared memory goes
-    if (tid == 0)
-      for (int i = issued > S ? issued - S : 0; i < issued; ++i) bulk::mbar_wait(&full[i % S], (i / S) & 1);
-    return;
-  }
+  if (*abort_flag) return;
 #pragma unroll
   for (int k = 0; k < RPS; ++k) {
     const int r = (warp + k * NW) * 32 + lane;
@@ -277,26 +414,23 @@ __global__ void __launch_bounds__(NW * 32) k_tiled(TArgs a, const float* __restr
   }
 }
 
-template <int NW, int RPS>
-void launch_tiled(const TiledOp& t, const TArgs& a, const float* x, float* y, int ldy, int m, int* err,
-                  cudaStream_t s) {
-  const size_t smem = kTiledHead + size_t(t.stages) * t.lmax * 32;
-  CG_CUDA(cudaFuncSetAttribute(k_tiled<NW, RPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  k_tiled<NW, RPS><<<unsigned(t.nb), NW * 32, smem, s>>>(a, x, y, ldy, m, err);
-  CG_CUDA(cudaGetLastError());
-  count_launch();
+}  // namespace
+
+size_t tiled_smem(const TiledOp& t, int stages) {
+  return kTiledHeadBytes + size_t(stages) * (kTiledSlotHead + size_t(t.lmax) * 32 + size_t(t.gmax) * 192);
 }
 
-template <int NW>
-void launch_nw(const TiledOp& t, const TArgs& a, const float* x, float* y, int ldy, int m, int* err, cudaStream_t s) {
-  const int rps = (t.smax + NW - 1) / NW;
-  switch (rps) {
-    case 1: launch_tiled<NW, 1>(t, a, x, y, ldy, m, err, s); break;
-    case 2: launch_tiled<NW, 2>(t, a, x, y, ldy, m, err, s); break;
-    case 3: launch_tiled<NW, 3>(t, a, x, y, ldy, m, err, s); break;
-    case 4: launch_tiled<NW, 4>(t, a, x, y, ldy, m, err, s); break;
-    default: throw Error(CG_ERR_INTERNAL, "tiled product: too many slices per warp");
-  }
+namespace {
+
+template <int RPS>
+void launch_tiled(const TiledOp& t, const TArgs& a, const float* x, float* y, int ldy, int m, int* err,
+                  cudaStream_t s) {
+  const size_t smem = tiled_smem(t, t.stages);
+  const int nw = (t.smax + RPS - 1) / RPS;
+  CG_CUDA(cudaFuncSetAttribute(k_tiled<RPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  k_tiled<RPS><<<unsigned(t.nb), (nw + 1) * 32, smem, s>>>(a, x, y, ldy, m, err);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
 }
 
 }  // namespace
@@ -399,14 +533,76 @@ void tiled_build(Hamiltonian& h, const std::vector<uint64_t>& bs) {
   k_tfill<<<grid, 256, 0, s>>>(h.n, h.rowptr.p, h.col.p, h.hi.p, ti, t.roff.p, t.col.p, t.val.p);
   CG_CUDA(cudaGetLastError());
   count_launch();
+  if (nruns) {
+    k_tbalance<<<unsigned(std::min<uint64_t>((nruns * 32 + 255) / 256, 152ull * 64)), 256, 0, s>>>(
+        nruns, t.roff.p, t.col.p, t.val.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+  }
+  // scaled-identity tiles
+  std::vector<uint32_t> tblock(ntiles);
+  for (int b = 0; b < nb; ++b)
+    for (uint32_t tt = tptr[b]; tt < tptr[b + 1]; ++tt) tblock[tt] = uint32_t(b);
+  DBuf<uint32_t> dtblock, dident(std::max<uint64_t>(ntiles, 1));
+  dtblock.upload(tblock, s);
+  if (ntiles) {
+    k_tident<<<unsigned(std::min<uint64_t>((ntiles * 32 + 255) / 256, 152ull * 64)), 256, 0, s>>>(
+        ntiles, dtblock.p, t.bstart.p, t.tptr.p, t.runbase.p, t.roff.p, t.col.p, t.val.p, dident.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+  }
+  std::vector<uint32_t> ident(ntiles);
+  if (ntiles) CG_CUDA(cudaMemcpyAsync(ident.data(), dident.p, ntiles * 4, cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  // staged units: each tile's entry groups in chunks of at most gmax groups,
+  // with a 16-byte aligned copy of the tile's run offsets
+  t.gmax = std::max(8, t.lmax / 6);  // entry area ~ the x area of a slot
+  std::vector<uint32_t> iptr(nb + 1), rcopy, dptr(nb + 1);
+  std::vector<TItem> items;
+  std::vector<uint2> iden;
+  for (int b = 0; b < nb; ++b) {
+    iptr[b] = uint32_t(items.size());
+    dptr[b] = uint32_t(iden.size());
+    const uint32_t sl = uint32_t((bs[b + 1] - bs[b] + 31) / 32);
+    const uint32_t cpb = (sl + 1 + 3) / 4 * 16;  // bytes of one copy
+    for (uint32_t tt = tptr[b]; tt < tptr[b + 1]; ++tt) {
+      const uint32_t q = runbase[b] + (tt - tptr[b]) * sl;
+      const uint32_t G0 = roff[q], G1 = roff[q + sl];
+      if (ident[tt]) {  // read straight from x, nothing staged
+        iden.push_back(make_uint2(uint32_t(bs[tcb[tt]]), ident[tt]));
+        t.ident_tiles += 1;
+        t.ident_nnz += bs[b + 1] - bs[b];
+        continue;
+      }
+      const uint32_t rc = uint32_t(rcopy.size());
+      for (uint32_t v = 0; v < cpb / 4; ++v) rcopy.push_back(v <= sl ? roff[q + v] : 0u);
+      const uint32_t cb = tcb[tt];
+      for (uint32_t g = G0; g < G1; g += uint32_t(t.gmax))
+        items.push_back({uint32_t(bs[cb]), uint32_t(bs[cb + 1] - bs[cb]), g, std::min(G1, g + uint32_t(t.gmax)), rc,
+                         cpb, 0, 0});
+    }
+    if (rcopy.size() >= (1ull << 32)) return;
+  }
+  iptr[nb] = uint32_t(items.size());
+  dptr[nb] = uint32_t(iden.size());
+  t.dptr.upload(dptr, s);
+  t.iden.alloc(std::max<size_t>(iden.size(), 1) * sizeof(uint2));
+  if (!iden.empty())
+    CG_CUDA(cudaMemcpyAsync(t.iden.p, iden.data(), iden.size() * sizeof(uint2), cudaMemcpyHostToDevice, s));
+  t.nitems = items.size();
+  t.iptr.upload(iptr, s);
+  t.rcopy.upload(rcopy, s);
+  t.items.alloc(items.size() * sizeof(TItem));
+  if (!items.empty())
+    CG_CUDA(cudaMemcpyAsync(t.items.p, items.data(), items.size() * sizeof(TItem), cudaMemcpyHostToDevice, s));
   CG_CUDA(cudaStreamSynchronize(s));
 
-  // default launch shape (spmm_autotune refines it): 8 warps while 3 slices
-  // per warp cover the longest block, else 16; as many ring slots (2..4) as
-  // keep three CTAs per SM
-  t.warps = t.smax <= 24 ? 8 : 16;
-  const size_t slot = size_t(t.lmax) * 32;
-  t.stages = int(std::max<size_t>(2, std::min<size_t>(4, (72 * 1024 - kTiledHead) / slot)));
+  // default launch shape (spmm_autotune refines it): two slices per consumer
+  // warp (one for blocks of at most 8 slices), two ring slots (on fp 4+4 this
+  // keeps three CTAs per SM, the fastest of 1..3 slices x 2..4 slots)
+  t.rps = t.smax <= 8 ? 1 : (t.smax <= 62 ? 2 : 3);
+  t.warps = (t.smax + t.rps - 1) / t.rps;
+  t.stages = 2;
   t.err.alloc(1);
   h.tiled = tp;
 }
@@ -415,12 +611,19 @@ void tiled_product(const Hamiltonian& h, const float* x, float* y, int ldy, int 
   const TiledOp& t = *h.tiled;
   if (m < 1 || m > 8) throw Error(CG_ERR_ARG, "tiled product takes 1..8 vectors");
   if (reinterpret_cast<uintptr_t>(x) % 16) throw Error(CG_ERR_ARG, "tiled product needs a 16-byte aligned x");
-  if (t.stages < 2 || 2 * t.stages * 8 + 4 > kTiledHead || kTiledHead + size_t(t.stages) * t.lmax * 32 > 227 * 1024)
+  if (t.stages < 2 || 2 * t.stages * 8 + 4 > kTiledHead || tiled_smem(t, t.stages) > 227 * 1024)
     throw Error(CG_ERR_ARG, "tiled product: ring slots out of range");
-  TArgs a{t.bstart.p, t.order.p, t.tptr.p, t.tcb.p, t.runbase.p, t.roff.p, t.col.p, t.val.p, t.lmax, t.stages};
+  TArgs a{t.bstart.p, t.order.p, t.iptr.p, reinterpret_cast<const TItem*>(t.items.p), t.rcopy.p, t.col.p, t.val.p,
+          t.dptr.p, reinterpret_cast<const uint2*>(t.iden.p), t.lmax, t.gmax, t.stages};
   CG_CUDA(cudaMemsetAsync(t.err.p, 0, sizeof(int), s));
-  if (t.warps == 8) launch_nw<8>(t, a, x, y, ldy, m, t.err.p, s);
-  else launch_nw<16>(t, a, x, y, ldy, m, t.err.p, s);
+  if (t.warps != (t.smax + t.rps - 1) / t.rps || t.warps > 31) throw Error(CG_ERR_ARG, "tiled product: bad launch shape");
+  switch (t.rps) {
+    case 1: launch_tiled<1>(t, a, x, y, ldy, m, t.err.p, s); break;
+    case 2: launch_tiled<2>(t, a, x, y, ldy, m, t.err.p, s); break;
+    case 3: launch_tiled<3>(t, a, x, y, ldy, m, t.err.p, s); break;
+    case 4: launch_tiled<4>(t, a, x, y, ldy, m, t.err.p, s); break;
+    default: throw Error(CG_ERR_ARG, "tiled product: slices per warp must be 1..4");
+  }
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, t.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaStreamSynchronize(s));

@@ -230,9 +230,25 @@ cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* c
  * entries including the slice padding. */
 #define CG_FORMAT_ROWS 0
 #define CG_FORMAT_TILED 1
+typedef struct {
+  int32_t format;          /* CG_FORMAT_ROWS or CG_FORMAT_TILED (in use for <= 8 FP32 vectors) */
+  int32_t tiled_available; /* the block-tiled copy exists */
+  int32_t warps, stages;   /* tiled product: consumer warps per CTA, ring slots */
+  int32_t slices_per_warp; /* tiled product: 32-row slices per consumer warp */
+  int32_t reserved;
+  uint64_t entries;        /* tiled entries stored, including the slice padding */
+  uint64_t units;          /* staged units (tile, entry-group range) */
+  uint64_t meta_bytes;     /* per-unit descriptors and run offsets read by one product */
+  uint64_t device_bytes;   /* HBM held by the tiled copy */
+  uint64_t ident_tiles;    /* scaled-identity tiles (one value each, x read in place) */
+  uint64_t ident_entries;  /* stored entries those tiles stand for */
+} cg_spmm_format_info;
 cg_status cg_spmm_set_format(cg_hamiltonian* h, int32_t format);
-cg_status cg_spmm_get_format(const cg_hamiltonian* h, int32_t* format, int32_t* tiled_available,
-                             uint64_t* tiled_entries);
+cg_status cg_spmm_get_format(const cg_hamiltonian* h, cg_spmm_format_info* info);
+/* Launch shape of the tiled product (e.g. from a cached tuning): 32-row slices
+ * per consumer warp (1..4, at most 31 consumer warps) and ring slots (2..7,
+ * within 227 KB of shared memory). */
+cg_status cg_spmm_set_tiled_shape(cg_hamiltonian* h, int32_t slices_per_warp, int32_t stages);
 
 /* -------------------------------------------------------------- Davidson */
 /* Block Davidson for the lowest eigenpairs (Davidson-Liu with diagonal

@@ -72,3 +72,19 @@ def test_tiled_autotune_reports_format(gpu_available, tmp_path):
     fmt = h32.format()[0]
     best = min(res["candidates"], key=lambda c: c[2])
     assert (fmt == cg.CG_FORMAT_TILED) == (best[1] == 0)
+
+
+def test_tiled_tuning_cache_roundtrip(gpu_available, tmp_path):
+    """A cached choice restores the format and the tiled launch shape without timing."""
+    name = "sd66m0s5"
+    cache = str(tmp_path / "tune.json")
+    h1, _ = _h32(name, str(tmp_path))
+    r1 = h1.autotune(nvec=8, reps=2, cache=cache)
+    assert r1["cached"] is False
+    h2, _ = _h32(name, str(tmp_path))
+    h2.set_tiled_shape(1, 2)
+    r2 = h2.autotune(nvec=8, reps=2, cache=cache)
+    assert r2["cached"] is True and r2["format"] == r1["format"]
+    f1, f2 = h1.format_info(), h2.format_info()
+    assert (f1["slices_per_warp"], f1["stages"]) == (f2["slices_per_warp"], f2["stages"])
+    assert h1.tuning()[:2] == h2.tuning()[:2]
