@@ -798,7 +798,7 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
     bs.dims[p] = b.n;
     if (b.n == 0) continue;
     hs[p] = std::make_unique<Hamiltonian>();
-    hamiltonian_build(*sys[p], *ops[p], b, CG_PREC_FP32, *hs[p]);
+    hamiltonian_build(*sys[p], *ops[p], b, CG_PREC_FP32, *hs[p], false);  // rows go into the block-diagonal CSR
     if (b.n <= uint64_t(kDense)) {
       bs.kind[p] = 1;
       bs.slot[p] = nd++;

@@ -612,8 +612,14 @@ cg_status cg_spmm_set_format(cg_hamiltonian* h, int32_t format) {
   return guard([&] {
     CG_NOT_NULL(h);
     if (format != CG_FORMAT_ROWS && format != CG_FORMAT_TILED) throw cg::Error(CG_ERR_ARG, "unknown SpMM format");
+    if (format == CG_FORMAT_TILED && !h->h.tiled && !h->h.virt && h->h.precision == CG_PREC_FP32 &&
+        !h->h.blocks.empty()) {
+      CG_CUDA(cudaSetDevice(h->h.device));
+      cg::tiled_build(h->h, h->h.blocks);  // built on request
+    }
     if (format == CG_FORMAT_TILED && !h->h.tiled)
-      throw cg::Error(CG_ERR_UNSUPPORTED, "no block-tiled copy (FP32 matrix built from a basis, blocks <= 2048 rows)");
+      throw cg::Error(CG_ERR_UNSUPPORTED,
+                      "no block-tiled copy (needs an FP32 matrix built from a basis, blocks <= 1536 rows)");
     h->h.use_tiled = format == CG_FORMAT_TILED;
   });
 }
@@ -678,6 +684,8 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   prm->precond = 1;
   prm->refine_lim = 0;
   prm->refine_keep = 0;
+  prm->ortho_pip = 1;
+  prm->reserved = 0;
 }
 
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
@@ -714,6 +722,7 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     if (algo != 0 && algo != 1) throw cg::Error(CG_ERR_ARG, "algorithm must be -1, 0 or 1");
     c.seq_ortho = !prm->ortho_block && algo == 0;
     c.modern = algo == 1;
+    c.pip = algo == 1 && prm->ortho_pip != 0;
     c.keep = prm->keep;
     c.precond = prm->precond;
     cg::DavidsonRequest rq;

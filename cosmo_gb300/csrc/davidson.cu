@@ -844,6 +844,7 @@ struct Engine {
   double spmm_s = 0;
   // host wall time per phase (verbose >= 2 prints them)
   double t_eig = 0, t_resid = 0, t_ortho = 0, t_collapse = 0, t_abs = 0;
+  int pip_calls_ = 0, pip_fallbacks_ = 0;
   static double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
   }
@@ -1165,11 +1166,69 @@ struct Engine {
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));
   }
+  // Block Gram-Schmidt with Pythagorean inner products, twice (BCGS-PIP2):
+  // one X^T Y over [basis | block] gives the projections G = X^T Y and the
+  // block's Gram M = Y^T Y at once; the projected block's Gram is M - G^T G
+  // (X orthonormal), whose Cholesky factor L gives the whole update in one
+  // product, Y <- [X Y] [-G L^-T ; L^-T].  Two passes of (X^T Y, X G) per
+  // call instead of Gram + scale + 2 x (X^T Y, X G) + 2 x (Gram, Y R^-1).
+  // Returns false (Y possibly updated by a first pass, still spanning the same
+  // space modulo the basis) when the block is nearly inside the basis or a
+  // factorisation fails: the classical form then takes over.
+  bool orthogonalize_pip(int basis_dim, int m) {
+    const int K = basis_dim + m;
+    if (K > 64 || m > 16) return false;
+    const double min_ratio = sizeof(T) == 4 ? 1e-3 : 1e-8;  // |Y_perp|^2 / |Y|^2 below: cancellation
+    for (int pass = 0; pass < 2; ++pass) {
+      std::vector<double> W;
+      xty(B.p, 0, K, B.p, basis_dim, m, W);  // K x m
+      std::vector<double> S(size_t(m) * m), d(m);
+      for (int j = 0; j < m; ++j) {
+        const double mjj = W[size_t(basis_dim + j) * m + j];
+        if (!(mjj > 0.0) || !std::isfinite(mjj)) return false;
+        d[j] = 1.0 / std::sqrt(mjj);
+      }
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) {
+          double v = W[size_t(basis_dim + i) * m + j];
+          for (int k = 0; k < basis_dim; ++k) v -= W[size_t(k) * m + i] * W[size_t(k) * m + j];
+          S[size_t(i) * m + j] = v * d[i] * d[j];  // scaled to unit input columns
+        }
+      for (int j = 0; j < m; ++j)
+        if (!(S[size_t(j) * m + j] > min_ratio)) return false;
+      if (cholesky(m, S) >= 0) return false;
+      // R^-1 = D L^-T (upper triangular in the scaled frame, rescaled)
+      std::vector<double> Ri(size_t(m) * m, 0.0);
+      for (int j = 0; j < m; ++j) {
+        std::vector<double> x(m, 0.0);
+        for (int i = m - 1; i >= 0; --i) {
+          double r = (i == j) ? 1.0 : 0.0;
+          for (int k = i + 1; k < m; ++k) r -= S[size_t(k) * m + i] * x[k];
+          x[i] = r / S[size_t(i) * m + i];
+        }
+        for (int i = 0; i < m; ++i) Ri[size_t(i) * m + j] = d[i] * x[i];
+      }
+      std::vector<double> C(size_t(K) * m, 0.0);
+      for (int k = 0; k < basis_dim; ++k)
+        for (int j = 0; j < m; ++j) {
+          double v = 0.0;
+          for (int i = 0; i < m; ++i) v -= W[size_t(k) * m + i] * Ri[size_t(i) * m + j];
+          C[size_t(k) * m + j] = v;
+        }
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) C[size_t(basis_dim + i) * m + j] = Ri[size_t(i) * m + j];
+      gemm(B.p, 0, K, C, B.p, basis_dim, m, 1.0, 0.0);  // in place: each row read before written
+    }
+    ++pip_calls_;
+    return true;
+  }
   bool orthogonalize_block(int basis_dim, int& nncv) {
     struct Acc { double& t; double t0; ~Acc() { t += now() - t0; } } acc_{t_ortho, now()};
     const double drop = sizeof(T) == 4 ? 1e-8 : 1e-20;  // squared norm after projection
     int m = nncv;
     if (m == 0) return true;
+    if (cfg.pip && orthogonalize_pip(basis_dim, m)) return true;
+    if (cfg.pip) ++pip_fallbacks_;
     std::vector<double> M;
     gram(basis_dim, m, M);
     {
@@ -1340,9 +1399,9 @@ struct Engine {
     if (cfg.verbose >= 2)
       std::fprintf(stderr,
                    "dav[%s] phases: total %.3f s, spmm %.3f, ab+S %.3f, eig %.3f, resid %.3f, ortho %.3f, "
-                   "collapse %.3f (iterations %d)\n",
+                   "collapse %.3f (iterations %d, PIP orthogonalisations %d, fallbacks %d)\n",
                    sizeof(T) == 4 ? "fp32" : "fp64", out.seconds, spmm_s, t_abs, t_eig, t_resid, t_ortho,
-                   t_collapse, nloops);
+                   t_collapse, nloops, pip_calls_, pip_fallbacks_);
     return out;
   }
   bool ierr_stall = false;

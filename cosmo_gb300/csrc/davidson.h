@@ -15,6 +15,7 @@ struct DavConfig {
   double crite = 1e-15, critc = 1e-12, critr = 1e-8, ortho = 1e-9;
   int spmm_prec = 0;   // CG_PREC_*
   bool seq_ortho = true;  // reference one-vector-at-a-time Gram-Schmidt
+  bool pip = false;       // block Gram-Schmidt with Pythagorean inner products (Cholesky-QR folded in)
   bool modern = false;    // residual-driven iteration with thick restart
   int keep = 0;           // Ritz vectors kept at a restart (modern; 0: 2 * nume)
   int precond = 1;        // modern: 1 diagonal preconditioner, 0 plain residuals

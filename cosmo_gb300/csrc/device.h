@@ -153,13 +153,16 @@ struct Hamiltonian {
   SpmmTuning tuning;
   std::shared_ptr<VirtualOp> virt;  // set for the on-the-fly product (nothing stored)
   std::shared_ptr<TiledOp> tiled;   // block-tiled copy of the FP32 values (8-vector product)
+  std::vector<uint64_t> blocks;     // neutron-block starts (+ n) when built from a basis
   bool use_tiled = true;            // route 8-vector FP32 products through `tiled` when present
   cudaStream_t stream = nullptr;
   ~Hamiltonian();
   uint64_t device_bytes() const;  // HBM held by the matrix (or the on-the-fly tables)
 };
 
-void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h);
+// tiled_copy: also build the block-tiled copy of an FP32 matrix (tiled.h)
+void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h,
+                       bool tiled_copy = true);
 void hamiltonian_upper_rows(const Hamiltonian& h, uint64_t row0, uint64_t nrows, uint64_t* rowptr, uint32_t* cols,
                             double* vals);
 // stored H from a .HH file (both triangles rebuilt from the stored upper rows)

@@ -367,7 +367,8 @@ __global__ void k_max_u32(const uint32_t* __restrict__ a, uint64_t n, unsigned* 
 
 }  // namespace
 
-void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h) {
+void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h,
+                       bool tiled_copy) {
   if (precision != CG_PREC_FP64 && precision != CG_PREC_FP32)
     throw Error(CG_ERR_ARG, "Hamiltonian precision must be CG_PREC_FP64 or CG_PREC_FP32");
   CG_CUDA(cudaGetDevice(&h.device));
@@ -487,12 +488,12 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   h.build_seconds = ms * 1e-3;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (precision == CG_PREC_FP32) {
+  h.blocks = b.h_bstart;
+  h.blocks.push_back(b.n);
+  if (precision == CG_PREC_FP32 && tiled_copy && h.nnz >= kTiledMinEntries) {
     // block-tiled copy for the 8-vector product, blocks = neutron blocks
     const auto t0 = std::chrono::steady_clock::now();
-    std::vector<uint64_t> bs = b.h_bstart;
-    bs.push_back(b.n);
-    tiled_build(h, bs);
+    tiled_build(h, h.blocks);
     h.build_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
 }

@@ -137,24 +137,34 @@ __global__ void k_tbalance(uint64_t nruns, const uint32_t* __restrict__ roff, ui
   for (uint64_t r = w0; r < nruns; r += nw) {
     const uint64_t g0 = roff[r];
     const uint32_t w = roff[r + 1] - roff[r];
-    for (uint32_t j = 0; j + 1 < w; ++j) {
-      const uint32_t target = 2 * (((lane >> 1) + j) & 3) + p;
-      const uint32_t jw = min(w, j + 8);
-      uint32_t hit = jw, pad = jw;
-      for (uint32_t q = j; q < jw && hit == jw; ++q) {
-        const uint64_t e = (g0 + q) * 32 + lane;
-        if (val[e] == 0.f) {
-          if (pad == jw) pad = q;
-        } else if (((2u * col[e] + p) & 7u) == target) {
-          hit = q;
+    for (uint32_t j = 0; j < w; ++j) {
+      const uint64_t ej = (g0 + j) * 32 + lane;
+      if (j + 1 < w) {
+        const uint32_t target = 2 * (((lane >> 1) + j) & 3) + p;
+        const uint32_t jw = min(w, j + 8);
+        uint32_t hit = jw, pad = jw;
+        for (uint32_t q = j; q < jw && hit == jw; ++q) {
+          const uint64_t e = (g0 + q) * 32 + lane;
+          if (val[e] == 0.f) {
+            if (pad == jw) pad = q;
+          } else if (((2u * col[e] + p) & 7u) == target) {
+            hit = q;
+          }
+        }
+        const uint32_t best = hit < jw ? hit : (pad < jw ? pad : j);
+        if (best != j) {
+          const uint64_t eb = (g0 + best) * 32 + lane;
+          const uint16_t tc = col[ej]; col[ej] = col[eb]; col[eb] = tc;
+          const float tv = val[ej]; val[ej] = val[eb]; val[eb] = tv;
         }
       }
-      const uint32_t best = hit < jw ? hit : (pad < jw ? pad : j);
-      if (best != j) {
-        const uint64_t ej = (g0 + j) * 32 + lane, eb = (g0 + best) * 32 + lane;
-        const uint16_t tc = col[ej]; col[ej] = col[eb]; col[eb] = tc;
-        const float tv = val[ej]; val[ej] = val[eb]; val[eb] = tv;
-      }
+      // padding (value 0) still reads a row: point it at the row a real lane
+      // of the same parity reads in this step (same address, no extra access)
+      const bool real = val[ej] != 0.f;
+      const uint32_t same = __ballot_sync(0xffffffffu, real) & (p ? 0xaaaaaaaau : 0x55555555u);
+      const uint32_t mine = col[ej];
+      const uint32_t other = __shfl_sync(0xffffffffu, mine, same ? __ffs(same) - 1 : lane);
+      if (!real && same) col[ej] = uint16_t(other);
     }
   }
 }

@@ -48,6 +48,10 @@ struct TiledOp {
   }
 };
 
+// Stored entries from which an FP32 matrix built from a basis gets its tiled
+// copy by default (below, the row-wise kernel is as fast and the copy is
+// built on request, cg_spmm_set_format).
+constexpr uint64_t kTiledMinEntries = uint64_t(1) << 26;
 // Longest block the product's shared-memory staging takes.
 constexpr int kTiledMaxBlock = 1536;
 // Shared memory ahead of the ring of staged units (mbarriers, abort flag).

@@ -165,7 +165,10 @@ __global__ void __launch_bounds__(512) k_virtual(VArgs a, VTab<T> tb, const T* _
   T* un1 = un0 + 32;
   T* Pp = un1 + 32;
 
-  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, sw = lane & 1;
+  // half-swapped row reads (Row) for up to 2 rows per thread: fp 4+4 (2 rows)
+  // 4.46 -> 4.04 ms; with 4 rows per thread (fp 5+5) they measured slower
+  // (75.9 -> 83.2 ms), so those launches read halves in order
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31, sw = RPT <= 2 ? (lane & 1) : 0;
   const uint32_t beta = a.order[blockIdx.x];
   const uint64_t start = a.bstart[beta];
   const int L = int(a.blen[beta]);

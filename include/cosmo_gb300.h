@@ -225,9 +225,10 @@ cg_status cg_spmm_get_tuning(const cg_hamiltonian* h, int32_t* warps, int32_t* c
  * block) pairs, 16-bit in-tile columns, x of the column block staged in shared
  * memory per tile.  The reference's counterpart is its fixed CSB blocking
  * (PPMatrix2CSBBlk, include/sm/PPMatrix.cxx:571-656); the choice of format has
- * no counterpart there.  cg_spmm_autotune picks the faster format (its tiled
- * candidate is reported with ctas_per_sm = 0); tiled_entries counts stored
- * entries including the slice padding. */
+ * no counterpart there.  The copy is built with the matrix from 2^26 stored
+ * entries up, and on request (cg_spmm_set_format(h, CG_FORMAT_TILED)) below.
+ * cg_spmm_autotune picks the faster format when the copy exists (its tiled
+ * candidate is reported with ctas_per_sm = 0). */
 #define CG_FORMAT_ROWS 0
 #define CG_FORMAT_TILED 1
 typedef struct {
@@ -283,6 +284,13 @@ typedef struct {
   int32_t precond;   /* algorithm 1: 1 = diagonal preconditioner (lambda - H_ii), 0 = none */
   int32_t refine_lim;   /* mixed solve: basis limit of the FP64 refinement phase (0: lim) */
   int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep) */
+  int32_t ortho_pip;    /* algorithm 1 (default 1): orthogonalise each new block by two
+                           passes of block Gram-Schmidt with Pythagorean inner products,
+                           the Cholesky-QR of the block folded into the same update
+                           (per pass one X^T Y and one X G over basis + block); falls back
+                           to the classical two passes + Cholesky-QR twice when the block
+                           is nearly inside the basis.  0: always the classical form. */
+  int32_t reserved;
 } cg_davidson_params;
 
 typedef struct {

@@ -161,17 +161,22 @@ def test_davidson_fp64_reference_algorithm(gpu_available, name, tmp_path):
 
 
 @pytest.mark.parametrize("name", ["sd32m1s2", "fp22m0s3", "sd44m0s4", "mg24usdb", "sd66m0s5"])
-def test_davidson_mixed_vs_exact(gpu_available, name, tmp_path):
+@pytest.mark.parametrize("pip", [1, 0])
+def test_davidson_mixed_vs_exact(gpu_available, name, pip, tmp_path):
     """Mixed precision (FP32 H and vectors, FP64 projection, FP64 refinement):
-    lowest eigenvalues within 1e-4 MeV of an exact solve, residuals <= 1e-5."""
+    lowest eigenvalues within 1e-4 MeV of an exact solve, residuals <= 1e-5,
+    orthonormal eigenvectors; with the Pythagorean block orthogonalisation
+    (ortho_pip=1, default) and the classical one (0)."""
     nst = 5 if name == "sd32m1s2" else 10
     exact = _exact(name, str(tmp_path), nst)
     _, _, h = _gpu(name, str(tmp_path), cg.CG_PREC_FP32)
     r = cg.davidson_diagonalization(h, nst, want_vectors=True, precision=cg.CG_PREC_FP32, tol_resid=1e-5,
-                                    block=nst, lim=min(48, nst * 4))
+                                    block=nst, lim=min(48, nst * 4), ortho_pip=pip)
     assert r.stats.converged == nst, (r.resid, r.stats.ierr)
     assert np.all(r.resid <= 1e-5)
     np.testing.assert_allclose(r.eig, exact, rtol=0, atol=1e-4)
+    V = r.vecs
+    np.testing.assert_allclose(V @ V.T, np.eye(nst), rtol=0, atol=1e-8)
 
 
 def test_ee_roundtrip(gpu_available, tmp_path):

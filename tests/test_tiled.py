@@ -16,9 +16,12 @@ NAMES = ["sd22m0s1", "sd32m1s2", "fp21m3s6", "fp22m0s3", "sd44m0s4", "mg24usdb",
 
 
 def _h32(name, tmp):
+    """FP32 matrix with its tiled copy (built on request below 2^26 entries) and the FP64 matrix."""
     p = problem_for(name, tmp)
     b = cg.ManyBodyStates(p)
-    return cg.Hamiltonian(p, b, cg.CG_PREC_FP32), cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
+    h32 = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    h32.set_format(cg.CG_FORMAT_TILED)
+    return h32, cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -38,6 +41,15 @@ def test_tiled_product_matches_oracle(gpu_available, name, tmp_path):
         yr = h32.times_matrix(x, cg.CG_PREC_FP32)
         h32.set_format(cg.CG_FORMAT_TILED)
         np.testing.assert_allclose(yt, yr, rtol=0, atol=2e-6 * scale)
+
+
+def test_tiled_built_on_request_only_below_threshold(gpu_available, tmp_path):
+    p = problem_for("sd66m0s5", str(tmp_path))
+    b = cg.ManyBodyStates(p)
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    assert h.info.nnz_full < 2 ** 26 and h.format()[1] is False
+    h.set_format(cg.CG_FORMAT_TILED)
+    assert h.format()[:2] == (cg.CG_FORMAT_TILED, True)
 
 
 def test_tiled_device_call_and_format_switch(gpu_available, tmp_path):
@@ -83,6 +95,7 @@ def test_tiled_tuning_cache_roundtrip(gpu_available, tmp_path):
     assert r1["cached"] is False
     h2, _ = _h32(name, str(tmp_path))
     h2.set_tiled_shape(1, 2)
+    h2.set_format(cg.CG_FORMAT_ROWS)
     r2 = h2.autotune(nvec=8, reps=2, cache=cache)
     assert r2["cached"] is True and r2["format"] == r1["format"]
     f1, f2 = h1.format_info(), h2.format_info()
