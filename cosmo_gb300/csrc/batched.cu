@@ -458,55 +458,6 @@ __global__ void k_bconv(int Q, int nev, int b, const double* __restrict__ G, dou
   if (threadIdx.x == 0) *nconv = cnt;
 }
 
-// Cholesky of each problem's b x b Gram matrix G = T^T T; writes M = L^{-T}
-// (upper triangular, ld kMaxB) so that T M has orthonormal columns.  A pivot
-// below 1e-24 of the largest diagonal marks the column for replacement.
-__global__ void k_bchol(int Q, int b, const double* __restrict__ G, double* __restrict__ M, int* __restrict__ bad,
-                        const int* __restrict__ fz) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= Q) return;
-  if (fz[q]) {
-    bad[q] = 0;
-    return;
-  }
-  double L[kMaxB][kMaxB], Li[kMaxB][kMaxB];
-  const double* g = G + size_t(q) * (kMaxLim * kMaxB);
-  double dmax = 0.0;
-  for (int i = 0; i < b; ++i) dmax = fmax(dmax, g[i * b + i]);
-  int badmask = 0;
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j <= i; ++j) {
-      double s = g[i * b + j];
-      for (int t = 0; t < j; ++t) s -= L[i][t] * L[j][t];
-      if (i == j) {
-        if (s <= 1e-24 * dmax || !(s > 0.0)) {
-          badmask |= 1 << i;
-          L[i][i] = 1.0;
-          for (int t = 0; t < i; ++t) L[i][t] = 0.0;
-        } else {
-          L[i][i] = sqrt(s);
-        }
-      } else {
-        L[i][j] = (badmask >> i & 1) ? 0.0 : s / L[j][j];
-      }
-    }
-  // Li = L^{-1} (lower)
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j < b; ++j) Li[i][j] = 0.0;
-  for (int j = 0; j < b; ++j) {
-    Li[j][j] = 1.0 / L[j][j];
-    for (int i = j + 1; i < b; ++i) {
-      double s = 0.0;
-      for (int t = j; t < i; ++t) s += L[i][t] * Li[t][j];
-      Li[i][j] = -s / L[i][i];
-    }
-  }
-  double* m = M + size_t(q) * (kMaxLim * kMaxB);
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j < b; ++j) m[i * kMaxB + j] = Li[j][i];  // (L^{-1})^T
-  bad[q] = badmask;
-}
-
 // replace marked columns by a fixed pseudo-random vector (hash of row and column)
 template <class T>
 __global__ void k_bfill(uint32_t nrows, const uint32_t* __restrict__ rowprob, const int* __restrict__ bad, T* V,
@@ -536,16 +487,96 @@ __global__ void k_bset_diag(int keep, const double* __restrict__ w, double* __re
 }
 
 // M[q][i][j] = diag(1 / sqrt(G[q][j][j])) for normalisation (ld kMaxB)
-__global__ void k_bnorm_mat(int Q, int b, const double* __restrict__ G, double* __restrict__ M,
-                            const int* __restrict__ fz) {
+// Block Gram-Schmidt with Pythagorean inner products for each problem: W =
+// [V_basis | T]^T T ((c0 + b) x b, ld b) gives the projections Gp (first c0
+// rows) and the block Gram Mt; S = Mt - Gp^T Gp is the Gram of the projected
+// block.  Columns with |T_perp|^2 / |T|^2 >= min_ratio are orthonormalised by
+// the Cholesky factor of S restricted to them (scaled to unit columns);
+// weaker columns are only projected (the next pass normalises them), and a
+// column with nothing left is marked in bad[] for replacement.  Writes the
+// update coefficients C ((c0 + b) x b, ld kMaxB): T <- [V_basis | T] C.
+__global__ void k_bpip(int Q, int c0, int b, const double* __restrict__ G, double* __restrict__ M,
+                       int* __restrict__ bad, const int* __restrict__ fz, double min_ratio) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= Q || fz[q]) return;
-  double* m = M + size_t(q) * (kMaxLim * kMaxB);
+  if (q >= Q) return;
+  if (fz[q]) {
+    bad[q] = 0;
+    return;
+  }
+  const double* w = G + size_t(q) * (kMaxLim * kMaxB);
+  double* c = M + size_t(q) * (kMaxLim * kMaxB);
+  double S[kMaxB][kMaxB], L[kMaxB][kMaxB], d[kMaxB];
+  int weak = 0, badmask = 0;
+  for (int j = 0; j < b; ++j) {
+    const double mjj = w[(c0 + j) * b + j];
+    d[j] = mjj > 0.0 ? 1.0 / sqrt(mjj) : 0.0;
+    if (!(mjj > 0.0)) badmask |= 1 << j;
+  }
   for (int i = 0; i < b; ++i)
     for (int j = 0; j < b; ++j) {
-      double g = G[size_t(q) * (kMaxLim * kMaxB) + j * b + j];
-      m[i * kMaxB + j] = (i == j) ? (g > 0.0 ? 1.0 / sqrt(g) : 1.0) : 0.0;
+      double v = w[(c0 + i) * b + j];
+      for (int k = 0; k < c0; ++k) v -= w[k * b + i] * w[k * b + j];
+      S[i][j] = v * d[i] * d[j];
     }
+  for (int j = 0; j < b; ++j)
+    if (!(badmask >> j & 1) && !(S[j][j] >= min_ratio)) {
+      weak |= 1 << j;
+      if (!(S[j][j] > 1e-24)) badmask |= 1 << j;  // nothing outside the basis
+    }
+  const int skip = weak | badmask;
+  // Cholesky of S on the healthy columns (skipped rows/columns: identity)
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j <= i; ++j) {
+      if ((skip >> i & 1) || (skip >> j & 1)) {
+        L[i][j] = i == j ? 1.0 : 0.0;
+        continue;
+      }
+      double sum = S[i][j];
+      for (int t = 0; t < j; ++t) sum -= L[i][t] * L[j][t];
+      if (i == j) {
+        if (!(sum > 1e-24)) {  // numerically dependent on the columns before: project only
+          weak |= 1 << i;
+          L[i][i] = 1.0;
+          for (int t = 0; t < i; ++t) L[i][t] = 0.0;
+        } else {
+          L[i][i] = sqrt(sum);
+        }
+      } else {
+        L[i][j] = (weak >> i & 1) ? 0.0 : sum / L[j][j];
+      }
+    }
+  const int proj = weak | badmask;  // columns that are only projected
+  // R = D L^{-T} on the healthy columns, e_j on the others (upper triangular)
+  double R[kMaxB][kMaxB];
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) R[i][j] = 0.0;
+  for (int j = 0; j < b; ++j) {
+    if (proj >> j & 1) {
+      R[j][j] = 1.0;
+      continue;
+    }
+    // x = L^{-T} e_j restricted to healthy indices
+    double x[kMaxB];
+    for (int i = b - 1; i >= 0; --i) {
+      if (proj >> i & 1) {
+        x[i] = 0.0;
+        continue;
+      }
+      double r = i == j ? 1.0 : 0.0;
+      for (int k = i + 1; k < b; ++k) r -= L[k][i] * x[k];
+      x[i] = r / L[i][i];
+    }
+    for (int i = 0; i < b; ++i) R[i][j] = d[i] * x[i];
+  }
+  for (int k = 0; k < c0; ++k)
+    for (int j = 0; j < b; ++j) {
+      double v = 0.0;
+      for (int i = 0; i < b; ++i) v -= w[k * b + i] * R[i][j];
+      c[k * kMaxB + j] = v;
+    }
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) c[(c0 + i) * kMaxB + j] = R[i][j];
+  bad[q] = badmask;
 }
 
 template <class T>
@@ -677,22 +708,18 @@ struct BEngine {
       spmm_refine_df(bs.H, V.p + c0, lim, AV.p + c0, lim, b, dfstage.p, s);
     }
   }
-  // orthonormalise V[:, c0:c0+b] against V[:, 0:c0] and within the block
+  // orthonormalise V[:, c0:c0+b] against V[:, 0:c0] and within the block:
+  // two passes of block Gram-Schmidt with Pythagorean inner products (one
+  // X^T Y and one X C over basis + block per pass, k_bpip)
   void orthonormalise(int c0) {
     const size_t ms = kMaxLim * kMaxB;
-    xty(V.p, lim, c0, b, V.p, lim, c0, b);
-    k_bnorm_mat<<<nblk(Q, 64), 64, 0, s>>>(Q, b, G.p, M.p, fz.p);
-    gemm(V.p, lim, c0, b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
     for (int pass = 0; pass < 2; ++pass) {
-      if (c0 > 0) {
-        for (int rep = 0; rep < 2; ++rep) {
-          xty(V.p, lim, 0, c0, V.p, lim, c0, b);  // G = V^T T (c0 x b)
-          gemm(V.p, lim, 0, c0, G.p, ms, b, V.p, lim, c0, b, -1.0, 1.0);
-        }
-      }
-      xty(V.p, lim, c0, b, V.p, lim, c0, b);
-      k_bchol<<<nblk(Q, 64), 64, 0, s>>>(Q, b, G.p, M.p, bad.p, fz.p);
-      gemm(V.p, lim, c0, b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
+      // first pass: columns mostly inside the basis are only projected; the
+      // second normalises every column that has anything left
+      const double min_ratio = pass ? 0.0 : (sizeof(T) == 4 ? 1e-3 : 1e-8);
+      xty(V.p, lim, 0, c0 + b, V.p, lim, c0, b);  // [V_basis | T]^T T
+      k_bpip<<<nblk(Q, 64), 64, 0, s>>>(Q, c0, b, G.p, M.p, bad.p, fz.p, min_ratio);
+      gemm(V.p, lim, 0, c0 + b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
       k_bfill<T><<<nblk(N), 256, 0, s>>>(N, bs.rowprob.p, bad.p, V.p, lim, c0, b, 0x1234567u + pass, fz.p);
     }
   }
