@@ -62,23 +62,35 @@ __global__ void k_dense_fill(int n, uint64_t r0, const uint64_t* __restrict__ rp
 }
 
 // ------------------------------------------------ batched Jacobi eigensolver
-// One CTA per matrix: A (k x k, symmetric, FP64, ld kJac) -> eigenvalues
-// ascending w[0..k) and eigenvectors Z (column j of the k x k block, ld kJac).
-// Cyclic Jacobi with the round-robin ordering: each round applies k/2 disjoint
-// rotations at once; sweeps repeat until the off-diagonal norm falls below
-// 1e-15 of the Frobenius norm (at most 40 sweeps).
-constexpr size_t kJacSmem = (size_t(2) * kJac * (kJac + 1) + 256 + kJac) * sizeof(double) + (2 * kJac + 8) * sizeof(int);
+// One CTA per matrix: A (k x k, symmetric, FP64 in, ld kJac) -> eigenvalues
+// ascending w[0..k) and eigenvectors Z (column j of the k x k block, ld kJac),
+// computed in R (FP64 here: off-diagonal norm down to 1e-15 of the Frobenius
+// norm; an FP32 Jacobi for the FP32 phase measured 0.43 instead of 1.08 ms
+// per launch but its Ritz vectors, off by ~eps32 |S| / gap, kept the phase
+// from reaching its 1e-4 residuals: 300 instead of 133 iterations).  Cyclic
+// Jacobi with the round-robin ordering: each round applies k/2 disjoint
+// rotations at once, skipping those whose |a_pq| is below 1e-17 (FP32: 1e-7)
+// of sqrt|a_pp a_qq|; at most 40 sweeps.
+template <class R>
+constexpr size_t jac_smem() {
+  return (size_t(2) * kJac * (kJac + 1) + 256 + kJac) * sizeof(R) + (2 * kJac + 8) * sizeof(int);
+}
 
+template <class R>
 __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain, const int* __restrict__ kdim,
                                                  int kconst, double* __restrict__ w, double* __restrict__ Zout,
                                                  const int* __restrict__ fz) {
+  constexpr R kConv = sizeof(R) == 4 ? R(1e-12) : R(1e-30);   // (off / total)^2 at convergence
+  constexpr R kTiny = sizeof(R) == 4 ? R(1e-30) : R(1e-300);
+  constexpr R kSkip = sizeof(R) == 4 ? R(1e-7) : R(1e-17);
   if (fz && fz[blockIdx.x]) return;
-  extern __shared__ double jsm[];
-  double(*A)[kJac + 1] = reinterpret_cast<double(*)[kJac + 1]>(jsm);
-  double(*Z)[kJac + 1] = reinterpret_cast<double(*)[kJac + 1]>(jsm + kJac * (kJac + 1));
-  double* red = jsm + 2 * kJac * (kJac + 1);
-  double* rc = red + 256;
-  double* rs = rc + kJac / 2;
+  extern __shared__ __align__(16) unsigned char jsm_raw[];
+  R* jsm = reinterpret_cast<R*>(jsm_raw);
+  R(*A)[kJac + 1] = reinterpret_cast<R(*)[kJac + 1]>(jsm);
+  R(*Z)[kJac + 1] = reinterpret_cast<R(*)[kJac + 1]>(jsm + kJac * (kJac + 1));
+  R* red = jsm + 2 * kJac * (kJac + 1);
+  R* rc = red + 256;
+  R* rs = rc + kJac / 2;
   int* rp = reinterpret_cast<int*>(rs + kJac / 2);
   int* rq = rp + kJac / 2;
   int* order = rq + kJac / 2;
@@ -88,17 +100,17 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   const double* Ab = Ain + size_t(b) * kJac * kJac;
   for (int i = tid; i < kJac * kJac; i += blockDim.x) {
     const int r = i / kJac, c = i % kJac;
-    A[r][c] = (r < k && c < k) ? Ab[r * kJac + c] : 0.0;
-    Z[r][c] = r == c ? 1.0 : 0.0;
+    A[r][c] = (r < k && c < k) ? R(Ab[r * kJac + c]) : R(0);
+    Z[r][c] = r == c ? R(1) : R(0);
   }
   __syncthreads();
   const int kk = k + (k & 1);  // even player count; player k (if odd) is idle
   for (int sweep = 0; sweep < 40 && k > 1; ++sweep) {
     // convergence: off-diagonal vs total
-    double off = 0.0, tot = 0.0;
+    R off = 0, tot = 0;
     for (int i = tid; i < k * k; i += blockDim.x) {
       const int r = i / k, c = i % k;
-      const double v = A[r][c] * A[r][c];
+      const R v = A[r][c] * A[r][c];
       tot += v;
       if (r != c) off += v;
     }
@@ -108,7 +120,7 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
       if (tid < s) red[tid] += red[tid + s];
       __syncthreads();
     }
-    const double offs = red[0];
+    const R offs = red[0];
     __syncthreads();
     red[tid] = tot;
     __syncthreads();
@@ -116,7 +128,7 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
       if (tid < s) red[tid] += red[tid + s];
       __syncthreads();
     }
-    if (tid == 0) done = offs <= 1e-30 * red[0] || offs == 0.0;
+    if (tid == 0) done = offs <= kConv * red[0] || offs == R(0);
     __syncthreads();
     if (done) break;
     for (int round = 0; round < kk - 1; ++round) {
@@ -125,18 +137,20 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
         auto player = [&](int pos) { return pos == 0 ? 0 : 1 + (pos - 1 + round) % (kk - 1); };
         int p = player(tid), q = player(kk - 1 - tid);
         if (p > q) { int t = p; p = q; q = t; }
-        double c = 1.0, s = 0.0;
+        R c = 1, s = 0;
+        bool rot = false;
         if (q < k) {
-          const double apq = A[p][q];
-          if (fabs(apq) > 1e-300) {
-            const double tau = (A[q][q] - A[p][p]) / (2.0 * apq);
-            const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + t * t);
+          const R apq = A[p][q];
+          if (fabs(apq) > kTiny && fabs(apq) > kSkip * sqrt(fabs(A[p][p] * A[q][q]))) {
+            const R tau = (A[q][q] - A[p][p]) / (R(2) * apq);
+            const R t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
+            c = R(1) / sqrt(R(1) + t * t);
             s = t * c;
+            rot = true;
           }
         }
         rp[tid] = p;
-        rq[tid] = q;
+        rq[tid] = rot ? q : kJac;  // kJac: no rotation this round
         rc[tid] = c;
         rs[tid] = s;
       }
@@ -146,8 +160,8 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
         const int pr = i / k, j = i % k;
         const int p = rp[pr], q = rq[pr];
         if (q < k) {
-          const double c = rc[pr], s = rs[pr];
-          const double ap = A[p][j], aq = A[q][j];
+          const R c = rc[pr], s = rs[pr];
+          const R ap = A[p][j], aq = A[q][j];
           A[p][j] = c * ap - s * aq;
           A[q][j] = s * ap + c * aq;
         }
@@ -158,11 +172,11 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
         const int pr = i / k, j = i % k;
         const int p = rp[pr], q = rq[pr];
         if (q < k) {
-          const double c = rc[pr], s = rs[pr];
-          const double ap = A[j][p], aq = A[j][q];
+          const R c = rc[pr], s = rs[pr];
+          const R ap = A[j][p], aq = A[j][q];
           A[j][p] = c * ap - s * aq;
           A[j][q] = s * ap + c * aq;
-          const double zp = Z[j][p], zq = Z[j][q];
+          const R zp = Z[j][p], zq = Z[j][q];
           Z[j][p] = c * zp - s * zq;
           Z[j][q] = s * zp + c * zq;
         }
@@ -173,9 +187,9 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   // ascending order (ties by index)
   for (int i = tid; i < k; i += blockDim.x) {
     int rank = 0;
-    const double di = A[i][i];
+    const R di = A[i][i];
     for (int j = 0; j < k; ++j) {
-      const double dj = A[j][j];
+      const R dj = A[j][j];
       rank += (dj < di) || (dj == di && j < i);
     }
     order[rank] = i;
@@ -183,10 +197,10 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   __syncthreads();
   double* wb = w + size_t(b) * kJac;
   double* Zb = Zout + size_t(b) * kJac * kJac;
-  for (int i = tid; i < kJac; i += blockDim.x) wb[i] = i < k ? A[order[i]][order[i]] : 0.0;
+  for (int i = tid; i < kJac; i += blockDim.x) wb[i] = i < k ? double(A[order[i]][order[i]]) : 0.0;
   for (int i = tid; i < kJac * kJac; i += blockDim.x) {
     const int r = i / kJac, c = i % kJac;
-    Zb[r * kJac + c] = (r < k && c < k) ? Z[r][order[c]] : 0.0;
+    Zb[r * kJac + c] = (r < k && c < k) ? double(Z[r][order[c]]) : 0.0;
   }
 }
 
@@ -495,88 +509,102 @@ __global__ void k_bset_diag(int keep, const double* __restrict__ w, double* __re
 // weaker columns are only projected (the next pass normalises them), and a
 // column with nothing left is marked in bad[] for replacement.  Writes the
 // update coefficients C ((c0 + b) x b, ld kMaxB): T <- [V_basis | T] C.
-__global__ void k_bpip(int Q, int c0, int b, const double* __restrict__ G, double* __restrict__ M,
-                       int* __restrict__ bad, const int* __restrict__ fz, double min_ratio) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(64) k_bpip(int Q, int c0, int b, const double* __restrict__ G,
+                                              double* __restrict__ M, int* __restrict__ bad,
+                                              const int* __restrict__ fz, double min_ratio) {
+  // one CTA of 64 threads per problem: the b x b Gram correction and the
+  // (c0 + b) x b coefficients in parallel, the b x b factorisation on thread 0
+  const int q = blockIdx.x, tid = threadIdx.x;
   if (q >= Q) return;
   if (fz[q]) {
-    bad[q] = 0;
+    if (tid == 0) bad[q] = 0;
     return;
   }
-  const double* w = G + size_t(q) * (kMaxLim * kMaxB);
-  double* c = M + size_t(q) * (kMaxLim * kMaxB);
-  double S[kMaxB][kMaxB], L[kMaxB][kMaxB], d[kMaxB];
-  int weak = 0, badmask = 0;
-  for (int j = 0; j < b; ++j) {
-    const double mjj = w[(c0 + j) * b + j];
-    d[j] = mjj > 0.0 ? 1.0 / sqrt(mjj) : 0.0;
-    if (!(mjj > 0.0)) badmask |= 1 << j;
+  __shared__ double w[kMaxLim * kMaxB], S[kMaxB][kMaxB], R[kMaxB][kMaxB], d[kMaxB];
+  __shared__ int bmask;
+  const int K = c0 + b;
+  for (int i = tid; i < K * b; i += blockDim.x) w[i] = G[size_t(q) * (kMaxLim * kMaxB) + i];
+  __syncthreads();
+  if (tid < b) {
+    const double mjj = w[(c0 + tid) * b + tid];
+    d[tid] = mjj > 0.0 ? 1.0 / sqrt(mjj) : 0.0;
   }
-  for (int i = 0; i < b; ++i)
+  __syncthreads();
+  for (int t = tid; t < b * b; t += blockDim.x) {
+    const int i = t / b, j = t % b;
+    double v = w[(c0 + i) * b + j];
+    for (int k = 0; k < c0; ++k) v -= w[k * b + i] * w[k * b + j];
+    S[i][j] = v * d[i] * d[j];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int weak = 0, badmask = 0;
     for (int j = 0; j < b; ++j) {
-      double v = w[(c0 + i) * b + j];
-      for (int k = 0; k < c0; ++k) v -= w[k * b + i] * w[k * b + j];
-      S[i][j] = v * d[i] * d[j];
-    }
-  for (int j = 0; j < b; ++j)
-    if (!(badmask >> j & 1) && !(S[j][j] >= min_ratio)) {
-      weak |= 1 << j;
-      if (!(S[j][j] > 1e-24)) badmask |= 1 << j;  // nothing outside the basis
-    }
-  const int skip = weak | badmask;
-  // Cholesky of S on the healthy columns (skipped rows/columns: identity)
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j <= i; ++j) {
-      if ((skip >> i & 1) || (skip >> j & 1)) {
-        L[i][j] = i == j ? 1.0 : 0.0;
-        continue;
+      if (!(d[j] > 0.0)) badmask |= 1 << j;
+      else if (!(S[j][j] >= min_ratio)) {
+        weak |= 1 << j;
+        if (!(S[j][j] > 1e-24)) badmask |= 1 << j;  // nothing outside the basis
       }
-      double sum = S[i][j];
-      for (int t = 0; t < j; ++t) sum -= L[i][t] * L[j][t];
-      if (i == j) {
-        if (!(sum > 1e-24)) {  // numerically dependent on the columns before: project only
-          weak |= 1 << i;
-          L[i][i] = 1.0;
-          for (int t = 0; t < i; ++t) L[i][t] = 0.0;
-        } else {
-          L[i][i] = sqrt(sum);
+    }
+    const int skip = weak | badmask;
+    // Cholesky of S on the healthy columns (skipped rows/columns: identity)
+    double L[kMaxB][kMaxB];
+    for (int i = 0; i < b; ++i)
+      for (int j = 0; j <= i; ++j) {
+        if ((skip >> i & 1) || (skip >> j & 1)) {
+          L[i][j] = i == j ? 1.0 : 0.0;
+          continue;
         }
-      } else {
-        L[i][j] = (weak >> i & 1) ? 0.0 : sum / L[j][j];
+        double sum = S[i][j];
+        for (int t = 0; t < j; ++t) sum -= L[i][t] * L[j][t];
+        if (i == j) {
+          if (!(sum > 1e-24)) {  // numerically dependent on the columns before: project only
+            weak |= 1 << i;
+            L[i][i] = 1.0;
+            for (int t = 0; t < i; ++t) L[i][t] = 0.0;
+          } else {
+            L[i][i] = sqrt(sum);
+          }
+        } else {
+          L[i][j] = (weak >> i & 1) ? 0.0 : sum / L[j][j];
+        }
       }
-    }
-  const int proj = weak | badmask;  // columns that are only projected
-  // R = D L^{-T} on the healthy columns, e_j on the others (upper triangular)
-  double R[kMaxB][kMaxB];
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j < b; ++j) R[i][j] = 0.0;
-  for (int j = 0; j < b; ++j) {
-    if (proj >> j & 1) {
-      R[j][j] = 1.0;
-      continue;
-    }
-    // x = L^{-T} e_j restricted to healthy indices
-    double x[kMaxB];
-    for (int i = b - 1; i >= 0; --i) {
-      if (proj >> i & 1) {
-        x[i] = 0.0;
+    const int proj = weak | badmask;  // columns that are only projected
+    // R = D L^{-T} on the healthy columns, e_j on the others (upper triangular)
+    for (int j = 0; j < b; ++j) {
+      for (int i = 0; i < b; ++i) R[i][j] = 0.0;
+      if (proj >> j & 1) {
+        R[j][j] = 1.0;
         continue;
       }
-      double r = i == j ? 1.0 : 0.0;
-      for (int k = i + 1; k < b; ++k) r -= L[k][i] * x[k];
-      x[i] = r / L[i][i];
+      double x[kMaxB];
+      for (int i = b - 1; i >= 0; --i) {
+        if (proj >> i & 1) {
+          x[i] = 0.0;
+          continue;
+        }
+        double r = i == j ? 1.0 : 0.0;
+        for (int k = i + 1; k < b; ++k) r -= L[k][i] * x[k];
+        x[i] = r / L[i][i];
+      }
+      for (int i = 0; i < b; ++i) R[i][j] = d[i] * x[i];
     }
-    for (int i = 0; i < b; ++i) R[i][j] = d[i] * x[i];
+    bmask = badmask;
   }
-  for (int k = 0; k < c0; ++k)
-    for (int j = 0; j < b; ++j) {
-      double v = 0.0;
+  __syncthreads();
+  double* c = M + size_t(q) * (kMaxLim * kMaxB);
+  for (int t = tid; t < K * b; t += blockDim.x) {
+    const int k = t / b, j = t % b;
+    double v;
+    if (k < c0) {
+      v = 0.0;
       for (int i = 0; i < b; ++i) v -= w[k * b + i] * R[i][j];
-      c[k * kMaxB + j] = v;
+    } else {
+      v = R[k - c0][j];
     }
-  for (int i = 0; i < b; ++i)
-    for (int j = 0; j < b; ++j) c[(c0 + i) * kMaxB + j] = R[i][j];
-  bad[q] = badmask;
+    c[k * kMaxB + j] = v;
+  }
+  if (tid == 0) bad[q] = bmask;
 }
 
 template <class T>
@@ -718,7 +746,7 @@ struct BEngine {
       // second normalises every column that has anything left
       const double min_ratio = pass ? 0.0 : (sizeof(T) == 4 ? 1e-3 : 1e-8);
       xty(V.p, lim, 0, c0 + b, V.p, lim, c0, b);  // [V_basis | T]^T T
-      k_bpip<<<nblk(Q, 64), 64, 0, s>>>(Q, c0, b, G.p, M.p, bad.p, fz.p, min_ratio);
+      k_bpip<<<Q, 64, 0, s>>>(Q, c0, b, G.p, M.p, bad.p, fz.p, min_ratio);
       gemm(V.p, lim, 0, c0 + b, M.p, ms, kMaxB, V.p, lim, c0, b, 1.0, 0.0);
       k_bfill<T><<<nblk(N), 256, 0, s>>>(N, bs.rowprob.p, bad.p, V.p, lim, c0, b, 0x1234567u + pass, fz.p);
     }
@@ -728,7 +756,7 @@ struct BEngine {
     spmm(k - b);
     xty(V.p, lim, 0, k, AV.p, lim, k - b, b);
     k_bset_proj<<<Q, 128, 0, s>>>(k, b, k - b, G.p, S.p, fz.p);
-    k_bjacobi<<<Q, 256, kJacSmem, s>>>(S.p, nullptr, k, w.p, Z.p, fz.p);
+    k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p);
     k_bresid<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, V.p, AV.p, lim, k, w.p, Z.p, R.p, 8, b, fz.p);
     xty(R.p, 8, 0, b, R.p, 8, 0, b);
     k_bconv<<<1, 256, 0, s>>>(Q, nev, b, G.p, tol, rnorm.p, fz.p, kfreeze.p, k, nconv.p);
@@ -906,7 +934,8 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
 }
 
 void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
-  CG_CUDA(cudaFuncSetAttribute(k_bjacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kJacSmem)));
+  CG_CUDA(cudaFuncSetAttribute(k_bjacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(jac_smem<double>())));
   if (prm.nev < 1 || prm.nev > kMaxB) throw Error(CG_ERR_ARG, "batched solve: nstates must be in 1..8");
   if (prm.block < prm.nev || prm.block > kMaxB) throw Error(CG_ERR_ARG, "batched solve: block must be in nstates..8");
   if (prm.lim > kMaxLim || prm.keep < prm.block || prm.keep + prm.block > prm.lim)
@@ -925,7 +954,7 @@ void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
     DBuf<double> w(size_t(bs.nd) * kJac), Z(size_t(bs.nd) * kJac * kJac);
     DBuf<int> kd;
     kd.upload(bs.ddim, s);
-    k_bjacobi<<<bs.nd, 256, kJacSmem, s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr);
+    k_bjacobi<double><<<bs.nd, 256, jac_smem<double>(), s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr);
     CG_CUDA(cudaGetLastError());
     count_launch();
     dw.resize(size_t(bs.nd) * kJac);
