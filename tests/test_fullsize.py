@@ -1,0 +1,81 @@
+"""Full-size workloads (fp 4+4, n = 1,963,461; fp 5+5, n = 18,600,516) checked
+through size-independent properties, since the oracle cannot run them in
+seconds: basis sizes, the block-tiled product against the row-wise product,
+symmetry (x . H y = y . H x, dots accumulated in FP64) and linearity of the
+stored and on-the-fly products, and the on-the-fly product against the stored
+one.  Tolerances: 2e-6 of max|y| between the two FP32 stored kernels (same
+values, different summation order), 1e-5 for FP32 products against each other
+or in linear combinations, 1e-6 relative for the FP32 symmetry defect."""
+import numpy as np
+import pytest
+
+import cosmo_gb300 as cg
+from cosmo_gb300.synthetic import SyntheticSystem, make_system
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _system(tmp, space, nv, zv, seed):
+    xml = make_system(str(tmp), SyntheticSystem(space, nv, zv, 0, "+", 0.5, seed))[1]
+    p = cg.Problem(xml)
+    return p, cg.ManyBodyStates(p)
+
+
+def _prod(h, x, prec=cg.CG_PREC_FP32):
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    h.spmm_device(x.data_ptr(), x.shape[1], y.data_ptr(), y.shape[1], x.shape[1], prec)
+    torch.cuda.synchronize()
+    return y
+
+
+def _sym_defect(h, n, gen):
+    x = torch.randn(n, 8, generator=gen, dtype=torch.float32).cuda()
+    y = torch.randn(n, 8, generator=gen, dtype=torch.float32).cuda()
+    hx, hy = _prod(h, x), _prod(h, y)
+    a = (x.double() * hy.double()).sum(0)
+    b = (y.double() * hx.double()).sum(0)
+    scale = (x.double().norm(dim=0) * hy.double().norm(dim=0))
+    return float(((a - b).abs() / scale).max())
+
+
+def test_fp44_tiled_rows_symmetry_linearity(gpu_available, tmp_path):
+    p, b = _system(tmp_path, "fp", 4, 4, 7)
+    assert b.n == 1963461
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    fi = h.format_info()
+    assert fi["tiled_available"] and fi["entries"] >= h.info.nnz_full
+    gen = torch.Generator().manual_seed(44)
+    x = torch.randn(b.n, 8, generator=gen, dtype=torch.float32).cuda()
+    h.set_format(cg.CG_FORMAT_TILED)
+    yt = _prod(h, x)
+    h.set_format(cg.CG_FORMAT_ROWS)
+    yr = _prod(h, x)
+    h.set_format(cg.CG_FORMAT_TILED)
+    scale = float(yr.abs().max())
+    assert float((yt - yr).abs().max()) <= 2e-6 * scale
+    # symmetry and linearity of the tiled product at full size
+    assert _sym_defect(h, b.n, gen) <= 1e-6
+    z = torch.randn(b.n, 8, generator=gen, dtype=torch.float32).cuda()
+    lhs = _prod(h, 2 * x + 3 * z)
+    rhs = 2 * yt + 3 * _prod(h, z)
+    assert float((lhs - rhs).abs().max()) <= 1e-5 * float(rhs.abs().max())
+    # the on-the-fly product of the same operator
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
+    yv = _prod(hv, x)
+    assert float((yv - yt).abs().max()) <= 1e-5 * scale
+
+
+def test_fp55_on_the_fly_symmetry_linearity(gpu_available, tmp_path):
+    p, b = _system(tmp_path, "fp", 5, 5, 8)
+    assert b.n == 18600516
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
+    gen = torch.Generator().manual_seed(55)
+    assert _sym_defect(hv, b.n, gen) <= 1e-6
+    x = torch.randn(b.n, 8, generator=gen, dtype=torch.float32).cuda()
+    z = torch.randn(b.n, 8, generator=gen, dtype=torch.float32).cuda()
+    lhs = _prod(hv, 2 * x - 0.5 * z)
+    rhs = 2 * _prod(hv, x) - 0.5 * _prod(hv, z)
+    assert float((lhs - rhs).abs().max()) <= 1e-5 * float(rhs.abs().max())
