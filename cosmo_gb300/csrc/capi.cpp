@@ -685,7 +685,7 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   prm->refine_lim = 0;
   prm->refine_keep = 0;
   prm->ortho_pip = 1;
-  prm->reserved = 0;
+  prm->refine_block = 0;
 }
 
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
@@ -747,6 +747,10 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
         c2.lim = prm->refine_lim;
       }
       if (prm->refine_keep > 0) c2.keep = prm->refine_keep;
+      if (prm->refine_block > 0) {
+        if (prm->refine_block > 16) throw cg::Error(CG_ERR_ARG, "refine_block must be in 1..16");
+        c2.block = prm->refine_block;
+      }
       if (c2.keep + c2.block > c2.lim) c2.keep = std::max(nume, c2.lim - c2.block);
 
       rq.phase2 = c2;

@@ -290,7 +290,7 @@ typedef struct {
                            (per pass one X^T Y and one X G over basis + block); falls back
                            to the classical two passes + Cholesky-QR twice when the block
                            is nearly inside the basis.  0: always the classical form. */
-  int32_t reserved;
+  int32_t refine_block; /* mixed solve: vectors added per refinement iteration (0: block) */
 } cg_davidson_params;
 
 typedef struct {
