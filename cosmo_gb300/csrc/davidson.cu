@@ -482,6 +482,18 @@ __global__ void __launch_bounds__(256, 4) k_xty_t(uint64_t n, const T* __restric
 // R[:, c] = AB s_c - lam_c B s_c for C candidates, one thread per row with the
 // row read 4 values at a time, s in shared memory; per-CTA partial |R[:, c]|^2
 // (FP32 over a thread's rows, FP64 across threads, fixed order).
+// 32-byte load of 8 consecutive floats (32-byte aligned address): one L1
+// request per thread for a whole 8-float segment of a row (thread-per-row
+// kernels read rows 256 bytes apart, so every request touches one sector per
+// lane; halving the requests halves the L1 work).  Coherent (not .nc): the
+// gemm may write the rows it reads.
+__device__ __forceinline__ void ld8c(const float* p, float (&v)[8]) {
+  asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "l"(p)
+               : "memory");
+}
+
 template <class T, int CMAX>
 __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
                                                  int ld, int K, const double* __restrict__ Sc,
@@ -500,43 +512,37 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
 #pragma unroll
   for (int c = 0; c < CMAX; ++c) nrm[c] = T(0);
   for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
-    T a[CMAX], b[CMAX];
+    // res_c = sum_k (AB_k - lam_c B_k) s_kc: one accumulator per candidate
+    T res[CMAX];
 #pragma unroll
-    for (int c = 0; c < CMAX; ++c) { a[c] = T(0); b[c] = T(0); }
+    for (int c = 0; c < CMAX; ++c) res[c] = T(0);
     const T* br = B + r * ld;
     const T* abr = AB + r * ld;
     int k = 0;
     if constexpr (sizeof(T) == 4) {
-      if (vec) {
-        for (; k + 4 <= K; k += 4) {
-          const float4 bv = *reinterpret_cast<const float4*>(br + k);
-          const float4 av = *reinterpret_cast<const float4*>(abr + k);
-          const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, aa[4] = {av.x, av.y, av.z, av.w};
+      if (vec) {  // rows 32-byte aligned
+        for (; k + 8 <= K; k += 8) {
+          float bb[8], aa[8];
+          ld8c(br + k, bb);
+          ld8c(abr + k, aa);
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
+          for (int u = 0; u < 8; ++u)
 #pragma unroll
-            for (int c = 0; c < CMAX; ++c) {
-              const T sv = ss[(k + u) * CMAX + c];
-              a[c] = fma(aa[u], sv, a[c]);
-              b[c] = fma(bb[u], sv, b[c]);
-            }
+            for (int c = 0; c < CMAX; ++c)
+              res[c] = fma(fma(-ls[c], bb[u], aa[u]), ss[(k + u) * CMAX + c], res[c]);
         }
       }
     }
     for (; k < K; ++k) {
       const T bv = br[k], av = abr[k];
 #pragma unroll
-      for (int c = 0; c < CMAX; ++c) {
-        a[c] = fma(av, ss[k * CMAX + c], a[c]);
-        b[c] = fma(bv, ss[k * CMAX + c], b[c]);
-      }
+      for (int c = 0; c < CMAX; ++c) res[c] = fma(fma(-ls[c], bv, av), ss[k * CMAX + c], res[c]);
     }
 #pragma unroll
     for (int c = 0; c < CMAX; ++c)
       if (c < C) {
-        const T res = a[c] - ls[c] * b[c];
-        R[r * ldr + c] = res;
-        nrm[c] = fma(res, res, nrm[c]);
+        R[r * ldr + c] = res[c];
+        nrm[c] = fma(res[c], res[c], nrm[c]);
       }
   }
   // CTA partials: warp shuffles then the 8 warps in order
@@ -557,7 +563,7 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
 
 // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G, one thread per row, all J
 // outputs of the row in registers, G (alpha folded in) in shared memory read
-// as broadcast; X rows read 4 values at a time when 16-byte aligned.  A row is
+// as broadcast; FP32 X rows read 8 values (32 bytes) at a time when aligned.  A row is
 // read completely before it is written, so X and Y may alias.
 template <class T, int JMAX>
 __global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx, int xo, int K,
@@ -577,12 +583,12 @@ __global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx,
     const T* xr = X + r * ldx + xo;
     int k = 0;
     if constexpr (sizeof(T) == 4) {
-      if (vec_x) {
-        for (; k + 4 <= K; k += 4) {
-          const float4 v = *reinterpret_cast<const float4*>(xr + k);
-          const float xv[4] = {v.x, v.y, v.z, v.w};
+      if (vec_x) {  // row segment 32-byte aligned
+        for (; k + 8 <= K; k += 8) {
+          float xv[8];
+          ld8c(xr + k, xv);
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
+          for (int u = 0; u < 8; ++u)
 #pragma unroll
             for (int j = 0; j < JMAX; ++j) acc[j] = fma(xv[u], gs[(k + u) * JMAX + j], acc[j]);
         }
@@ -931,7 +937,7 @@ struct Engine {
   // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
-    const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 16 == 0 && L % 4 == 0;
+    const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
     const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     if constexpr (sizeof(T) == 8) {
       if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
@@ -1058,7 +1064,8 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(small2.p, Sc.data(), sizeof(double) * Sc.size(), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(dlam.p, lam.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s));
     const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
-    const bool vec = L % 4 == 0;
+    const bool vec = L % 8 == 0 && reinterpret_cast<uintptr_t>(B.p) % 32 == 0 &&
+                     reinterpret_cast<uintptr_t>(AB.p) % 32 == 0;
     bool done = false;
     if constexpr (sizeof(T) == 8) {
       if (cfg.spmm_prec == CG_PREC_REFINE) {
