@@ -149,7 +149,7 @@ struct Row<double, 4> {
 };
 
 template <class T, int VB, int RPT>
-__global__ void __launch_bounds__(512) k_virtual(VArgs a, VTab<T> tb, const T* __restrict__ x, T* __restrict__ y,
+__global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab<T> tb, const T* __restrict__ x, T* __restrict__ y,
                                                  int ldy, int m, int* __restrict__ err) {
   // shared memory: [3 mbarriers | pad to 128 B] own buf0 buf1 (lmax x VB each)
   //                wsl0 wsl1 (np*np + 1, last = 0) un0 un1 (32) Pp (np*np + 1, last = 0)
@@ -399,8 +399,13 @@ void virtual_product(const Hamiltonian& h, const T* x, T* y, int ldy, int m, con
   const int npp = v.np * v.np;
   const size_t smem = kVirtualSmemHead + (size_t(3) * v.lmax * VB + 3 * size_t(npp + 4) + 64) * sizeof(T);
   if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "neutron block too long for the shared-memory staging");
+  // rows per thread: threads <= 512, or <= 1024 when the staging buffers
+  // leave room for one CTA per SM only (long blocks, e.g. fp 5+5): there two
+  // rows per thread and twice the warps hide the shared-memory latency better
+  // than four rows per thread
+  const int thread_cap = smem > 113 * 1024 ? 1024 : 512;
   int rpt = 1;
-  while ((v.lmax + rpt - 1) / rpt > 512) rpt <<= 1;
+  while ((v.lmax + rpt - 1) / rpt > thread_cap) rpt <<= 1;
   int threads = (v.lmax + rpt - 1) / rpt;
   threads = std::max(64, (threads + 31) / 32 * 32);
   if (rpt > 8) throw Error(CG_ERR_UNSUPPORTED, "neutron block longer than 4096 rows");
