@@ -462,6 +462,7 @@ def virtual_subbench(cg, fp64_iters):
 
     ms32 = product_ms(cg.CG_PREC_FP32, 8, 5)
     ms64 = product_ms(cg.CG_PREC_FP64, 4, 2)
+    msdf = product_ms(cg.CG_PREC_REFINE, 4, 2)  # double-float (refinement) product
     kw = dict(precision=cg.CG_PREC_FP32, tol_resid=TOL, **MIXED)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -477,6 +478,8 @@ def virtual_subbench(cg, fp64_iters):
     return {"workload": "fp-shell 5p+5n M=0, lowest 10 eigenpairs, resid<=1e-5, on-the-fly product",
             "n": int(n), "connections_per_product": conn, "table_bytes": int(hv.info.device_bytes),
             "setup_seconds": setup, "fp32_product_ms_8vec": ms32, "fp64_product_ms_4vec": ms64,
+            "double_float_product_ms_4vec": msdf,
+            "product_timing_note": "device API calls: pack kernel + product, staging buffer allocated per call",
             "fp32_connection_vectors_per_s": conn * 8 / (ms32 * 1e-3),
             "fp64_connection_vectors_per_s": conn * 4 / (ms64 * 1e-3),
             "mixed_solve_seconds": mixed, "mixed_iterations": int(r.stats.iterations),

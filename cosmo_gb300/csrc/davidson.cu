@@ -978,6 +978,13 @@ struct Engine {
           virtual_pack_f32(n, reinterpret_cast<const float*>(B.p), L, c0 + c, mc, stage.p, s);
           virtual_product_f32(H, stage.p, reinterpret_cast<float*>(AB.p) + c0 + c, L, mc, s);
         }
+      } else if (cfg.spmm_prec == CG_PREC_REFINE) {
+        // refinement: double-float product, 4 vectors a pass as (hi, lo) pairs
+        for (int c = 0; c < m; c += 4) {
+          const int mc = std::min(4, m - c);
+          virtual_pack_df(n, reinterpret_cast<const double*>(B.p), L, c0 + c, mc, stage.p, s);
+          virtual_product_df(H, stage.p, reinterpret_cast<double*>(AB.p) + c0 + c, L, mc, s);
+        }
       } else {
         double* w = reinterpret_cast<double*>(stage.p);
         for (int c = 0; c < m; c += kVirtualVB64) {

@@ -26,4 +26,14 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al,
   sl = err - (sh - t);
 }
 
+// (ah, al) + (bh, bl), compensated
+__device__ __forceinline__ void df_add(float& h, float& l, float ah, float al, float bh, float bl) {
+  const float s = ah + bh;
+  const float bb = s - ah;
+  float e = (ah - (s - bb)) + (bh - bb);
+  e += al + bl;
+  h = s + e;
+  l = e - (h - s);
+}
+
 }  // namespace cg

@@ -23,6 +23,7 @@
 #include <numeric>
 
 #include "bulk.h"
+#include "dfloat.h"
 #include "tiled.h"
 #include "virtual.h"
 
@@ -148,22 +149,83 @@ struct Row<double, 4> {
   }
 };
 
-template <class T, int VB, int RPT>
-__global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab<T> tb, const T* __restrict__ x, T* __restrict__ y,
-                                                 int ldy, int m, int* __restrict__ err) {
-  // shared memory: [3 mbarriers | pad to 128 B] own buf0 buf1 (lmax x VB each)
-  //                wsl0 wsl1 (np*np + 1, last = 0) un0 un1 (32) Pp (np*np + 1, last = 0)
+// Element values: T for the FP32 / FP64 products, an FP32 (hi, lo) pair for
+// the double-float one (FP64-accurate to ~2^-44 on the FP32 pipe).
+struct DF2 {
+  float h, l;
+};
+template <class T, bool DF>
+struct VT {
+  using type = T;
+};
+template <class T>
+struct VT<T, true> {
+  using type = DF2;
+};
+__device__ __forceinline__ float vneg(float v) { return -v; }
+__device__ __forceinline__ double vneg(double v) { return -v; }
+__device__ __forceinline__ DF2 vneg(DF2 v) { return {-v.h, -v.l}; }
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+__device__ __forceinline__ DF2 vadd(DF2 a, DF2 b) {
+  DF2 r;
+  df_add(r.h, r.l, a.h, a.l, b.h, b.l);
+  return r;
+}
+template <class V>
+__device__ __forceinline__ V vfrom(double d);
+template <>
+__device__ __forceinline__ float vfrom<float>(double d) { return float(d); }
+template <>
+__device__ __forceinline__ double vfrom<double>(double d) { return d; }
+template <>
+__device__ __forceinline__ DF2 vfrom<DF2>(double d) {
+  DF2 r;
+  df_split(d, r.h, r.l);
+  return r;
+}
+// table value i: the T table, or its (hi, lo) pair
+template <class V, class T>
+__device__ __forceinline__ V vtab(const T* hi, const T* lo, size_t i) {
+  if constexpr (sizeof(V) == 2 * sizeof(float) && sizeof(T) == sizeof(float)) return V{hi[i], lo[i]};
+  else return V(hi[i]);
+}
+// acc += v * row: VB values of T, or VB / 2 double-float pairs (hi at even,
+// lo at odd positions of the row and of the accumulators)
+template <class T, int VB>
+__device__ __forceinline__ void vmac(T (&acc)[VB], T v, const T (&x)[VB]) {
+#pragma unroll
+  for (int j = 0; j < VB; ++j) acc[j] += v * x[j];
+}
+template <class T, int VB>
+__device__ __forceinline__ void vmac(T (&acc)[VB], DF2 v, const T (&x)[VB]) {
+#pragma unroll
+  for (int u = 0; u < VB / 2; ++u) df_mac(acc[2 * u], acc[2 * u + 1], x[2 * u], x[2 * u + 1], v.h, v.l);
+}
+
+// DF = false: Y = H X in T (FP32 8 vectors or FP64 4 vectors per pass).
+// DF = true (T = float): X as 4 vectors of (hi, lo) FP32 pairs in the 8-float
+// rows, table values as (hi, lo) pairs (tl holds the low parts), products and
+// sums in double-float, Y written as FP64: the refinement product on the FP32
+// pipe instead of the FP64 one.
+template <class T, int VB, int RPT, bool DF>
+__global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab<T> tb, VTab<T> tl,
+                                                                   const T* __restrict__ x, void* __restrict__ yv,
+                                                                   int ldy, int m, int* __restrict__ err) {
+  using V = typename VT<T, DF>::type;
+  // shared memory: [3 mbarriers | pad to 128 B] own buf0 buf1 (lmax x VB each of T)
+  //                wsl0 wsl1 (np*np + 4, last = 0) un0 un1 (32) Pp (np*np + 1, last = 0), of V
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int npp = a.np * a.np, nw = npp + 4;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
   T* own = reinterpret_cast<T*>(smem_raw + kVirtualSmemHead);
   T* buf0 = own + size_t(a.lmax) * VB;
   T* buf1 = buf0 + size_t(a.lmax) * VB;
-  T* wsl0 = buf1 + size_t(a.lmax) * VB;
-  T* wsl1 = wsl0 + nw;
-  T* un0 = wsl1 + nw;
-  T* un1 = un0 + 32;
-  T* Pp = un1 + 32;
+  V* wsl0 = reinterpret_cast<V*>(buf1 + size_t(a.lmax) * VB);
+  V* wsl1 = wsl0 + nw;
+  V* un0 = wsl1 + nw;
+  V* un1 = un0 + 32;
+  V* Pp = un1 + 32;
 
   // half-swapped row reads (Row) for up to 2 rows per thread: fp 4+4 (2 rows)
   // 4.46 -> 4.04 ms; with 4 rows per thread (fp 5+5) they measured slower
@@ -185,14 +247,14 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   }
   // P1 neutron-spectator sums of this block: Pp[b*np+d] = sum_{q in nu} Up[b][d][q]
   for (int i = tid; i <= npp; i += NT) {
-    T s = 0;
+    V s = vfrom<V>(0.0);
     if (i < npp)
-      for (uint32_t w = nmask; w; w &= w - 1) s += tb.Up[size_t(i) * a.nn + (__ffs(w) - 1)];
+      for (uint32_t w = nmask; w; w &= w - 1) s = vadd(s, vtab<V>(tb.Up, tl.Up, size_t(i) * a.nn + (__ffs(w) - 1)));
     Pp[i] = s;
   }
   if (tid == 0) {
-    wsl0[npp] = T(0);
-    wsl1[npp] = T(0);
+    wsl0[npp] = vfrom<V>(0.0);
+    wsl1[npp] = vfrom<V>(0.0);
   }
   __syncthreads();
   if (tid == 0) {
@@ -213,15 +275,14 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   for (uint32_t e = a.nn_off[beta], e1 = a.nn_off[beta + 1]; e < e1; ++e) {
     const VPair q = a.nn2[e];
     const uint64_t ts = a.bstart[q.target];
-    const T h = T(q.h);
+    const V h = vfrom<V>(q.h);
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
       const int r = tid + k * NT;
       if (r < L) {
         Row<T, VB> xr;
         xr.load_g(x + (ts + r) * VB, sw);
-#pragma unroll
-        for (int j = 0; j < VB; ++j) acc[k][j] += h * xr.v[j];
+        vmac(acc[k], h, xr.v);
       }
     }
   }
@@ -248,24 +309,20 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       Row<T, VB> xr;
       if (r < L) {
         xr.load_s(own + size_t(r) * VB, sw);
-        const T d = T(a.diag[start + r]);
-#pragma unroll
-        for (int j = 0; j < VB; ++j) acc[k][j] += d * xr.v[j];
+        vmac(acc[k], vfrom<V>(a.diag[start + r]), xr.v);
       }
       for (uint32_t e = a.pp_off[sl] + lane, e1 = a.pp_off[sl + 1]; e < e1; e += 32) {
-        const T h = tb.pp_h[e];
+        const V h = vtab<V>(tb.pp_h, tl.pp_h, e);
         xr.load_s(own + size_t(a.pp_rank[e]) * VB, sw);
-#pragma unroll
-        for (int j = 0; j < VB; ++j) acc[k][j] += h * xr.v[j];
+        vmac(acc[k], h, xr.v);
       }
       const size_t o = size_t(sl) * a.ndm + a.dm0;
       for (uint32_t e = a.sl_off[o] + lane, e1 = a.sl_off[o + 1]; e < e1; e += 32) {
         const uint32_t q = a.sl_e[e];
-        T v = Pp[(q >> 16) & 0x7ff];
-        v = tb.sl_c[e] + (((q >> 27) & 1) ? -v : v);
+        V v = Pp[(q >> 16) & 0x7ff];
+        v = vadd(vtab<V>(tb.sl_c, tl.sl_c, e), ((q >> 27) & 1) ? vneg(v) : v);
         xr.load_s(own + size_t(q & 0xffff) * VB, sw);
-#pragma unroll
-        for (int j = 0; j < VB; ++j) acc[k][j] += v * xr.v[j];
+        vmac(acc[k], v, xr.v);
       }
     }
   }
@@ -274,14 +331,17 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   for (uint32_t t = t0; t < t1; ++t, ++u) {
     const int jb = u & 1;
     const NTrans tr = a.nt[t];
-    T* wsl = jb ? wsl1 : wsl0;
-    T* un = jb ? un1 : un0;
-    const T* Wrow = tb.W + (size_t(tr.a) * a.nn + tr.c) * npp;
-    for (int i = tid; i < npp; i += NT) wsl[i] = tr.sign ? -Wrow[i] : Wrow[i];
+    V* wsl = jb ? wsl1 : wsl0;
+    V* un = jb ? un1 : un0;
+    const size_t wrow = (size_t(tr.a) * a.nn + tr.c) * npp;
+    for (int i = tid; i < npp; i += NT) {
+      const V w = vtab<V>(tb.W, tl.W, wrow + i);
+      wsl[i] = tr.sign ? vneg(w) : w;
+    }
     const bool same_m = tr.dmi == a.dm0;
     if (same_m && tid < a.np) {
-      const T w = tb.Un[(size_t(tr.a) * a.nn + tr.c) * a.np + tid];
-      un[tid] = tr.sign ? -w : w;
+      const V w = vtab<V>(tb.Un, tl.Un, (size_t(tr.a) * a.nn + tr.c) * a.np + tid);
+      un[tid] = tr.sign ? vneg(w) : w;
     }
     __syncthreads();
     if (tid == 0 && t + 1 < t1) {
@@ -301,7 +361,7 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
     }
     const T* bf = jb ? buf1 : buf0;
     const int dmp = a.ndm - 2 - (tr.dmi & ~1) + (tr.dmi & 1);  // opposite 2m change, same parity change
-    const T cn = T(tr.cn);
+    const V cn = vfrom<V>(tr.cn);
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
       const int rb = (tid & ~31) + k * NT;
@@ -311,20 +371,18 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
         const size_t o = size_t(sl) * a.ndm + dmp;
         for (uint32_t e = a.sl_off[o] + lane, e1 = a.sl_off[o + 1]; e < e1; e += 32) {
           const uint32_t q = a.sl_e[e];
-          T w = wsl[(q >> 16) & 0x7ff];
-          w = ((q >> 27) & 1) ? -w : w;
+          V w = wsl[(q >> 16) & 0x7ff];
+          w = ((q >> 27) & 1) ? vneg(w) : w;
           Row<T, VB> xr;
           xr.load_s(bf + size_t(q & 0xffff) * VB, sw);
-#pragma unroll
-          for (int j = 0; j < VB; ++j) acc[k][j] += w * xr.v[j];
+          vmac(acc[k], w, xr.v);
         }
         if (same_m && r < L) {
-          T v = cn;
-          for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v += un[__ffs(w) - 1];
+          V v = cn;
+          for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v = vadd(v, un[__ffs(w) - 1]);
           Row<T, VB> xr;
           xr.load_s(bf + size_t(r) * VB, sw);
-#pragma unroll
-          for (int j = 0; j < VB; ++j) acc[k][j] += v * xr.v[j];
+          vmac(acc[k], v, xr.v);
         }
       }
     }
@@ -333,11 +391,21 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   for (int k = 0; k < RPT; ++k) {
     const int r = tid + k * NT;
     if (r < L) {
-      T* yr = y + (start + r) * size_t(ldy);
+      if constexpr (DF) {
+        // register pair u holds vector u, or u ^ (VB / 4) with the halves swapped
+        double* yr = static_cast<double*>(yv) + (start + r) * size_t(ldy);
 #pragma unroll
-      for (int j = 0; j < VB; ++j) {
-        const int jj = sw ? (j ^ (VB / 2)) : j;
-        if (jj < m) yr[jj] = acc[k][j];
+        for (int u = 0; u < VB / 2; ++u) {
+          const int jj = sw ? (u ^ (VB / 4)) : u;
+          if (jj < m) yr[jj] = double(acc[k][2 * u]) + double(acc[k][2 * u + 1]);
+        }
+      } else {
+        T* yr = static_cast<T*>(yv) + (start + r) * size_t(ldy);
+#pragma unroll
+        for (int j = 0; j < VB; ++j) {
+          const int jj = sw ? (j ^ (VB / 2)) : j;
+          if (jj < m) yr[jj] = acc[k][j];
+        }
       }
     }
   }
@@ -366,12 +434,12 @@ __global__ void k_virtual_diag(uint64_t n, int nblocks, const uint64_t* __restri
   diag[i] = d;
 }
 
-template <class T, int VB, int RPT>
-void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const T* x, T* y, int ldy, int m,
-                int threads, size_t smem, int* err, cudaStream_t s) {
-  auto kern = k_virtual<T, VB, RPT>;
+template <class T, int VB, int RPT, bool DF>
+void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const VTab<T>& tl, const T* x, void* y,
+                int ldy, int m, int threads, size_t smem, int* err, cudaStream_t s) {
+  auto kern = k_virtual<T, VB, RPT, DF>;
   CG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  kern<<<unsigned(a.lmax ? h.virt->nblocks : 0), threads, smem, s>>>(a, tb, x, y, ldy, m, err);
+  kern<<<unsigned(a.lmax ? h.virt->nblocks : 0), threads, smem, s>>>(a, tb, tl, x, y, ldy, m, err);
   CG_CUDA(cudaGetLastError());
   count_launch();
 }
@@ -387,17 +455,20 @@ VArgs make_args(const VirtualOp& v, const Hamiltonian& h) {
   return a;
 }
 
-template <class T, int VB>
-void virtual_product(const Hamiltonian& h, const T* x, T* y, int ldy, int m, const VTab<T>& tb, cudaStream_t s) {
+// DF: x holds VB / 2 vectors as (hi, lo) pairs, y is FP64 (VB / 2 columns)
+template <class T, int VB, bool DF = false>
+void virtual_product(const Hamiltonian& h, const T* x, void* y, int ldy, int m, const VTab<T>& tb,
+                     const VTab<T>& tl, cudaStream_t s) {
   if (!h.virt) throw Error(CG_ERR_INTERNAL, "not an on-the-fly Hamiltonian");
   const VirtualOp& v = *h.virt;
-  if (m < 1 || m > VB) throw Error(CG_ERR_ARG, "on-the-fly product: too many vectors for one pass");
+  if (m < 1 || m > (DF ? VB / 2 : VB)) throw Error(CG_ERR_ARG, "on-the-fly product: too many vectors for one pass");
   if (ldy < m) throw Error(CG_ERR_ARG, "leading dimension smaller than the vector count");
   if (reinterpret_cast<uintptr_t>(x) % 16) throw Error(CG_ERR_ARG, "on-the-fly product needs 16-byte aligned x");
   if (v.nblocks == 0) return;
   VArgs a = make_args(v, h);
   const int npp = v.np * v.np;
-  const size_t smem = kVirtualSmemHead + (size_t(3) * v.lmax * VB + 3 * size_t(npp + 4) + 64) * sizeof(T);
+  const size_t vsz = DF ? 2 * sizeof(float) : sizeof(T);  // bytes of one element value
+  const size_t smem = kVirtualSmemHead + size_t(3) * v.lmax * VB * sizeof(T) + (3 * size_t(npp + 4) + 64) * vsz;
   if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "neutron block too long for the shared-memory staging");
   // rows per thread: threads <= 512, or <= 1024 when the staging buffers
   // leave room for one CTA per SM only (long blocks, e.g. fp 5+5): there two
@@ -412,10 +483,10 @@ void virtual_product(const Hamiltonian& h, const T* x, T* y, int ldy, int m, con
   DBuf<int>& err = v.err;
   CG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
   switch (rpt) {
-    case 1: launch_rpt<T, VB, 1>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
-    case 2: launch_rpt<T, VB, 2>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
-    case 4: launch_rpt<T, VB, 4>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
-    default: launch_rpt<T, VB, 8>(h, a, tb, x, y, ldy, m, threads, smem, err.p, s); break;
+    case 1: launch_rpt<T, VB, 1, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+    case 2: launch_rpt<T, VB, 2, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+    case 4: launch_rpt<T, VB, 4, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+    default: launch_rpt<T, VB, 8, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
   }
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -462,7 +533,14 @@ void virtual_launch(const Hamiltonian& h, int precision, const void* x, int ldx,
       virtual_pack_f32(n, static_cast<const float*>(x), ldx, c0, mc, w.p, s);
       virtual_product_f32(h, w.p, static_cast<float*>(y) + c0, ldy, mc, s);
     }
-  } else if (precision == CG_PREC_FP64 || precision == CG_PREC_REFINE) {
+  } else if (precision == CG_PREC_REFINE) {
+    DBuf<float> w(std::max<uint64_t>(n * 8, 1));
+    for (int c0 = 0; c0 < m; c0 += 4) {
+      const int mc = std::min(4, m - c0);
+      virtual_pack_df(n, static_cast<const double*>(x), ldx, c0, mc, w.p, s);
+      virtual_product_df(h, w.p, static_cast<double*>(y) + c0, ldy, mc, s);
+    }
+  } else if (precision == CG_PREC_FP64) {
     DBuf<double> w(std::max<uint64_t>(n * kVirtualVB64, 1));
     for (int c0 = 0; c0 < m; c0 += kVirtualVB64) {
       const int mc = std::min(kVirtualVB64, m - c0);
@@ -476,12 +554,40 @@ void virtual_launch(const Hamiltonian& h, int precision, const void* x, int ldx,
 
 void virtual_product_f32(const Hamiltonian& h, const float* x, float* y, int ldy, int m, cudaStream_t s) {
   VTab<float> tb{h.virt->Wf.p, h.virt->Unf.p, h.virt->Upf.p, h.virt->sl_cf.p, h.virt->pp_hf.p};
-  virtual_product<float, kVirtualVB32>(h, x, y, ldy, m, tb, s);
+  virtual_product<float, kVirtualVB32>(h, x, y, ldy, m, tb, tb, s);
 }
 
 void virtual_product_f64(const Hamiltonian& h, const double* x, double* y, int ldy, int m, cudaStream_t s) {
   VTab<double> tb{h.virt->W.p, h.virt->Un.p, h.virt->Up.p, h.virt->sl_c.p, h.virt->pp_h.p};
-  virtual_product<double, kVirtualVB64>(h, x, y, ldy, m, tb, s);
+  virtual_product<double, kVirtualVB64>(h, x, y, ldy, m, tb, tb, s);
+}
+
+// x: 4 vectors as (hi, lo) FP32 pairs per row (virtual_pack_df), y FP64
+void virtual_product_df(const Hamiltonian& h, const float* x, double* y, int ldy, int m, cudaStream_t s) {
+  VTab<float> tb{h.virt->Wf.p, h.virt->Unf.p, h.virt->Upf.p, h.virt->sl_cf.p, h.virt->pp_hf.p};
+  VTab<float> tl{h.virt->Wl.p, h.virt->Unl.p, h.virt->Upl.p, h.virt->sl_cl.p, h.virt->pp_hl.p};
+  virtual_product<float, kVirtualVB32, true>(h, x, y, ldy, m, tb, tl, s);
+}
+
+namespace {
+// 8 floats per row = 4 vectors as (hi, lo) pairs, columns c0 .. c0+m of x
+__global__ void k_pack_df(uint64_t n, const double* __restrict__ x, int ld, int c0, int m, float* __restrict__ w) {
+  const uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * 4) return;
+  const uint64_t i = idx >> 2;
+  const int j = int(idx & 3);
+  float h, l;
+  df_split(j < m ? x[i * ld + c0 + j] : 0.0, h, l);
+  w[i * 8 + 2 * j] = h;
+  w[i * 8 + 2 * j + 1] = l;
+}
+}  // namespace
+
+void virtual_pack_df(uint64_t n, const double* x, int ld, int c0, int m, float* w, cudaStream_t s) {
+  if (!n) return;
+  k_pack_df<<<unsigned((n * 4 + 255) / 256), 256, 0, s>>>(n, x, ld, c0, m, w);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
 }
 
 uint64_t Hamiltonian::device_bytes() const {
@@ -824,6 +930,13 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   std::vector<float> sl_cf(sl_c.begin(), sl_c.end()), pp_hf(pp_h.begin(), pp_h.end());
   v.sl_cf.upload(sl_cf, s);
   v.pp_hf.upload(pp_hf, s);
+  auto lo_part = [](const std::vector<double>& d, const std::vector<float>& f) {
+    std::vector<float> l(d.size());
+    for (size_t i = 0; i < d.size(); ++i) l[i] = float(d[i] - double(f[i]));
+    return l;
+  };
+  v.sl_cl.upload(lo_part(sl_c, sl_cf), s);
+  v.pp_hl.upload(lo_part(pp_h, pp_hf), s);
   v.W.upload(W, s);
   v.Un.upload(Un, s);
   v.Up.upload(Up, s);
@@ -831,6 +944,9 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   v.Wf.upload(Wf, s);
   v.Unf.upload(Unf, s);
   v.Upf.upload(Upf, s);
+  v.Wl.upload(lo_part(W, Wf), s);
+  v.Unl.upload(lo_part(Un, Unf), s);
+  v.Upl.upload(lo_part(Up, Upf), s);
   h.diag.alloc(std::max<uint64_t>(b.n, 1));
   if (b.n) {
     DBuf<double> dEn, dEp, dVd;

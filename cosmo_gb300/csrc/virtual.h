@@ -71,13 +71,15 @@ struct VirtualOp {
   DBuf<float> pp_hf;
   DBuf<double> W, Un, Up;                           // nn*nn*np*np, nn*nn*np, np*np*nn
   DBuf<float> Wf, Unf, Upf;
+  DBuf<float> Wl, Unl, Upl, sl_cl, pp_hl;            // low parts (value - float(value)), double-float product
   mutable DBuf<int> err;                            // staged-copy timeout flag
   uint64_t bytes() const {
     return bstart.bytes() + blen.bytes() + bclass.bytes() + bmask.bytes() + order.bytes() + cstart.bytes() +
            cmask.bytes() + nt_off.bytes() + nt.bytes() + nn_off.bytes() + nn2.bytes() + cslice.bytes() +
            sl_off.bytes() + sl_e.bytes() + sl_c.bytes() + sl_cf.bytes() + pp_off.bytes() + pp_rank.bytes() +
            pp_h.bytes() + pp_hf.bytes() + W.bytes() + Un.bytes() + Up.bytes() +
-           Wf.bytes() + Unf.bytes() + Upf.bytes();
+           Wf.bytes() + Unf.bytes() + Upf.bytes() + Wl.bytes() + Unl.bytes() + Upl.bytes() + sl_cl.bytes() +
+           pp_hl.bytes();
   }
 };
 
@@ -88,6 +90,11 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
 // values (zero-padded columns).  FP32: 8 vectors a row; FP64: 4.
 void virtual_product_f32(const Hamiltonian& h, const float* x, float* y, int ldy, int m, cudaStream_t s);
 void virtual_product_f64(const Hamiltonian& h, const double* x, double* y, int ldy, int m, cudaStream_t s);
+// Double-float product (the refinement product): x packed by virtual_pack_df
+// as n rows of 4 vectors in (hi, lo) FP32 pairs, y FP64, m <= 4; products and
+// sums on the FP32 pipe, FP64-accurate to ~2^-44.
+void virtual_product_df(const Hamiltonian& h, const float* x, double* y, int ldy, int m, cudaStream_t s);
+void virtual_pack_df(uint64_t n, const double* x, int ld, int c0, int m, float* w, cudaStream_t s);
 constexpr int kVirtualVB32 = 8, kVirtualVB64 = 4;
 // pack columns c0 .. c0+m of a row-interleaved block into the product's layout
 void virtual_pack_f32(uint64_t n, const float* x, int ld, int c0, int m, float* w, cudaStream_t s);
