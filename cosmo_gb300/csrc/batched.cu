@@ -73,13 +73,18 @@ __global__ void k_dense_fill(int n, uint64_t r0, const uint64_t* __restrict__ rp
 // of sqrt|a_pp a_qq|; at most 40 sweeps.
 template <class R>
 constexpr size_t jac_smem() {
-  return (size_t(2) * kJac * (kJac + 1) + 256 + kJac) * sizeof(R) + (2 * kJac + 8) * sizeof(int);
+  return (size_t(3) * kJac * (kJac + 1) + 256 + kJac) * sizeof(R) + (2 * kJac + 8) * sizeof(int);
 }
 
+// Warm start (kprev > 0): the leading kprev x kprev block of A is the
+// previous step's projected matrix, whose eigenvectors Zout still holds; the
+// sweeps start from A' = P^T A P, P = diag(Z_prev, I), whose leading block is
+// already diagonal, with Z = P, so only the coupling to the newest rows is
+// left to rotate away.
 template <class R>
 __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain, const int* __restrict__ kdim,
-                                                 int kconst, double* __restrict__ w, double* __restrict__ Zout,
-                                                 const int* __restrict__ fz) {
+                                                 int kconst, double* __restrict__ w, double* Zout,
+                                                 const int* __restrict__ fz, int kprev) {
   constexpr R kConv = sizeof(R) == 4 ? R(1e-12) : R(1e-30);   // (off / total)^2 at convergence
   constexpr R kTiny = sizeof(R) == 4 ? R(1e-30) : R(1e-300);
   constexpr R kSkip = sizeof(R) == 4 ? R(1e-7) : R(1e-17);
@@ -88,7 +93,8 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   R* jsm = reinterpret_cast<R*>(jsm_raw);
   R(*A)[kJac + 1] = reinterpret_cast<R(*)[kJac + 1]>(jsm);
   R(*Z)[kJac + 1] = reinterpret_cast<R(*)[kJac + 1]>(jsm + kJac * (kJac + 1));
-  R* red = jsm + 2 * kJac * (kJac + 1);
+  R(*Tm)[kJac + 1] = reinterpret_cast<R(*)[kJac + 1]>(jsm + 2 * kJac * (kJac + 1));
+  R* red = jsm + 3 * kJac * (kJac + 1);
   R* rc = red + 256;
   R* rs = rc + kJac / 2;
   int* rp = reinterpret_cast<int*>(rs + kJac / 2);
@@ -98,12 +104,47 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   const int b = blockIdx.x, tid = threadIdx.x;
   const int k = kdim ? kdim[b] : kconst;
   const double* Ab = Ain + size_t(b) * kJac * kJac;
+  const int kp = (kprev > 0 && kprev < k) ? kprev : 0;
+  const double* Zp = Zout + size_t(b) * kJac * kJac;
   for (int i = tid; i < kJac * kJac; i += blockDim.x) {
     const int r = i / kJac, c = i % kJac;
     A[r][c] = (r < k && c < k) ? R(Ab[r * kJac + c]) : R(0);
-    Z[r][c] = r == c ? R(1) : R(0);
+    Z[r][c] = (r < kp && c < kp) ? R(Zp[r * kJac + c]) : (r == c && r >= kp ? R(1) : R(0));
   }
   __syncthreads();
+  if (kp > 0) {
+    // Tm = A P (only the first kp columns change), then A = P^T Tm (first kp rows)
+    for (int i = tid; i < k * k; i += blockDim.x) {
+      const int r = i / k, c = i % k;
+      R v = 0;
+      if (c < kp)
+        for (int t = 0; t < kp; ++t) v += A[r][t] * Z[t][c];
+      else
+        v = A[r][c];
+      Tm[r][c] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < k * k; i += blockDim.x) {
+      const int r = i / k, c = i % k;
+      R v = 0;
+      if (r < kp)
+        for (int t = 0; t < kp; ++t) v += Z[t][r] * Tm[t][c];
+      else
+        v = Tm[r][c];
+      A[r][c] = v;
+    }
+    __syncthreads();
+    // exact symmetry (the two products round differently)
+    for (int i = tid; i < k * k; i += blockDim.x) {
+      const int r = i / k, c = i % k;
+      if (r < c) {
+        const R v = R(0.5) * (A[r][c] + A[c][r]);
+        A[r][c] = v;
+        A[c][r] = v;
+      }
+    }
+    __syncthreads();
+  }
   const int kk = k + (k & 1);  // even player count; player k (if odd) is idle
   for (int sweep = 0; sweep < 40 && k > 1; ++sweep) {
     // convergence: off-diagonal vs total
@@ -489,18 +530,21 @@ __global__ void k_bfill(uint32_t nrows, const uint32_t* __restrict__ rowprob, co
 }
 
 // S[q] = diag(w[q][0..keep)), rest zero
-__global__ void k_bset_diag(int keep, const double* __restrict__ w, double* __restrict__ S,
+// after a thick restart: S = diag(kept Ritz values); the eigenvectors of that
+// block are the identity (the warm start of the next Jacobi reads them from Z)
+__global__ void k_bset_diag(int keep, const double* __restrict__ w, double* __restrict__ S, double* __restrict__ Z,
                             const int* __restrict__ fz) {
   const int q = blockIdx.x;
   if (fz[q]) return;
   double* Sq = S + size_t(q) * kJac * kJac;
+  double* Zq = Z + size_t(q) * kJac * kJac;
   for (int i = threadIdx.x; i < kJac * kJac; i += blockDim.x) {
     const int r = i / kJac, c = i % kJac;
     Sq[i] = (r == c && r < keep) ? w[size_t(q) * kJac + r] : 0.0;
+    Zq[i] = (r == c && r < keep) ? 1.0 : 0.0;
   }
 }
 
-// M[q][i][j] = diag(1 / sqrt(G[q][j][j])) for normalisation (ld kMaxB)
 // Block Gram-Schmidt with Pythagorean inner products for each problem: W =
 // [V_basis | T]^T T ((c0 + b) x b, ld b) gives the projections Gp (first c0
 // rows) and the block Gram Mt; S = Mt - Gp^T Gp is the Gram of the projected
@@ -756,7 +800,9 @@ struct BEngine {
     spmm(k - b);
     xty(V.p, lim, 0, k, AV.p, lim, k - b, b);
     k_bset_proj<<<Q, 128, 0, s>>>(k, b, k - b, G.p, S.p, fz.p);
-    k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p);
+    // warm start from the previous step's eigenvectors (size k - b; after a
+    // restart the kept block is diagonal and Z's leading block the identity)
+    k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p, k - b);
     k_bresid<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, V.p, AV.p, lim, k, w.p, Z.p, R.p, 8, b, fz.p);
     xty(R.p, 8, 0, b, R.p, 8, 0, b);
     k_bconv<<<1, 256, 0, s>>>(Q, nev, b, G.p, tol, rnorm.p, fz.p, kfreeze.p, k, nconv.p);
@@ -766,7 +812,7 @@ struct BEngine {
       const size_t zs = size_t(kJac) * kJac;
       gemm(V.p, lim, 0, k, Z.p, zs, kJac, V.p, lim, 0, keep, 1.0, 0.0);
       gemm(AV.p, lim, 0, k, Z.p, zs, kJac, AV.p, lim, 0, keep, 1.0, 0.0);
-      k_bset_diag<<<Q, 256, 0, s>>>(keep, w.p, S.p, fz.p);
+      k_bset_diag<<<Q, 256, 0, s>>>(keep, w.p, S.p, Z.p, fz.p);
       c0 = keep;
     }
     k_bprecond<T><<<nblk(N, 128), 128, 0, s>>>(N, bs.rowprob.p, R.p, 8, w.p, bs.diag.p, V.p, lim, c0, b, fz.p);
@@ -954,7 +1000,7 @@ void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
     DBuf<double> w(size_t(bs.nd) * kJac), Z(size_t(bs.nd) * kJac * kJac);
     DBuf<int> kd;
     kd.upload(bs.ddim, s);
-    k_bjacobi<double><<<bs.nd, 256, jac_smem<double>(), s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr);
+    k_bjacobi<double><<<bs.nd, 256, jac_smem<double>(), s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr, 0);
     CG_CUDA(cudaGetLastError());
     count_launch();
     dw.resize(size_t(bs.nd) * kJac);
