@@ -445,13 +445,6 @@ void launch_tiled(const TiledOp& t, const TArgs& a, const float* x, float* y, in
 
 }  // namespace
 
-std::vector<uint64_t> tiled_uniform_blocks(uint64_t n) {
-  std::vector<uint64_t> b;
-  for (uint64_t r = 0; r < n; r += 512) b.push_back(r);
-  b.push_back(n);
-  return b;
-}
-
 void tiled_build(Hamiltonian& h, const std::vector<uint64_t>& bs) {
   h.tiled.reset();
   if (h.precision != CG_PREC_FP32 || h.n == 0 || bs.size() < 2 || bs.back() != h.n) return;

@@ -2,8 +2,9 @@
 //
 // Rows and columns are cut at the same boundaries (the neutron blocks of the
 // basis: one neutron configuration followed by all its proton configurations;
-// for a matrix read from a file, fixed 512-row ranges).  A tile is the nonzero
-// part H[row block b, column block c]; the tiles of b are kept in ascending c.
+// a matrix read from a .HH file has no basis and keeps the row-wise kernel).
+// A tile is the nonzero part H[row block b, column block c]; the tiles of b
+// are kept in ascending c.
 // Inside a tile the entries are stored per 32-row slice of b, lane-interleaved
 // (SELL-32: entry j of slice row l at run_start + 32 j + l, rows shorter than
 // the slice's longest padded with value 0), each entry a 16-bit column inside
@@ -66,8 +67,6 @@ constexpr int kTiledSlotHead = 256;
 void tiled_build(Hamiltonian& h, const std::vector<uint64_t>& bstart);
 // Dynamic shared memory of the product with `stages` ring slots.
 size_t tiled_smem(const TiledOp& t, int stages);
-// Block starts used for a matrix without a basis: fixed 512-row ranges.
-std::vector<uint64_t> tiled_uniform_blocks(uint64_t n);
 // Y = H X for m <= 8 FP32 vectors; x rows are 8 floats (32 bytes, the
 // buffer 16-byte aligned), only the first m outputs of each row are stored.
 void tiled_product(const Hamiltonian& h, const float* x, float* y, int ldy, int m, cudaStream_t s);
