@@ -483,51 +483,123 @@ namespace {
 // 1/sqrt((1+d_ab)(1+d_cd)), sqrt(2) for pn pairs of separately indexed orbits,
 // fermion sign on pair reordering, forward pair order, /2 for a line whose bra
 // and ket orbit pairs coincide and x2 on the m-pair diagonal.
-void add_pp_vsp(std::map<Key4, double>& vsp, const std::vector<SPState>& sps, const std::array<int, 6>& ijk,
-                double V) {
-  const int ns = int(sps.size());
-  int a_min1 = 0;
-  while (a_min1 < ns && sps[a_min1].level != ijk[1]) a_min1 += sps[a_min1].j2 + 1;
-  if (a_min1 >= ns) return;
-  const int l2 = sps[a_min1].j2, l3 = 2 * ijk[4];
-  for (int a0 = 0; a0 < ns; ++a0) {
-    if (sps[a0].level != ijk[0]) { a0 += sps[a0].j2; continue; }
+// Clebsch-Gordan coefficients <j1 m1 j2 m2 | J m1+m2> of two s.p. states
+// (odd doubled j1, j2 <= jmax) and of their isospins (t = 1/2), tabulated once
+// per operator build from clebsch_gordan itself (same values, looked up
+// instead of recomputed for every m-state combination of every TBME line).
+struct CGTable {
+  int jmax = 0, nj = 0, nm = 0;
+  std::vector<double> tab;  // [j1][m1][j2][m2][J]
+  double tz[2][2][2];       // [tz1 > 0][tz2 > 0][T]
+  explicit CGTable(int jmax_) : jmax(jmax_ | 1), nj((jmax_ + 2) / 2), nm(jmax_ + 2) {
+    const int nJ = nm;
+    tab.assign(size_t(nj) * nm * nj * nm * nJ, 0.0);
+    for (int a = 0; a < nj; ++a)
+      for (int b = 0; b < nj; ++b) {
+        const int j1 = 2 * a + 1, j2 = 2 * b + 1;
+        for (int m1 = -j1; m1 <= j1; m1 += 2)
+          for (int m2 = -j2; m2 <= j2; m2 += 2)
+            for (int J = std::abs(j1 - j2); J <= j1 + j2 && J / 2 < nJ; J += 2)
+              tab[idx(j1, m1, j2, m2, J)] = clebsch_gordan(j1, m1, j2, m2, J, m1 + m2);
+      }
+    for (int p = 0; p < 2; ++p)
+      for (int q = 0; q < 2; ++q)
+        for (int T = 0; T < 2; ++T) tz[p][q][T] = clebsch_gordan(1, p ? 1 : -1, 1, q ? 1 : -1, 2 * T, (p ? 1 : -1) + (q ? 1 : -1));
+  }
+  size_t idx(int j1, int m1, int j2, int m2, int J) const {
+    return (((size_t(j1 / 2) * nm + (m1 + jmax) / 2) * nj + j2 / 2) * nm + (m2 + jmax) / 2) * nm + J / 2;
+  }
+  double j(int j1, int m1, int j2, int m2, int J) const {
+    if ((j1 & 1) == 0 || (j2 & 1) == 0 || (J & 1) || J / 2 >= nm || j1 > jmax || j2 > jmax)
+      return clebsch_gordan(j1, m1, j2, m2, J, m1 + m2);
+    return tab[idx(j1, m1, j2, m2, J)];
+  }
+  double t(int tz1, int tz2, int T) const {
+    if (T < 0 || T > 1) return clebsch_gordan(1, tz1, 1, tz2, 2 * T, tz1 + tz2);
+    return tz[tz1 > 0][tz2 > 0][T];
+  }
+};
+
+// s.p. indices of each orbit level (ascending; both species), and the index
+// of (level, tz, m) for the direct lookup of the fourth state of a TBME term
+struct SPIndex {
+  int jmax = 1;
+  std::vector<std::vector<int>> by_level;
+  std::vector<int> at;  // [level][tz > 0][(m + jmax) / 2] -> index or -1
+  explicit SPIndex(const std::vector<SPState>& sps) {
+    int nl = 0;
+    for (const auto& sp : sps) {
+      nl = std::max(nl, sp.level + 1);
+      jmax = std::max(jmax, sp.j2);
+    }
+    by_level.assign(nl, {});
+    at.assign(size_t(nl) * 2 * (jmax + 1), -1);
+    for (int i = 0; i < int(sps.size()); ++i) {
+      by_level[sps[i].level].push_back(i);
+      at[slot(sps[i].level, sps[i].tz2, sps[i].m2)] = i;
+    }
+  }
+  size_t slot(int level, int tz2, int m2) const {
+    return (size_t(level) * 2 + (tz2 > 0)) * (jmax + 1) + (m2 + jmax) / 2;
+  }
+  int find(int level, int tz2, int m2) const {
+    if (level < 0 || level >= int(by_level.size()) || m2 < -jmax || m2 > jmax || (tz2 != 1 && tz2 != -1)) return -1;
+    return at[slot(level, tz2, m2)];
+  }
+};
+
+// AddPPVsp, 4-argument form (include/sm/AddPPVsp.cxx:32-147): every m-state
+// combination of the four orbits, Clebsch-Gordan weights in J and T,
+// 1/sqrt((1+d_ab)(1+d_cd)), sqrt(2) for pn pairs of separately indexed orbits,
+// fermion sign on pair reordering, forward pair order, /2 for a line whose bra
+// and ket orbit pairs coincide and x2 on the m-pair diagonal.  The states are
+// visited in ascending index order as in the reference (a0, a1, a2; the fourth
+// is fixed by m and tz conservation), so every key accumulates its terms in
+// the reference's order.
+void add_pp_vsp(std::map<Key4, double>& vsp, const std::vector<SPState>& sps, const CGTable& cgt,
+                const SPIndex& spi, const std::array<int, 6>& ijk, double V) {
+  const int nl = int(spi.by_level.size());
+  for (int q = 0; q < 4; ++q)
+    if (ijk[q] < 0 || ijk[q] >= nl || spi.by_level[ijk[q]].empty()) return;
+  const int l2 = sps[spi.by_level[ijk[1]][0]].j2, l3 = 2 * ijk[4];
+  for (int a0 : spi.by_level[ijk[0]]) {
     const int l1 = sps[a0].j2, m1 = sps[a0].m2;
-    for (int a1 = a_min1; a1 < ns; ++a1) {
-      if (sps[a1].level != ijk[1]) { a1 += sps[a1].j2; continue; }
+    for (int a1 : spi.by_level[ijk[1]]) {
       if ((sps[a0].j2 & 1) && a1 == a0) continue;
       const int m2 = sps[a1].m2;
-      const double cg_ab = clebsch_gordan(l1, m1, l2, m2, l3, m1 + m2);
-      for (int a2 = 0; a2 < ns; ++a2) {
-        if (sps[a2].level != ijk[2]) { a2 += sps[a2].j2; continue; }
-        for (int a3 = 0; a3 < ns; ++a3) {
-          if (sps[a3].level != ijk[3]) { a3 += sps[a3].j2; continue; }
-          if ((sps[a2].j2 & 1) && a2 == a3) continue;
-          if (sps[a0].m2 + sps[a1].m2 != sps[a3].m2 + sps[a2].m2) continue;
-          if (sps[a0].tz2 + sps[a1].tz2 != sps[a3].tz2 + sps[a2].tz2) continue;
-          double h = cg_ab;
-          h *= clebsch_gordan(sps[a2].j2, sps[a2].m2, sps[a3].j2, sps[a3].m2, l3, sps[a2].m2 + sps[a3].m2);
+      const double cg_ab = cgt.j(l1, m1, l2, m2, l3);
+      for (int a2 : spi.by_level[ijk[2]]) {
+        const int a3 = spi.find(ijk[3], sps[a0].tz2 + sps[a1].tz2 - sps[a2].tz2,
+                                sps[a0].m2 + sps[a1].m2 - sps[a2].m2);
+        if (a3 < 0) continue;
+        if ((sps[a2].j2 & 1) && a2 == a3) continue;
+        double h = cg_ab;
+        h *= cgt.j(sps[a2].j2, sps[a2].m2, sps[a3].j2, sps[a3].m2, l3);
+        if (sps[a0].t2 == 1 && sps[a1].t2 == 1 && sps[a2].t2 == 1 && sps[a3].t2 == 1) {
+          h *= cgt.t(sps[a0].tz2, sps[a1].tz2, ijk[5]);
+          h *= cgt.t(sps[a2].tz2, sps[a3].tz2, ijk[5]);
+        } else {
           h *= clebsch_gordan(sps[a0].t2, sps[a0].tz2, sps[a1].t2, sps[a1].tz2, 2 * ijk[5],
                               sps[a0].tz2 + sps[a1].tz2);
           h *= clebsch_gordan(sps[a2].t2, sps[a2].tz2, sps[a3].t2, sps[a3].tz2, 2 * ijk[5],
                               sps[a2].tz2 + sps[a3].tz2);
-          if (std::fabs(h) < 1e-9) continue;
-          h = h * V / std::sqrt((double(ijk[0] == ijk[1]) + 1.) * (double(ijk[2] == ijk[3]) + 1.));
-          auto pn_pair = [&](int x, int y) {
-            return sps[x].n == sps[y].n && sps[x].j2 == sps[y].j2 && sps[x].tz2 == -sps[y].tz2 &&
-                   sps[x].parity == sps[y].parity;
-          };
-          if (ijk[0] != ijk[1] && pn_pair(a0, a1)) h *= std::sqrt(2.);
-          if (ijk[2] != ijk[3] && pn_pair(a2, a3)) h *= std::sqrt(2.);
-          Key4 b{a0, a1, a2, a3};
-          bool phase = false;
-          if (b[0] > b[1]) { std::swap(b[0], b[1]); phase ^= bool(sps[a0].j2 & 1); }
-          if (b[2] > b[3]) { std::swap(b[2], b[3]); phase ^= bool(sps[a2].j2 & 1); }
-          if (b[2] < b[0] || (b[2] == b[0] && b[3] < b[1])) { std::swap(b[0], b[2]); std::swap(b[1], b[3]); }
-          if (ijk[0] == ijk[2] && ijk[1] == ijk[3]) h /= 2.0;
-          if (b[0] == b[2] && b[1] == b[3]) h *= 2.0;
-          vsp[b] += phase ? -h : h;
         }
+        if (std::fabs(h) < 1e-9) continue;
+        h = h * V / std::sqrt((double(ijk[0] == ijk[1]) + 1.) * (double(ijk[2] == ijk[3]) + 1.));
+        auto pn_pair = [&](int x, int y) {
+          return sps[x].n == sps[y].n && sps[x].j2 == sps[y].j2 && sps[x].tz2 == -sps[y].tz2 &&
+                 sps[x].parity == sps[y].parity;
+        };
+        if (ijk[0] != ijk[1] && pn_pair(a0, a1)) h *= std::sqrt(2.);
+        if (ijk[2] != ijk[3] && pn_pair(a2, a3)) h *= std::sqrt(2.);
+        Key4 bk{a0, a1, a2, a3};
+        bool phase = false;
+        if (bk[0] > bk[1]) { std::swap(bk[0], bk[1]); phase ^= bool(sps[a0].j2 & 1); }
+        if (bk[2] > bk[3]) { std::swap(bk[2], bk[3]); phase ^= bool(sps[a2].j2 & 1); }
+        if (bk[2] < bk[0] || (bk[2] == bk[0] && bk[3] < bk[1])) { std::swap(bk[0], bk[2]); std::swap(bk[1], bk[3]); }
+        if (ijk[0] == ijk[2] && ijk[1] == ijk[3]) h /= 2.0;
+        if (bk[0] == bk[2] && bk[1] == bk[3]) h *= 2.0;
+        vsp[bk] += phase ? -h : h;
       }
     }
   }
@@ -589,7 +661,11 @@ Operator build_operator(const System& sys) {
     if (lv >= int(si.spe.size())) throw Error(CG_ERR_PARSE, "interaction has fewer s.p. energies than orbits");
     op.one[{i, i}] += si.spe[lv];
   }
-  for (auto& kv : si.tbme) add_pp_vsp(op.two, sys.sps, kv.first, kv.second);
+  int jmax = 1;
+  for (const auto& sp : sys.sps) jmax = std::max(jmax, sp.j2);
+  const CGTable cgt(jmax);
+  const SPIndex spi(sys.sps);
+  for (auto& kv : si.tbme) add_pp_vsp(op.two, sys.sps, cgt, spi, kv.first, kv.second);
   if (sys.has_jj) {
     std::map<Key2, double> jsp;
     std::map<Key4, double> vjj;
