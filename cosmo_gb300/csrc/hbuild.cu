@@ -308,7 +308,7 @@ __global__ void k_scan_add(uint64_t* __restrict__ out, uint64_t n, const uint64_
 // write columns and values (FP64, or FP32 hi + lo) in ascending column order.
 __global__ void k_sort_rows(uint64_t n, const uint64_t* __restrict__ rowptr, uint32_t* __restrict__ col,
                             const double* __restrict__ val, double* __restrict__ out64, float* __restrict__ hi,
-                            float* __restrict__ lo, unsigned long long* __restrict__ upper_count) {
+                            float* __restrict__ lo, unsigned long long* __restrict__ upper_count, int min_len) {
   extern __shared__ uint64_t skey[];
   __shared__ unsigned long long up_blk;
   if (threadIdx.x == 0) up_blk = 0;
@@ -316,6 +316,7 @@ __global__ void k_sort_rows(uint64_t n, const uint64_t* __restrict__ rowptr, uin
   for (uint64_t row = blockIdx.x; row < n; row += gridDim.x) {
     uint64_t b = rowptr[row], e = rowptr[row + 1];
     int len = int(e - b);
+    if (len < min_len) continue;  // sorted by k_sort_rows_w (uniform across the CTA)
     int L = 1;
     while (L < len) L <<= 1;
     for (int i = threadIdx.x; i < L; i += blockDim.x)
@@ -355,6 +356,80 @@ __global__ void k_sort_rows(uint64_t n, const uint64_t* __restrict__ rowptr, uin
   }
   __syncthreads();
   if (threadIdx.x == 0 && up_blk) atomicAdd(upper_count, up_blk);
+}
+
+// Per-row sort for rows of at most 1024 entries in matrices of fewer than
+// 2^22 rows: one warp per row, the row's keys (column << 10 | position) held
+// 32 per lane in registers (lane l: positions 32 l .. 32 l + 31) and sorted
+// by a bitonic network whose stages of distance >= 32 exchange registers
+// between lanes by shuffles and whose shorter stages swap within a lane; then
+// columns and values are written in order.  Columns are unique within a row,
+// so the order is the column order.  Rows that do not fit are left to
+// k_sort_rows.
+__global__ void __launch_bounds__(256, 2) k_sort_rows_w(uint64_t n, const uint64_t* __restrict__ rowptr,
+                                                     uint32_t* __restrict__ col, const double* __restrict__ val,
+                                                     double* __restrict__ out64, float* __restrict__ hi,
+                                                     float* __restrict__ lo, unsigned long long* __restrict__ upper_count) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t w0 = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t nw = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long up = 0;
+  for (uint64_t row = w0; row < n; row += nw) {
+    const uint64_t b = rowptr[row];
+    const int len = int(rowptr[row + 1] - b);
+    if (len > 1024) continue;
+    uint32_t v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int pos = lane * 32 + i;
+      v[i] = pos < len ? (col[b + pos] << 10) | uint32_t(pos) : 0xffffffffu;
+    }
+#pragma unroll
+    for (int k = 2; k <= 1024; k <<= 1) {
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        if (j >= 32) {
+          const int lm = j >> 5;
+          const bool lower = (lane & lm) == 0;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            const bool asc = ((lane * 32 + i) & k) == 0;
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, v[i], lm);
+            v[i] = (asc == lower) ? min(v[i], o) : max(v[i], o);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            if (i & j) continue;
+            const bool asc = ((lane * 32 + i) & k) == 0;
+            const uint32_t a = v[i], c = v[i | j];
+            if ((a > c) == asc) {
+              v[i] = c;
+              v[i | j] = a;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int pos = lane * 32 + i;
+      if (pos < len) {
+        const uint32_t c = v[i] >> 10;
+        const double x = val[b + (v[i] & 1023u)];
+        col[b + pos] = c;
+        if (out64) out64[b + pos] = x;
+        if (hi) {
+          const float h = float(x);
+          hi[b + pos] = h;
+          lo[b + pos] = float(x - double(h));
+        }
+        up += c >= row;
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) up += __shfl_xor_sync(0xffffffffu, up, o);
+  if (lane == 0 && up) atomicAdd(upper_count, up);
 }
 
 __global__ void k_max_u32(const uint32_t* __restrict__ a, uint64_t n, unsigned* __restrict__ out) {
@@ -472,11 +547,24 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   DBuf<unsigned long long> dup(1);
   CG_CUDA(cudaMemsetAsync(dup.p, 0, 8, s));
   if (n) {
-    int st = std::min(256, std::max(32, L / 2));
-    unsigned sg = unsigned(std::min<uint64_t>(n, 152ull * 16));
-    k_sort_rows<<<sg, st, smem, s>>>(n, h.rowptr.p, h.col.p, tmpval.p, h.val64.p, h.hi.p, h.lo.p, dup.p);
-    CG_CUDA(cudaGetLastError());
-    count_launch();
+    // rows of up to 1024 entries: warp-per-row register sort; longer rows
+    // (or 2^22 rows and more, whose columns need more than 22 key bits):
+    // CTA-per-row shared-memory sort
+    const bool warp_sort = n < (1ull << 22);
+    if (warp_sort) {
+      const unsigned wg = unsigned(std::min<uint64_t>((n * 32 + 255) / 256, 152ull * 64));
+      k_sort_rows_w<<<wg, 256, 0, s>>>(n, h.rowptr.p, h.col.p, tmpval.p, h.val64.p, h.hi.p, h.lo.p, dup.p);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+    }
+    if (!warp_sort || h.max_row > 1024) {
+      int st = std::min(256, std::max(32, L / 2));
+      unsigned sg = unsigned(std::min<uint64_t>(n, 152ull * 16));
+      k_sort_rows<<<sg, st, smem, s>>>(n, h.rowptr.p, h.col.p, tmpval.p, h.val64.p, h.hi.p, h.lo.p, dup.p,
+                                       warp_sort ? 1025 : 0);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+    }
   }
   unsigned long long up = 0;
   CG_CUDA(cudaMemcpyAsync(&up, dup.p, 8, cudaMemcpyDeviceToHost, s));
