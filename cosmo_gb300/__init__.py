@@ -72,7 +72,8 @@ class DavidsonParams(C.Structure):
                 ("tol_resid", C.c_double), ("switch_resid", C.c_double), ("precision", C.c_int32),
                 ("verbose", C.c_int32), ("ortho_block", C.c_int32), ("algorithm", C.c_int32),
                 ("keep", C.c_int32), ("precond", C.c_int32), ("refine_lim", C.c_int32),
-                ("refine_keep", C.c_int32), ("ortho_pip", C.c_int32), ("refine_block", C.c_int32)]
+                ("refine_keep", C.c_int32), ("ortho_pip", C.c_int32), ("refine_block", C.c_int32),
+                ("refine_fp32_corrections", C.c_int32)]
 
 
 class BatchParams(C.Structure):
@@ -515,7 +516,8 @@ def davidson_diagonalization(h: Hamiltonian, nstates: int = 10, want_vectors: bo
 
     Keyword arguments set :class:`DavidsonParams` fields (block, lim, maxiter,
     crite, critc, critr, ortho, tol_resid, switch_resid, precision, verbose,
-    ortho_block, algorithm, keep, precond, refine_lim, refine_keep, ortho_pip, refine_block).  precision
+    ortho_block, algorithm, keep, precond, refine_lim, refine_keep, ortho_pip, refine_block,
+    refine_fp32_corrections).  precision
     defaults to the matrix precision."""
     kw.setdefault("precision", h.precision)
     p = davidson_params(nstates, **kw)

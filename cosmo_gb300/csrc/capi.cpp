@@ -686,6 +686,7 @@ void cg_davidson_defaults(cg_davidson_params* prm, int32_t nstates) {
   prm->refine_keep = 0;
   prm->ortho_pip = 1;
   prm->refine_block = 0;
+  prm->refine_fp32_corrections = 1;
 }
 
 cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, const double* init, int32_t n_init,
@@ -701,6 +702,9 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     if (prm->block < 1 || prm->block > nume) throw cg::Error(CG_ERR_ARG, "block must be in 1..nstates");
     if (prm->lim <= nume || prm->lim > 64) throw cg::Error(CG_ERR_ARG, "lim must be in nstates+1..64");
     if (n_init < 0 || (n_init > 0 && !init)) throw cg::Error(CG_ERR_ARG, "bad initial vectors");
+    // a restart forms the kept Ritz vectors in place, at most 32 columns a pass
+    if (prm->keep < 0 || prm->keep > 32) throw cg::Error(CG_ERR_ARG, "keep must be in 0..32");
+    if (prm->refine_keep < 0 || prm->refine_keep > 32) throw cg::Error(CG_ERR_ARG, "refine_keep must be in 0..32");
     if (prm->precision != CG_PREC_FP64 && prm->precision != CG_PREC_FP32)
       throw cg::Error(CG_ERR_ARG, "precision must be CG_PREC_FP64 or CG_PREC_FP32");
     if (prm->precision != h->h.precision && !h->h.virt)
@@ -751,6 +755,7 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
         if (prm->refine_block > 16) throw cg::Error(CG_ERR_ARG, "refine_block must be in 1..16");
         c2.block = prm->refine_block;
       }
+      c2.fp32_corr = prm->refine_fp32_corrections != 0;
       if (c2.keep + c2.block > c2.lim) c2.keep = std::max(nume, c2.lim - c2.block);
 
       rq.phase2 = c2;

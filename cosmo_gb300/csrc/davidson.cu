@@ -218,45 +218,6 @@ __global__ void __launch_bounds__(256) k_xty_w(uint64_t n, const T* __restrict__
   }
 }
 
-// Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G with JP lanes per row (JP =
-// J rounded up to a power of two <= 32).  A row's readers and writers are in
-// one warp and every read of the row happens before __syncwarp(), so X and Y
-// may alias (in-place collapse).
-template <class T>
-__global__ void __launch_bounds__(256) k_gemm_s(uint64_t n, const T* X, int ldx, int xo, int K,
-                                                const double* __restrict__ G, T* Y, int ldy, int yo, int J, int JP,
-                                                double alpha, double beta) {
-  __shared__ T gs[64 * 32];
-  for (int i = threadIdx.x; i < K * J; i += blockDim.x) gs[i] = T(alpha * G[i]);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, j = lane % JP, sub = lane / JP, rows_per_warp = 32 / JP;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const T tb = T(beta);
-  const bool act = j < J;
-  for (uint64_t base = uint64_t(warp) * rows_per_warp; base < n; base += uint64_t(nwarps) * rows_per_warp) {
-    const uint64_t r = base + sub;
-    T t = T(0), old = T(0);
-    const bool ok = act && r < n;
-    if (ok) {
-      const T* xr = X + r * ldx + xo;
-      int k = 0;
-      for (; k + 8 <= K; k += 8) {
-        T xv[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) xv[u] = xr[k + u];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) t = fma(xv[u], gs[(k + u) * J + j], t);
-      }
-      for (; k < K; ++k) t = fma(xr[k], gs[k * J + j], t);
-      if (beta != 0.0) old = Y[r * ldy + yo + j];
-    }
-    __syncwarp();
-    if (ok) Y[r * ldy + yo + j] = (beta == 0.0) ? t : fma(tb, old, t);
-    __syncwarp();
-  }
-}
-
 // ---- double-float arithmetic for the FP64 engine (dfloat.h) ----------------
 
 // X^T Y of the FP64 engine in double-float: as k_xty_t, with the staged Y chunk
@@ -802,6 +763,24 @@ __global__ void k_stage_block(uint64_t n, const float* __restrict__ B, int ld, i
   W[idx] = j < m ? B[i * ld + c0 + j] : 0.f;
 }
 
+// W (n x 8 FP32, zero-padded) = columns c0 .. c0+m of the FP64 block B, rounded
+__global__ void k_narrow8(uint64_t n, const double* __restrict__ B, int ld, int c0, int m, float* __restrict__ W) {
+  uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * 8) return;
+  uint64_t i = idx >> 3;
+  int j = int(idx & 7);
+  W[idx] = j < m ? float(B[i * ld + c0 + j]) : 0.f;
+}
+
+// Y[:, c0 .. c0+m] (FP64) = W (n x 8 FP32), first m columns
+__global__ void k_widen8(uint64_t n, const float* __restrict__ W, int m, double* __restrict__ Y, int ld, int c0) {
+  uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (idx >= n * 8) return;
+  uint64_t i = idx >> 3;
+  int j = int(idx & 7);
+  if (j < m) Y[i * ld + c0 + j] = double(W[idx]);
+}
+
 template <class T>
 __global__ void k_set_units(T* __restrict__ B, int ld, const uint64_t* __restrict__ rows, int m) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -936,6 +915,10 @@ struct Engine {
   }
   // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
+    // every kernel below holds G (K x J) in shared memory sized kMaxK x kMaxJ
+    // and gives a row at most 32 lanes
+    if (K < 0 || K > kMaxK || J < 0 || J > kMaxJ) throw Error(CG_ERR_INTERNAL, "gemm shape out of range");
+    if (K == 0 || J == 0) return;
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
     const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
@@ -955,21 +938,44 @@ struct Engine {
     if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
-    else if (J <= 32) k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
-    else {
-      int JP = 1;
-      while (JP < J) JP <<= 1;
-      unsigned g2 = unsigned(std::min<uint64_t>((n * JP + 255) / 256, uint64_t(nsm_) * 8));
-      k_gemm_s<T><<<g2, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, JP, alpha, beta);
-    }
+    else k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));  // G's staging buffer is reused by the next call
   }
   DBuf<float> stage;  // FP32 engine: aligned SpMM input block (n x 16)
+  // Refinement phase: once the starting vectors' products are in AB (double-
+  // float), the correction blocks are multiplied in FP32 (FP32 matrix values,
+  // vectors rounded to FP32).  A correction enters a converged Ritz vector
+  // with a coefficient of the order of the residual (<= the switch residual,
+  // 3e-5 in the mixed solve), so the FP32 product's ~1e-7 relative error
+  // reaches the Ritz vector's product as ~1e-7 |H| * 3e-5, far below the
+  // residual threshold; the final Ritz vectors are multiplied again in
+  // double-float and their residuals checked before the phase ends.
+  bool fp32_corr_ = false;
+  DBuf<float> y32_;
+  void spmm_narrow(int c0, int m) {
+    if (!stage.p) stage.alloc(n * 16);
+    if (!y32_.p) y32_.alloc(n * 8);
+    const double* Bd = reinterpret_cast<const double*>(B.p);
+    double* ABd = reinterpret_cast<double*>(AB.p);
+    for (int c = 0; c < m; c += 8) {
+      const int mc = std::min(8, m - c);
+      k_narrow8<<<blocks_for(n * 8), 256, 0, s>>>(n, Bd, L, c0 + c, mc, stage.p);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+      if (H.virt) virtual_product_f32(H, stage.p, y32_.p, 8, mc, s);
+      else spmm_f32_padded(H, stage.p, 8, y32_.p, 8, mc, s);
+      k_widen8<<<blocks_for(n * 8), 256, 0, s>>>(n, y32_.p, mc, ABd, L, c0 + c);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+    }
+  }
   void spmm(int c0, int m) {
     CG_CUDA(cudaEventRecord(ev0, s));
-    if (H.virt) {
+    if (fp32_corr_) {
+      spmm_narrow(c0, m);
+    } else if (H.virt) {
       // on-the-fly product: pack 8 (FP32) or 4 (FP64) columns at a time
       if (!stage.p) stage.alloc(n * 16);
       if constexpr (sizeof(T) == 4) {
@@ -1307,6 +1313,21 @@ struct Engine {
     count_launch();
   }
 
+  // B[:, 0:nume], AB[:, 0:nume] = the Ritz vectors of the current projection
+  // and their products; S = diag(Ritz values), kpass = nume
+  void to_ritz() {
+    std::vector<double> G(size_t(kpass) * nume);
+    for (int k = 0; k < kpass; ++k)
+      for (int j = 0; j < nume; ++j) G[size_t(k) * nume + j] = svec(j, k);
+    gemm(B.p, 0, kpass, G, B.p, 0, nume, 1.0, 0.0);
+    gemm(AB.p, 0, kpass, G, AB.p, 0, nume, 1.0, 0.0);
+    std::fill(S.begin(), S.end(), 0.0);
+    for (int i = 0; i < nume; ++i) S[size_t(i) * lim + i] = eigs[i];
+    kpass = nume;
+    zvec.assign(size_t(nume) * nume, 0.0);
+    for (int i = 0; i < nume; ++i) zvec[size_t(i) * nume + i] = 1.0;
+  }
+
   // Residual-driven block Davidson with thick restart (the mixed-precision
   // solve): every iteration re-checks the residual of every wanted pair, adds
   // the preconditioned residuals of the unconverged ones (largest first), and
@@ -1335,6 +1356,7 @@ struct Engine {
     }
     kpass = niv;
     add_ab_s(0, kpass, nmv);
+    fp32_corr_ = sizeof(T) == 8 && cfg.spmm_prec == CG_PREC_REFINE && cfg.fp32_corr;
     const int keep = std::max(nume, std::min(cfg.keep > 0 ? cfg.keep : 2 * nume, lim - mblock));
     int nloops = 0;
     bool done = false;
@@ -1371,6 +1393,24 @@ struct Engine {
         std::fprintf(stderr, "dav[%s] it %d kpass %d unconverged %zu max_resid %.3e E0 %.8f E%d %.8f\n",
                      sizeof(T) == 4 ? "fp32" : "fp64", nloops, kpass, unc.size(), mx, eigs[0], nume - 1,
                      eigs[nume - 1]);
+      }
+      if (unc.empty() && fp32_corr_) {
+        // every residual is below the threshold on the FP32 correction
+        // products: multiply the Ritz vectors again in double-float and take
+        // the residuals from those products
+        fp32_corr_ = false;
+        to_ritz();
+        add_ab_s(0, nume, nmv);
+        diagonalize();
+        to_ritz();
+        rn = residuals(all);
+        for (int i = 0; i < nume; ++i)
+          if (!(rn[i] < cfg.critr)) unc.push_back(i);
+        if (cfg.verbose & 1) {
+          double mx = 0;
+          for (double r : rn) mx = std::max(mx, r);
+          std::fprintf(stderr, "dav[fp64] double-float check: unconverged %zu max_resid %.3e\n", unc.size(), mx);
+        }
       }
       if (unc.empty()) { done = true; break; }
       if (nloops >= cfg.maxiter) break;

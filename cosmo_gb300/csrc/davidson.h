@@ -19,6 +19,7 @@ struct DavConfig {
   bool modern = false;    // residual-driven iteration with thick restart
   int keep = 0;           // Ritz vectors kept at a restart (modern; 0: 2 * nume)
   int precond = 1;        // modern: 1 diagonal preconditioner, 0 plain residuals
+  bool fp32_corr = false; // refinement (modern): correction blocks multiplied in FP32, result checked in double-float
   int verbose = 0;
 };
 

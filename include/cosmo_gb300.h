@@ -280,10 +280,10 @@ typedef struct {
                         Test_Convergence, collapse to nstates vectors);
                         1: residual-driven block Davidson: every wanted residual is
                         re-checked each iteration, restarts keep `keep` Ritz vectors */
-  int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates) */
+  int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates; at most 32) */
   int32_t precond;   /* algorithm 1: 1 = diagonal preconditioner (lambda - H_ii), 0 = none */
   int32_t refine_lim;   /* mixed solve: basis limit of the FP64 refinement phase (0: lim) */
-  int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep) */
+  int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep; at most 32) */
   int32_t ortho_pip;    /* algorithm 1 (default 1): orthogonalise each new block by two
                            passes of block Gram-Schmidt with Pythagorean inner products,
                            the Cholesky-QR of the block folded into the same update
@@ -291,6 +291,13 @@ typedef struct {
                            to the classical two passes + Cholesky-QR twice when the block
                            is nearly inside the basis.  0: always the classical form. */
   int32_t refine_block; /* mixed solve: vectors added per refinement iteration (0: block) */
+  int32_t refine_fp32_corrections; /* mixed solve, algorithm 1 (default 1): in the refinement
+                           phase only the starting vectors are multiplied in double-float;
+                           the correction blocks use the FP32 product (they enter the Ritz
+                           vectors with coefficients of the order of the residual), and the
+                           converged Ritz vectors are multiplied again in double-float, their
+                           residuals checked, iterating on with double-float products if one
+                           is above tol_resid.  0: every refinement product in double-float. */
 } cg_davidson_params;
 
 typedef struct {

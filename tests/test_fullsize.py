@@ -2,8 +2,8 @@
 through size-independent properties, since the oracle cannot run them in
 seconds: basis sizes, the block-tiled product against the row-wise product,
 symmetry (x . H y = y . H x, dots accumulated in FP64) and linearity of the
-stored and on-the-fly products, and the on-the-fly product against the stored
-one.  Tolerances: 2e-6 of max|y| between the two FP32 stored kernels (same
+stored and on-the-fly products, the on-the-fly product against the stored
+one, and the mixed solve's residuals under the FP64 product.  Tolerances: 2e-6 of max|y| between the two FP32 stored kernels (same
 values, different summation order), 1e-5 for FP32 products against each other
 or in linear combinations, 1e-6 relative for the FP32 symmetry defect."""
 import numpy as np
@@ -79,3 +79,21 @@ def test_fp55_on_the_fly_symmetry_linearity(gpu_available, tmp_path):
     lhs = _prod(hv, 2 * x - 0.5 * z)
     rhs = 2 * _prod(hv, x) - 0.5 * _prod(hv, z)
     assert float((lhs - rhs).abs().max()) <= 1e-5 * float(rhs.abs().max())
+
+
+def test_fp44_mixed_solve_true_residuals(gpu_available, tmp_path):
+    """The mixed solve at full size (the benchmark's parameters): the returned
+    vectors' residuals under the FP64 on-the-fly product equal the reported
+    ones and are <= 1e-5."""
+    p, b = _system(tmp_path, "fp", 4, 4, 7)
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    r = cg.davidson_diagonalization(h, 10, want_vectors=True, precision=cg.CG_PREC_FP32, tol_resid=1e-5,
+                                    block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5,
+                                    refine_lim=32, refine_keep=16)
+    assert r.stats.converged == 10, (r.resid, r.stats.ierr)
+    del h
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP64, virtual=True)
+    V = r.vecs.T
+    res = np.linalg.norm(hv.times_matrix(V, cg.CG_PREC_FP64) - V * r.eig, axis=0)
+    assert np.all(res <= 1e-5), res
+    np.testing.assert_allclose(res, r.resid, rtol=1e-3, atol=1e-8)

@@ -179,6 +179,42 @@ def test_davidson_mixed_vs_exact(gpu_available, name, pip, tmp_path):
     np.testing.assert_allclose(V @ V.T, np.eye(nst), rtol=0, atol=1e-8)
 
 
+MIXED = dict(precision=cg.CG_PREC_FP32, tol_resid=1e-5, block=8, lim=64, keep=32, algorithm=1, precond=1,
+             switch_resid=3e-5, refine_lim=32, refine_keep=16)
+
+
+@pytest.mark.parametrize("name", ["fp22m0s3", "sd44m0s4", "mg24usdb", "sd66m0s5"])
+def test_davidson_mixed_fp32_corrections(gpu_available, name, tmp_path):
+    """Refinement phase with the correction blocks multiplied in FP32
+    (refine_fp32_corrections=1, default) and in double-float (0): the reported
+    residuals are the residuals of the returned vectors under the FP64 matrix
+    (an FP64 build multiplied in FP64), all <= 1e-5, and both give the same
+    eigenvalues (to resid^2 / gap)."""
+    nst = 10
+    _, _, h = _gpu(name, str(tmp_path), cg.CG_PREC_FP32)
+    _, _, h64 = _gpu(name, str(tmp_path))
+    out = []
+    for corr in (1, 0):
+        r = cg.davidson_diagonalization(h, nst, want_vectors=True, refine_fp32_corrections=corr, **MIXED)
+        assert r.stats.converged == nst, (corr, r.resid, r.stats.ierr)
+        V = r.vecs.T
+        res = np.linalg.norm(h64.times_matrix(V) - V * r.eig, axis=0)
+        assert np.all(res <= 1e-5), (corr, res)
+        np.testing.assert_allclose(res, r.resid, rtol=1e-3, atol=1e-8)
+        np.testing.assert_allclose(V.T @ V, np.eye(nst), rtol=0, atol=1e-8)
+        out.append(r)
+    np.testing.assert_allclose(out[0].eig, out[1].eig, rtol=0, atol=1e-7)
+
+
+def test_davidson_keep_bound(gpu_available, tmp_path):
+    """A restart forms the kept Ritz vectors in place, at most 32 columns: keep
+    and refine_keep above 32 are refused on the host before any work."""
+    _, _, h = _gpu("sd22m0s1", str(tmp_path), cg.CG_PREC_FP32)
+    for kw in (dict(keep=40), dict(refine_keep=40)):
+        with pytest.raises(cg.CosmoError, match="keep must be in 0..32"):
+            cg.davidson_diagonalization(h, 4, precision=cg.CG_PREC_FP32, lim=64, block=4, **kw)
+
+
 def test_ee_roundtrip(gpu_available, tmp_path):
     _, _, h = _gpu("sd22m0s1", str(tmp_path))
     r = cg.davidson_diagonalization(h, 4, want_vectors=True)
