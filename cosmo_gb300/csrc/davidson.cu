@@ -455,11 +455,20 @@ __device__ __forceinline__ void ld8c(const float* p, float (&v)[8]) {
                : "memory");
 }
 
+// 32-byte store of 8 consecutive floats (32-byte aligned address): one L1
+// request per thread instead of eight partial-sector stores.
+__device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+               :
+               : "l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
+}
+
 template <class T, int CMAX>
 __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
                                                  int ld, int K, const double* __restrict__ Sc,
                                                  const double* __restrict__ lam, int C, T* __restrict__ R, int ldr,
-                                                 double* __restrict__ part, bool vec) {
+                                                 double* __restrict__ part, bool vec, bool vec_r) {
   __shared__ __align__(16) T ss[64 * CMAX];
   __shared__ T ls[CMAX];
   __shared__ double red[8][CMAX];
@@ -472,6 +481,7 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
   T nrm[CMAX];
 #pragma unroll
   for (int c = 0; c < CMAX; ++c) nrm[c] = T(0);
+  const int cvec = (sizeof(T) == 4 && vec_r) ? C / 8 * 8 : 0;  // columns written by 32-byte stores
   for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
     // res_c = sum_k (AB_k - lam_c B_k) s_kc: one accumulator per candidate
     T res[CMAX];
@@ -501,10 +511,22 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
     }
 #pragma unroll
     for (int c = 0; c < CMAX; ++c)
-      if (c < C) {
-        R[r * ldr + c] = res[c];
-        nrm[c] = fma(res[c], res[c], nrm[c]);
-      }
+      if (c < C) nrm[c] = fma(res[c], res[c], nrm[c]);
+    T* rr = R + r * ldr;
+    if constexpr (sizeof(T) == 4) {
+      // R rows 32-byte aligned: whole 8-column groups as one store each
+#pragma unroll
+      for (int g = 0; g < CMAX / 8; ++g)
+        if (8 * g + 8 <= cvec) {
+          float v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = res[8 * g + u];
+          st8(rr + 8 * g, v);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < CMAX; ++c)
+      if (c >= cvec && c < C) rr[c] = res[c];
   }
   // CTA partials: warp shuffles then the 8 warps in order
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -529,7 +551,7 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
 template <class T, int JMAX>
 __global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx, int xo, int K,
                                                 const double* __restrict__ G, T* Y, int ldy, int yo, int J,
-                                                double alpha, double beta, bool vec_x) {
+                                                double alpha, double beta, bool vec_x, bool vec_y) {
   __shared__ __align__(16) T gs[64 * JMAX];
   for (int i = threadIdx.x; i < 64 * JMAX; i += blockDim.x) {
     const int k = i / JMAX, j = i % JMAX;
@@ -561,6 +583,26 @@ __global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx,
       for (int j = 0; j < JMAX; ++j) acc[j] = fma(xv, gs[k * JMAX + j], acc[j]);
     }
     T* yr = Y + r * ldy + yo;
+    if constexpr (sizeof(T) == 4 && JMAX % 8 == 0) {
+      if (vec_y) {  // Y segment 32-byte aligned, J a multiple of 8: 32-byte stores
+#pragma unroll
+        for (int g = 0; g < JMAX / 8; ++g)
+          if (8 * g < J) {
+            float v[8];
+            if (beta != 0.0) {
+              float o[8];
+              ld8c(yr + 8 * g, o);
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = fma(tb, o[u], acc[8 * g + u]);
+            } else {
+#pragma unroll
+              for (int u = 0; u < 8; ++u) v[u] = acc[8 * g + u];
+            }
+            st8(yr + 8 * g, v);
+          }
+        continue;
+      }
+    }
 #pragma unroll
     for (int j = 0; j < JMAX; ++j)
       if (j < J) yr[j] = (beta == 0.0) ? acc[j] : fma(tb, yr[j], acc[j]);
@@ -859,7 +901,9 @@ struct Engine {
     nparts = int((n + rows_per_cta - 1) / rows_per_cta);
     B.alloc(n * L);
     AB.alloc(n * L);
-    ldr = (std::max(nume, 1) + align - 1) / align * align;
+    // FP32 residual rows padded to 32 bytes (stored 8 columns at a time)
+    const int ralign = sizeof(T) == 4 ? 8 : 2;
+    ldr = (std::max(nume, 1) + ralign - 1) / ralign * ralign;
     R.alloc(n * ldr);
     xwarps_ = uint64_t(nsm) * 32;  // 4 CTAs of 8 warps per SM
     xrows_ = (n + xwarps_ - 1) / xwarps_;
@@ -921,6 +965,7 @@ struct Engine {
     if (K == 0 || J == 0) return;
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
+    const bool vy = reinterpret_cast<uintptr_t>(Yp + yo) % 32 == 0 && L % 8 == 0 && J % 8 == 0;
     const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     if constexpr (sizeof(T) == 8) {
       if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
@@ -935,10 +980,10 @@ struct Engine {
         return;
       }
     }
-    if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
-    else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
-    else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
-    else k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx);
+    if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
+    else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
+    else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
+    else k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));  // G's staging buffer is reused by the next call
@@ -1079,6 +1124,7 @@ struct Engine {
     const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     const bool vec = L % 8 == 0 && reinterpret_cast<uintptr_t>(B.p) % 32 == 0 &&
                      reinterpret_cast<uintptr_t>(AB.p) % 32 == 0;
+    const bool vec_r = ldr % 8 == 0 && reinterpret_cast<uintptr_t>(R.p) % 32 == 0;
     bool done = false;
     if constexpr (sizeof(T) == 8) {
       if (cfg.spmm_prec == CG_PREC_REFINE) {
@@ -1091,9 +1137,9 @@ struct Engine {
     }
     if (!done) {
       if (C <= 8)
-        k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
+        k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec, vec_r);
       else
-        k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec);
+        k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec, vec_r);
     }
     CG_CUDA(cudaGetLastError());
     count_launch();
