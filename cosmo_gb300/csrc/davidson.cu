@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(256, 4) k_xty_t(uint64_t n, const T* __restric
     T c0v[JMAX], c1v[JMAX];
 #pragma unroll
     for (int j = 0; j < JMAX; ++j) { c0v[j] = T(0); c1v[j] = T(0); }
-    constexpr int U = 4;  // rows of X loads in flight per lane
+    constexpr int U = sizeof(T) == 4 ? 8 : 4;  // rows of X loads in flight per lane
     for (int rr = 0; rr < rows; rr += U) {
       const T* xr0 = X + (c0 + rr) * ldx + xo;
       T xa[U], xb[U];
