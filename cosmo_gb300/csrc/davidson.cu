@@ -481,7 +481,9 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
   T nrm[CMAX];
 #pragma unroll
   for (int c = 0; c < CMAX; ++c) nrm[c] = T(0);
-  const int cvec = (sizeof(T) == 4 && vec_r) ? C / 8 * 8 : 0;  // columns written by 32-byte stores
+  // columns written by 32-byte stores: whole groups of 8, the ones past C
+  // hold exact zeros (zero weights in ss and ls), so no sector is written in part
+  const int cvec = (sizeof(T) == 4 && vec_r) ? (C + 7) / 8 * 8 : 0;
   for (uint64_t r = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; r < n; r += uint64_t(gridDim.x) * blockDim.x) {
     // res_c = sum_k (AB_k - lam_c B_k) s_kc: one accumulator per candidate
     T res[CMAX];
@@ -1124,7 +1126,7 @@ struct Engine {
     const unsigned rgrid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     const bool vec = L % 8 == 0 && reinterpret_cast<uintptr_t>(B.p) % 32 == 0 &&
                      reinterpret_cast<uintptr_t>(AB.p) % 32 == 0;
-    const bool vec_r = ldr % 8 == 0 && reinterpret_cast<uintptr_t>(R.p) % 32 == 0;
+    const bool vec_r = ldr % 8 == 0 && (C + 7) / 8 * 8 <= ldr && reinterpret_cast<uintptr_t>(R.p) % 32 == 0;
     bool done = false;
     if constexpr (sizeof(T) == 8) {
       if (cfg.spmm_prec == CG_PREC_REFINE) {
