@@ -175,3 +175,44 @@ def test_problem_from_terms_rejects_backward_keys():
     with pytest.raises(cg.CosmoError) as e:
         cg.Problem.from_terms(g["sps"], 12, 2, 2, 0, 0, g["esp_keys"], g["esp_vals"], bad, np.array([1.0]))
     assert e.value.status == -1
+
+
+def _header_struct(hdr, name):
+    """(member name, byte size) in declaration order of `typedef struct {...} name;`."""
+    import re
+    body = re.search(r"typedef struct \{([^{}]*)\}\s*" + name + r";", hdr).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    sizes = {"int32_t": 4, "uint32_t": 4, "int64_t": 8, "uint64_t": 8, "double": 8, "float": 4}
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"(?:const\s+)?([A-Za-z_0-9]+)\s*(.*)$", " ".join(decl.split()))
+        assert m, decl
+        for var in m.group(2).split(","):
+            var = var.strip()
+            out.append((var.lstrip("*").strip(), 8 if var.startswith("*") else sizes[m.group(1)]))
+    return out
+
+
+def test_python_structs_mirror_header():
+    """Every ctypes structure of the Python mirror has the members, order and
+    sizes of its C struct in include/cosmo_gb300.h (a mismatch would let the
+    library write past the Python object), and cg_davidson_defaults fills the
+    documented defaults."""
+    import ctypes
+    import cosmo_gb300 as cg
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "cosmo_gb300.h")).read()
+    pairs = {"cg_problem_info": cg.ProblemInfo, "cg_problem_desc": cg.ProblemDesc,
+             "cg_hamiltonian_info": cg.HamiltonianInfo, "cg_spmm_format_info": cg.SpmmFormatInfo,
+             "cg_davidson_params": cg.DavidsonParams, "cg_davidson_stats": cg.DavidsonStats,
+             "cg_batch_params": cg.BatchParams, "cg_batch_stats": cg.BatchStats}
+    for cname, py in pairs.items():
+        want = _header_struct(hdr, cname)
+        got = [(f[0], ctypes.sizeof(f[1])) for f in py._fields_]
+        assert got == want, (cname, got, want)
+    p = cg.davidson_params(10)
+    assert (p.block, p.lim, p.ortho_pip, p.refine_block, p.refine_fp32_corrections) == (10, 30, 1, 0, 1)
+    assert (p.keep, p.refine_keep, p.algorithm, p.precond) == (0, 0, -1, 1)
