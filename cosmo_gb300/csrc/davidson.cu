@@ -998,8 +998,11 @@ struct Engine {
   // 3e-5 in the mixed solve), so the FP32 product's ~1e-7 relative error
   // reaches the Ritz vector's product as ~1e-7 |H| * 3e-5, far below the
   // residual threshold; the final Ritz vectors are multiplied again in
-  // double-float and their residuals checked before the phase ends.
+  // double-float and their residuals checked before the phase ends (and the
+  // phase goes on in double-float if the residuals stall first).
   bool fp32_corr_ = false;
+  double corr_best_ = 1e300;  // smallest largest-residual seen on FP32 correction products
+  int corr_stall_ = 0;        // iterations since it last dropped by 10 %
   DBuf<float> y32_;
   void spmm_narrow(int c0, int m) {
     if (!stage.p) stage.alloc(n * 16);
@@ -1405,6 +1408,8 @@ struct Engine {
     kpass = niv;
     add_ab_s(0, kpass, nmv);
     fp32_corr_ = sizeof(T) == 8 && cfg.spmm_prec == CG_PREC_REFINE && cfg.fp32_corr;
+    corr_best_ = 1e300;
+    corr_stall_ = 0;
     const int keep = std::max(nume, std::min(cfg.keep > 0 ? cfg.keep : 2 * nume, lim - mblock));
     int nloops = 0;
     bool done = false;
@@ -1442,22 +1447,39 @@ struct Engine {
                      sizeof(T) == 4 ? "fp32" : "fp64", nloops, kpass, unc.size(), mx, eigs[0], nume - 1,
                      eigs[nume - 1]);
       }
-      if (unc.empty() && fp32_corr_) {
+      // FP32 correction products carry a noise floor of ~1e-7 |H| times the
+      // corrections' weight in the Ritz vectors; if the largest residual has
+      // not dropped by 10 % for 4 iterations the threshold may lie below that
+      // floor, and the phase goes on in double-float as after a failed check
+      if (fp32_corr_) {
+        double mx = 0;
+        for (double r : rn) mx = std::max(mx, r);
+        if (mx < 0.9 * corr_best_) {
+          corr_best_ = mx;
+          corr_stall_ = 0;
+        } else {
+          ++corr_stall_;
+        }
+      }
+      const bool stalled = fp32_corr_ && corr_stall_ >= 4;
+      if (fp32_corr_ && (unc.empty() || stalled)) {
         // every residual is below the threshold on the FP32 correction
-        // products: multiply the Ritz vectors again in double-float and take
-        // the residuals from those products
+        // products (or they stall): multiply the Ritz vectors again in
+        // double-float and take the residuals from those products
         fp32_corr_ = false;
         to_ritz();
         add_ab_s(0, nume, nmv);
         diagonalize();
         to_ritz();
         rn = residuals(all);
+        unc.clear();
         for (int i = 0; i < nume; ++i)
           if (!(rn[i] < cfg.critr)) unc.push_back(i);
         if (cfg.verbose & 1) {
           double mx = 0;
           for (double r : rn) mx = std::max(mx, r);
-          std::fprintf(stderr, "dav[fp64] double-float check: unconverged %zu max_resid %.3e\n", unc.size(), mx);
+          std::fprintf(stderr, "dav[fp64] double-float %s: unconverged %zu max_resid %.3e\n",
+                       stalled ? "products after a stall" : "check", unc.size(), mx);
         }
       }
       if (unc.empty()) { done = true; break; }

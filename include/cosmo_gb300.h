@@ -297,7 +297,9 @@ typedef struct {
                            vectors with coefficients of the order of the residual), and the
                            converged Ritz vectors are multiplied again in double-float, their
                            residuals checked, iterating on with double-float products if one
-                           is above tol_resid.  0: every refinement product in double-float. */
+                           is above tol_resid (also when the largest residual has not dropped
+                           by 10 % for 4 iterations: tol_resid below the FP32 products' noise).
+                           0: every refinement product in double-float. */
 } cg_davidson_params;
 
 typedef struct {

@@ -207,18 +207,19 @@ def test_davidson_mixed_fp32_corrections(gpu_available, name, tmp_path):
 
 
 def test_davidson_fp32_corrections_check_fails_over(gpu_available, tmp_path, capfd):
-    """When the double-float check of the refinement finds residuals above the
-    threshold, the iteration goes on with double-float products: an early
-    switch (1e-2) lets the FP32-multiplied corrections carry coefficients of
-    ~1e-2 (product errors ~1e-7 |H| * 1e-2, above a 1e-8 threshold), and the
-    returned vectors still have residuals <= 1e-8 under the FP64 matrix."""
+    """When the residuals on FP32 correction products stall above the threshold
+    (or the double-float check finds them above it), the refinement goes on
+    with double-float products: an early switch (1e-2) lets the FP32-multiplied
+    corrections carry coefficients of ~1e-2 (product errors ~1e-7 |H| * 1e-2,
+    above a 1e-8 threshold), and the returned vectors still have residuals
+    <= 1e-8 under the FP64 matrix."""
     nst = 10
     _, _, h = _gpu("mg24usdb", str(tmp_path), cg.CG_PREC_FP32)
     _, _, h64 = _gpu("mg24usdb", str(tmp_path))
     kw = dict(MIXED, switch_resid=1e-2, tol_resid=1e-8, verbose=1)
     r = cg.davidson_diagonalization(h, nst, want_vectors=True, **kw)
     err = capfd.readouterr().err
-    checks = [ln for ln in err.splitlines() if "double-float check" in ln]
+    checks = [ln for ln in err.splitlines() if "dav[fp64] double-float" in ln]
     assert len(checks) == 1
     assert int(checks[0].split("unconverged")[1].split()[0]) > 0, checks[0]
     assert r.stats.converged == nst, (r.resid, r.stats.ierr)
