@@ -1,7 +1,7 @@
 /*
  * CPU ORACLE — test infrastructure only.  Never shipped, never on the product
  * path: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline arm
- * load this library, and only as the checker or the timed CPU reference.
+ * load this library, and only as the parity reference or the timed CPU baseline.
  *
  * A plain-C (+OpenMP) restatement of the reference CoSMo algorithms on the CI
  * hot path, each function citing the reference code it follows:

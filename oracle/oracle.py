@@ -2,7 +2,7 @@
 
 ctypes wrapper over oracle/_build/liboracle.so (cosmo_oracle.c,
 oracle_davidson.c): a plain-C restatement of the reference algorithms used as
-the checker in tests/ and smoke(), and as the timed CPU reference in bench.py.
+the parity reference in tests/ and smoke(), and as the timed CPU baseline in bench.py.
 It is never imported by the product package.
 """
 from __future__ import annotations

@@ -1,6 +1,6 @@
-// Test-infrastructure driver (oracle side, never shipped): calls the reference
+// Test-infrastructure harness (oracle side, never shipped): calls the reference
 // CoSMo headers as they lie in the reference tree and dumps every intermediate
-// of the CI hot path so the GB300 build can be pinned against it.
+// of the CI hot path so the GB300 library can be pinned against it.
 //
 // It follows the logic of xsm::DXHV (include/xsm/DEXHVcsb.cxx:33-71) without
 // the Eigen fallback, which is the path DEXHVJTcsb (davidson/DEXHVJTcsb.cpp:36)

@@ -1,4 +1,4 @@
-// Test-infrastructure driver (oracle side, never shipped): the <J-J+> and
+// Test-infrastructure harness (oracle side, never shipped): the <J-J+> and
 // <T-T+> computation of the reference's XSHLJT (include/xsm/XSHLJT.cxx:38-142)
 // run with the reference headers as they lie in the reference tree, printing
 // full-precision values instead of XSHLJT's 6-digit log lines, plus the

@@ -187,7 +187,7 @@ def jt_case(name: str, work: str, xml: str, nstates: int, manifest: dict, keep_v
 
 def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) -> None:
     """The reference's .HH file (XHH+JJ, PPMatrix::Write): sha256, and the bytes
-    for one small case so the .HH reader can be pinned on the GPU machine."""
+    for one small case so the .HH reader can be pinned on a GPU."""
     with open(os.path.join(work, name + ".hh.log"), "w") as log:
         subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XHH+JJ"), xml], cwd=work, stdin=subprocess.DEVNULL,
                        stdout=log, stderr=subprocess.STDOUT, check=True)

@@ -283,7 +283,7 @@ def _parse_hh(raw: bytes):
 def test_hh_writer_vs_reference_file(gpu_available, name, tmp_path):
     """.HH from the GPU matrix against the reference XHH+JJ output: same rows,
     except entries with |H_ij| < 1e-14 that the reference file keeps and the
-    CSB (and this build) drops; byte-identical when there are none."""
+    CSB (and this library) drops; byte-identical when there are none."""
     m = manifest()[name]
     _, _, h = _gpu(name, str(tmp_path))
     f = tmp_path / "x.HH"
