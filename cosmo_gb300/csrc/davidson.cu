@@ -874,6 +874,7 @@ struct Engine {
   // host wall time per phase (verbose >= 2 prints them)
   double t_eig = 0, t_resid = 0, t_ortho = 0, t_collapse = 0, t_abs = 0;
   int pip_calls_ = 0, pip_fallbacks_ = 0;
+  int gemm_occ_[4] = {0, 0, 0, 0};  // resident CTAs per SM of k_gemm_r<T, 4|8|16|32>
   static double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
   }
@@ -968,7 +969,7 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
     const bool vy = reinterpret_cast<uintptr_t>(Yp + yo) % 32 == 0 && L % 8 == 0 && J % 8 == 0;
-    const unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
+    unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     if constexpr (sizeof(T) == 8) {
       if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
         const double* Xd = reinterpret_cast<const double*>(Xp);
@@ -982,6 +983,18 @@ struct Engine {
         return;
       }
     }
+    // one wave of resident CTAs (the grid-stride loop gives each thread whole
+    // rows, so the grid changes no result)
+    const int jc = J <= 4 ? 0 : J <= 8 ? 1 : J <= 16 ? 2 : 3;
+    if (!gemm_occ_[jc]) {
+      int per_sm = 0;
+      if (jc == 0) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 4>, 256, 0));
+      if (jc == 1) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 8>, 256, 0));
+      if (jc == 2) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 16>, 256, 0));
+      if (jc == 3) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 32>, 256, 0));
+      gemm_occ_[jc] = std::max(per_sm, 1);
+    }
+    grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * gemm_occ_[jc])));
     if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
     else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
     else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
