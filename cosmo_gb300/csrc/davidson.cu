@@ -440,9 +440,6 @@ __global__ void __launch_bounds__(256, 4) k_xty_t(uint64_t n, const T* __restric
   }
 }
 
-// R[:, c] = AB s_c - lam_c B s_c for C candidates, one thread per row with the
-// row read 4 values at a time, s in shared memory; per-CTA partial |R[:, c]|^2
-// (FP32 over a thread's rows, FP64 across threads, fixed order).
 // 32-byte load of 8 consecutive floats (32-byte aligned address): one L1
 // request per thread for a whole 8-float segment of a row (thread-per-row
 // kernels read rows 256 bytes apart, so every request touches one sector per
@@ -464,6 +461,10 @@ __device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
                : "memory");
 }
 
+// R[:, c] = AB s_c - lam_c B s_c for C candidates, one thread per row with the
+// row read 8 values (32 bytes) at a time when aligned, s in shared memory, R
+// rows written 8 columns at a time; per-CTA partial |R[:, c]|^2 (FP32 over a
+// thread's rows, FP64 across threads, fixed order).
 template <class T, int CMAX>
 __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
                                                  int ld, int K, const double* __restrict__ Sc,
