@@ -1512,6 +1512,15 @@ struct Engine {
       kpass += nncv;
       ++nloops;
     }
+    if (fp32_corr_) {
+      // stopped (iteration cap, no new direction) while on FP32 correction
+      // products: the returned residuals come from double-float products too
+      fp32_corr_ = false;
+      to_ritz();
+      add_ab_s(0, nume, nmv);
+      diagonalize();
+      to_ritz();
+    }
     out.de.resize(nume);
     for (int i = 0; i < nume; ++i) out.de[i] = std::fabs(old[i] - eigs[i]);
     // final Ritz vectors in B[:, 0:nume]

@@ -330,3 +330,18 @@ def test_hh_reader_on_reference_file(gpu_available, tmp_path):
         assert p1.keys() == p2.keys()
         assert max(abs(p1[k] - p2[k]) for k in p1) < 1e-12
         assert all(int(c.min()) >= i for i, (c, v) in enumerate(rows2) if len(c))
+
+
+def test_davidson_mixed_iteration_cap_residuals(gpu_available, tmp_path):
+    """A mixed solve stopped by the iteration cap inside the refinement (still
+    on FP32 correction products) reports the residuals of its returned vectors
+    under the FP64 matrix, and the unconverged status."""
+    nst = 10
+    _, _, h = _gpu("sd66m0s5", str(tmp_path), cg.CG_PREC_FP32)
+    _, _, h64 = _gpu("sd66m0s5", str(tmp_path))
+    r = cg.davidson_diagonalization(h, nst, want_vectors=True, **dict(MIXED, maxiter=3))
+    assert r.stats.refine_iterations == 3 and r.stats.converged < nst and r.stats.ierr != 0
+    V = r.vecs.T
+    res = np.linalg.norm(h64.times_matrix(V) - V * r.eig, axis=0)
+    np.testing.assert_allclose(res, r.resid, rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(V.T @ V, np.eye(nst), rtol=0, atol=1e-8)
