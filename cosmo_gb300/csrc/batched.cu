@@ -668,15 +668,6 @@ __global__ void k_bunits(int Q, const uint32_t* __restrict__ rows, int b, float*
   if (V64) V64[size_t(rows[i]) * ld + j] = 1.0;
 }
 
-template <class S, class D>
-__global__ void k_bconvert(uint64_t n, const S* __restrict__ a, int lda, D* __restrict__ b, int ldb, int cols) {
-  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  if (i >= n * cols) return;
-  const uint64_t r = i / cols;
-  const int j = int(i - r * cols);
-  b[r * ldb + j] = D(a[r * lda + j]);
-}
-
 // X[r][0:b] = Ritz vectors of the problem of tile: V[:, 0:K] Z[:, 0:b] with K the
 // freeze-time basis size for frozen problems; otherwise the last iteration's
 // (V[:, 0:b] when that iteration restarted, V[:, 0:last_k] Z otherwise)
