@@ -85,6 +85,49 @@ def basis(sps: np.ndarray, N: int, twom: int, tz2: int, parity: int, cap: int | 
     return z
 
 
+def basis_truncated(sps: np.ndarray, nv: int, zv: int, twom: int, parity: int,
+                    hw: tuple[int, int] | None = None, rejections=()) -> np.ndarray:
+    """The reference's truncated bases as a filter of the untruncated one.
+
+    XsysmbsOMP (xmlshell/xmbs/XsysmbsOMP.cpp:214-300) builds occupation
+    partitions per orbital level (neutron levels, then proton levels, :99-117),
+    drops partitions, and writes the surviving determinants in the order of the
+    untruncated basis (a sorted map, :405-428), so a filter of `basis` in order
+    restates it:
+    * hw (hwmin, hwmax): with Q = sum of 2n + l over occupied states, neutron
+      partitions with Qn in [Ncore, Ncore + hwmax] and proton ones with Qp in
+      [Pcore, Pcore + hwmax] (Partition::MakeQ, PartitionClass.cxx:151-190),
+      then Qn + Qp in [Ncore + Pcore + hwmin, Ncore + Pcore + hwmax]
+      (QuantaMinMaxPurge, :390-413).  Ncore (Pcore) is CoreQuanta
+      (include/sm/SingleParticleStates.cxx:155-168): the quanta of the first
+      nv neutron (zv proton) s.p. states in list order, since its sort covers
+      an empty range.
+    * rejections [(nmin, nmax, levels)]: the particles of both species in the
+      listed 0-based orbital levels (type "pn") number nmin..nmax
+      (TestRestriction, PartitionClass.cxx:23-40).
+    sps: rows (level n l 2j 2m 2t 2tz parity) as cosmo_gb300.Problem.sps()."""
+    sps = np.asarray(sps)
+    z = basis(sps, nv + zv, twom, nv - zv, parity)
+    keep = np.ones(len(z), dtype=bool)
+    neut = sps[:, 6] > 0
+    if hw is not None:
+        hwmin, hwmax = hw
+        q = 2 * sps[:, 1] + sps[:, 2]
+        ncore = int(q[neut][:nv].sum())
+        pcore = int(q[~neut][:zv].sum())
+        qz = q[z.astype(np.int64)]
+        nz = neut[z.astype(np.int64)]
+        qn = np.where(nz, qz, 0).sum(1)
+        qp = np.where(nz, 0, qz).sum(1)
+        keep &= (qn >= ncore) & (qn <= ncore + hwmax) & (qp >= pcore) & (qp <= pcore + hwmax)
+        keep &= (qn + qp >= ncore + pcore + hwmin) & (qn + qp <= ncore + pcore + hwmax)
+    for nmin, nmax, levels in rejections:
+        flag = np.isin(sps[:, 0], levels)
+        cnt = flag[z.astype(np.int64)].sum(1)
+        keep &= (cnt >= nmin) & (cnt <= nmax)
+    return z[keep]
+
+
 def build_upper(ns: int, k1, v1, k2, v2, z: np.ndarray, nthreads: int = 0):
     """Upper-triangle rows (CSR) of H from forward-ordered operator terms."""
     k1 = np.ascontiguousarray(k1, dtype=np.int32)

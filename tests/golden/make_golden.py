@@ -18,7 +18,7 @@ the GPU build must reproduce:
   nodes the reference XSHLJT writes
 
 usage (needs the reference tree; the fixtures are committed):
-    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
+    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME[,NAME...]]
 """
 from __future__ import annotations
 
@@ -39,6 +39,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from cosmo_gb300.synthetic import SD_ORBITS, SyntheticSystem, make_system, write_xml  # noqa: E402
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import truncated as TRUNC  # noqa: E402
 
 # name: (system, full dumps, Davidson nstates, Davidson iterations)
 CASES = {
@@ -206,13 +209,17 @@ def main() -> None:
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    only = set(a.only.split(",")) if a.only else None
+
+    def skip(name: str) -> bool:
+        return only is not None and name not in only
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref}"], check=True)
     mpath = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(mpath)) if os.path.exists(mpath) else {}
     work = tempfile.mkdtemp(prefix="cg_golden_")
     try:
         for name, (sysd, full, nst, it) in CASES.items():
-            if a.only and a.only != name:
+            if skip(name):
                 continue
             sysd.name = name
             _, xml = make_system(work, sysd)
@@ -224,7 +231,7 @@ def main() -> None:
             if full:
                 hh_case(name, work, xml, manifest, keep_bytes=(name == "sd22m0s1"))
         for name, sysd in BASIS_CASES.items():
-            if a.only and a.only != name:
+            if skip(name):
                 continue
             sysd.name = name
             _, xml = make_system(work, sysd)
@@ -236,7 +243,22 @@ def main() -> None:
                                   system=dict(space=sysd.space, nv=sysd.nv, zv=sysd.zv, twom=sysd.twom,
                                               parity=sysd.parity, jj=sysd.jj, seed=sysd.seed))
             print(name, manifest[name])
-        if not a.only or a.only == "mg24usdb":
+        # truncated bases (hw truncation, orbital rejections): the reference's .mbs
+        for name in TRUNC.CASES:
+            if skip(name):
+                continue
+            xml = TRUNC.write_case(work, name)
+            run_ref("XsysmbsOMP", xml, name, work, 0, 0)
+            mbs = os.path.join(work, name + ".mbs")
+            raw = open(mbs, "rb").read()
+            N = int(np.frombuffer(raw[:4], np.int32)[0])
+            n = int(np.frombuffer(raw[4:12], np.uint64)[0])
+            hw, rej = TRUNC.truncation(name)
+            manifest[name] = dict(n=n, N=N, mbs_sha256=sha(mbs), truncation=dict(hw=hw, rejections=rej))
+            np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                                mbs=np.frombuffer(raw[12:], np.uint16).reshape(n, N))
+            print(name, manifest[name])
+        if not skip("mg24usdb"):
             sysd = SyntheticSystem("sd", 4, 4, 0, "+", 0.0, 0, name="mg24usdb")
             xml = os.path.join(work, "mg24usdb.xml")
             write_xml(xml, sysd, os.path.join(a.ref, "interactions", "sd", "usdb.int"), USDB_ORBITS, hname="usdb")

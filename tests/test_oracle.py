@@ -216,3 +216,30 @@ def test_python_structs_mirror_header():
     p = cg.davidson_params(10)
     assert (p.block, p.lim, p.ortho_pip, p.refine_block, p.refine_fp32_corrections) == (10, 30, 1, 0, 1)
     assert (p.keep, p.refine_keep, p.algorithm, p.precond) == (0, 0, -1, 1)
+
+
+@pytest.mark.parametrize("name", ["psd22m0_hw2", "psd32m1_hwr13", "psd22m0_hw2_rej", "psd21m1_rej", "sdp22m0_hw2"])
+def test_oracle_truncated_basis_matches_reference(name, tmp_path):
+    """Truncated bases (oscillator-quanta limits and orbital-occupation
+    rejections of the reference's XsysmbsOMP, on p+sd spaces): the oracle's
+    filter of the untruncated basis equals the reference's .mbs, byte for
+    byte (fixtures from tests/golden/make_golden.py)."""
+    import hashlib
+    import sys
+    import cosmo_gb300 as cg
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import truncated as T
+    m = manifest()[name]
+    p = cg.Problem(T.write_case(str(tmp_path), name))
+    inf = p.info
+    hw, rej = T.truncation(name)
+    assert [hw, rej] == [tuple(m["truncation"]["hw"]) if m["truncation"]["hw"] else None,
+                         [(a, b, list(c)) for a, b, c in m["truncation"]["rejections"]]]
+    z = O.basis_truncated(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw, rej)
+    assert z.shape == (m["n"], m["N"])
+    assert np.array_equal(z, golden(name)["mbs"])
+    raw = np.int32(m["N"]).tobytes() + np.uint64(m["n"]).tobytes() + z.astype("<u2").tobytes()
+    assert hashlib.sha256(raw).hexdigest() == m["mbs_sha256"]
+    # every truncation drops determinants of the untruncated basis, none is added
+    full = O.basis(p.sps(), inf.nv + inf.zv, inf.twom, inf.nv - inf.zv, inf.parity)
+    assert 0 < len(z) < len(full)
