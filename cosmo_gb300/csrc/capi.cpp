@@ -219,6 +219,10 @@ cg_status cg_basis_build(const cg_problem* p, cg_basis** out) {
     CG_NOT_NULL(p);
     CG_NOT_NULL(out);
     *out = nullptr;
+    if (!p->sys.truncation.empty())
+      throw cg::Error(CG_ERR_UNSUPPORTED, "truncated bases (" + p->sys.truncation +
+                                              "on the system) are not built; the full basis would differ from the "
+                                              "reference's");
     require_device();
     auto b = std::make_unique<cg_basis>();
     b->sys = p->sys;

@@ -275,6 +275,9 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   if (const std::string* ft = sn->attr("T")) sys.filter_twoT = parse_spin2(*ft);
   if (!sn->attr("P")) throw Error(CG_ERR_PARSE, "system needs P");
   sys.parity = ((*sn->attr("P"))[0] == '-') ? 1 : 0;
+  if (sn->attr("hwmax")) sys.truncation += "hwmax ";
+  if (sn->count("hwrejection")) sys.truncation += "<hwrejection> ";
+  if (sn->count("rejection")) sys.truncation += "<rejection> ";
   if (const XmlNode* mb = sn->child("ManyBodyStates"))
     if (mb->attr("name")) sys.mbs_name = *mb->attr("name");
   if (const XmlNode* mx = sn->child("matrix")) {

@@ -69,6 +69,10 @@ struct System {
   int filter_twoJ = -1;          // system J / T attributes: XSHLJT keeps only these states
   int filter_twoT = -1;
   std::string xml_dir;
+  // basis truncations of the system node (hwmax attribute, <hwrejection>,
+  // <rejection>, xmlshell/xmbs/XsysmbsOMP.cpp:214-300), listed; the basis
+  // builder refuses a truncated system instead of building the full basis
+  std::string truncation;
 };
 
 System load_system(const std::string& xml_path, const std::string& system_name);

@@ -100,7 +100,10 @@ cg_status cg_problem_two_body(const cg_problem* p, int32_t* keys, double* vals);
 /* M-scheme Slater-determinant basis, enumerated on the GPU from per-species
  * bitstrings; index order is the reference's lexicographic order of sorted
  * s.p. tuples.  Replaces SM::MakeMBS2 (include/sm/MakeMBS.cxx:186) and the
- * Xsysmbs/XsysmbsOMP tools (xmlshell/xmbs/XsysmbsOMP.cpp:323). */
+ * Xsysmbs/XsysmbsOMP tools (xmlshell/xmbs/XsysmbsOMP.cpp:323).  A system with
+ * a basis truncation (hwmax attribute, <hwrejection> or <rejection> children,
+ * XsysmbsOMP.cpp:214-300) is refused with CG_ERR_UNSUPPORTED before any
+ * device work: the full basis built here would not be the reference's. */
 typedef struct cg_basis cg_basis;
 
 cg_status cg_basis_build(const cg_problem* p, cg_basis** out);

@@ -243,3 +243,19 @@ def test_oracle_truncated_basis_matches_reference(name, tmp_path):
     # every truncation drops determinants of the untruncated basis, none is added
     full = O.basis(p.sps(), inf.nv + inf.zv, inf.twom, inf.nv - inf.zv, inf.parity)
     assert 0 < len(z) < len(full)
+
+
+def test_truncated_system_refused_by_basis_builder(tmp_path):
+    """A system with a basis truncation loads (its s.p. table is usable), but
+    the basis builder refuses it with CG_ERR_UNSUPPORTED on the host, before
+    any device work, instead of building the full basis."""
+    import sys
+    import cosmo_gb300 as cg
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import truncated as T
+    for name in ("psd22m0_hw2", "psd32m1_hwr13", "psd21m1_rej"):
+        p = cg.Problem(T.write_case(str(tmp_path), name))
+        assert len(p.sps()) == 36
+        with pytest.raises(cg.CosmoError) as e:
+            cg.ManyBodyStates(p)
+        assert e.value.status == -6 and "truncated bases" in str(e.value)
