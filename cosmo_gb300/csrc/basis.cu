@@ -133,6 +133,7 @@ void enumerate_species(SpeciesTables& sp, int norb, int k, const int* m2, const 
 }  // namespace
 
 void basis_build(const System& sys, Basis& b) {
+  refuse_truncated(sys);
   CG_CUDA(cudaGetDevice(&b.device));
   if (!b.stream) CG_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
   cudaStream_t s = b.stream;

@@ -219,10 +219,7 @@ cg_status cg_basis_build(const cg_problem* p, cg_basis** out) {
     CG_NOT_NULL(p);
     CG_NOT_NULL(out);
     *out = nullptr;
-    if (!p->sys.truncation.empty())
-      throw cg::Error(CG_ERR_UNSUPPORTED, "truncated bases (" + p->sys.truncation +
-                                              "on the system) are not built; the full basis would differ from the "
-                                              "reference's");
+    cg::refuse_truncated(p->sys);
     require_device();
     auto b = std::make_unique<cg_basis>();
     b->sys = p->sys;
@@ -468,14 +465,15 @@ cg_status cg_batch_create(const cg_problem* const* problems, int32_t count, cg_b
     CG_NOT_NULL(out);
     *out = nullptr;
     if (count < 1) throw cg::Error(CG_ERR_ARG, "count must be >= 1");
-    require_device();
     std::vector<const cg::System*> sys;
     std::vector<const cg::Operator*> ops;
     for (int i = 0; i < count; ++i) {
       CG_NOT_NULL(problems[i]);
+      cg::refuse_truncated(problems[i]->sys);
       sys.push_back(&problems[i]->sys);
       ops.push_back(&problems[i]->op);
     }
+    require_device();
     auto b = std::make_unique<cg_batch>();
     cg::batch_build(sys, ops, b->bs);
     *out = b.release();
@@ -562,9 +560,10 @@ cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* e
   return guard([&] {
     CG_NOT_NULL(xml_path);
     CG_NOT_NULL(ee_path);
-    require_device();
     const std::string sname = system_name ? system_name : "";
     cg::System sys = cg::load_system(xml_path, sname);
+    cg::refuse_truncated(sys);
+    require_device();
     cg::Basis b;
     cg::basis_build(sys, b);
     std::string file_attr = ee_path;

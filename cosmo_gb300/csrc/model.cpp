@@ -275,7 +275,8 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   if (const std::string* ft = sn->attr("T")) sys.filter_twoT = parse_spin2(*ft);
   if (!sn->attr("P")) throw Error(CG_ERR_PARSE, "system needs P");
   sys.parity = ((*sn->attr("P"))[0] == '-') ? 1 : 0;
-  if (sn->attr("hwmax")) sys.truncation += "hwmax ";
+  // getXMLData (include/xmlParser.cxx:129) takes hwmax from an attribute or a child element
+  if (sn->attr("hwmax") || sn->child("hwmax")) sys.truncation += "hwmax ";
   if (sn->count("hwrejection")) sys.truncation += "<hwrejection> ";
   if (sn->count("rejection")) sys.truncation += "<rejection> ";
   if (const XmlNode* mb = sn->child("ManyBodyStates"))
@@ -308,6 +309,13 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
     sys.int_scale.push_back(sc);
   }
   return sys;
+}
+
+void refuse_truncated(const System& sys) {
+  if (!sys.truncation.empty())
+    throw Error(CG_ERR_UNSUPPORTED, "truncated bases (" + sys.truncation +
+                                        "on the system) are not built; the full basis would differ from the "
+                                        "reference's");
 }
 
 // ----------------------------------------------------- Oxbash reader

@@ -77,6 +77,11 @@ struct System {
 
 System load_system(const std::string& xml_path, const std::string& system_name);
 
+// Throws CG_ERR_UNSUPPORTED for a system with a basis truncation: every route
+// that builds a basis (single problem, batch, XSHLJT) calls it before any
+// device work, so no truncated system is ever solved on the full basis.
+void refuse_truncated(const System& sys);
+
 // ------------------------------------------------------------ operators
 // Forward-ordered m-scheme operator terms.  Keys follow the reference's
 // STensor convention: the first half of a key is annihilated, the second half

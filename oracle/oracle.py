@@ -32,10 +32,20 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
+def reference_root() -> str | None:
+    """The reference checkout named by the COSMO_REFERENCE environment
+    variable, or None when it is unset or does not hold the reference tree."""
+    root = os.environ.get("COSMO_REFERENCE")
+    if root and os.path.isdir(os.path.join(root, "include")):
+        return root
+    return None
+
+
+def build_reference(ref_root: str | None = None) -> bool:
     """Compile the reference tools from the reference sources into oracle/_ref
-    (only where the reference tree exists; the GPU host uses prebuilt files)."""
-    if not os.path.isdir(os.path.join(ref_root, "include")):
+    (only where the reference tree is given, by argument or COSMO_REFERENCE)."""
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "include")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return True

@@ -18,7 +18,8 @@ the GPU build must reproduce:
   nodes the reference XSHLJT writes
 
 usage (needs the reference tree; the fixtures are committed):
-    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME[,NAME...]]
+    python tests/golden/make_golden.py --ref /path/to/reference [--only NAME[,NAME...]]
+(--ref defaults to the COSMO_REFERENCE environment variable)
 """
 from __future__ import annotations
 
@@ -206,9 +207,11 @@ def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) ->
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("COSMO_REFERENCE"))
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref or COSMO_REFERENCE")
     only = set(a.only.split(",")) if a.only else None
 
     def skip(name: str) -> bool:

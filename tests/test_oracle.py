@@ -40,9 +40,10 @@ def test_host_operator_terms_match_reference(name, tmp_path):
 
 def test_host_operator_usdb_matches_reference(tmp_path):
     """usdb with its mass scaling (needs the reference interaction file; skipped elsewhere)."""
-    usdb = "/root/reference/interactions/sd/usdb.int"
+    root = O.reference_root()
+    usdb = os.path.join(root, "interactions", "sd", "usdb.int") if root else ""
     if not os.path.exists(usdb):
-        pytest.skip("reference interaction file not present")
+        pytest.skip("reference checkout not given (COSMO_REFERENCE)")
     import cosmo_gb300 as cg
     from cosmo_gb300.synthetic import SyntheticSystem, write_xml
     orbits = [("0d3", 0, 2, 3), ("0d5", 0, 2, 5), ("1s1", 1, 0, 1)]
@@ -259,3 +260,29 @@ def test_truncated_system_refused_by_basis_builder(tmp_path):
         with pytest.raises(cg.CosmoError) as e:
             cg.ManyBodyStates(p)
         assert e.value.status == -6 and "truncated bases" in str(e.value)
+
+
+def test_truncated_system_refused_by_every_basis_route(tmp_path):
+    """The batched solver and the XSHLJT tool build bases too: both refuse a
+    truncated system on the host with CG_ERR_UNSUPPORTED (no device needed),
+    and hwmax given as a child element (<hwmax>2</hwmax>, which the
+    reference's getXMLData also reads) counts as a truncation."""
+    import sys
+    import cosmo_gb300 as cg
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import truncated as T
+    xml = T.write_case(str(tmp_path), "psd22m0_hw2")
+    with pytest.raises(cg.CosmoError) as e:
+        cg.Batch([cg.Problem(xml)])
+    assert e.value.status == -6 and "truncated bases" in str(e.value)
+    ee = tmp_path / "none.EE"
+    ee.write_bytes(b"")
+    with pytest.raises(cg.CosmoError) as e:
+        cg.xshljt(xml, str(ee), out=str(tmp_path / "out.xml"))
+    assert e.value.status == -6 and "truncated bases" in str(e.value)
+    txt = open(xml).read().replace(' hwmax="2"', "", 1).replace("<matrix JJ", "<hwmax>2</hwmax><matrix JJ", 1)
+    child = tmp_path / "child.xml"
+    child.write_text(txt)
+    with pytest.raises(cg.CosmoError) as e:
+        cg.ManyBodyStates(cg.Problem(str(child)))
+    assert e.value.status == -6 and "hwmax" in str(e.value)
