@@ -13,10 +13,12 @@ everything) and the SpMM kernel against the HBM roofline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-With --impl reference the reference algorithm runs on the host CPU cores
-(the C restatement in oracle/: CSB pull-form SpMM + Davidson, OpenMP) on the
-same problem, each step a bounded sample of Davidson iterations extrapolated
-to the iteration count of a full solve.
+With --impl reference the reference algorithm runs on the host CPU cores with
+nothing from the product library (oracle/: the XML and interaction
+restatement, basis, row builder, CSB pull-form SpMM and Davidson in C with
+OpenMP) on the same problem; each step is one Davidson iteration of one
+continuous run, and the value scales the measured seconds per iteration to the
+iteration cap at which that algorithm stops on this problem.
 """
 from __future__ import annotations
 
@@ -43,6 +45,9 @@ WORKLOAD = dict(workload="fp-shell 4p+4n M=0, lowest 10 eigenpairs, |dE|<=1e-4 M
                 l2="inputs larger than L2 (stored H ~15 GB, vectors ~300 MB)")
 # Davidson settings of the mixed solve (block vectors per SpMM, basis limit)
 MIXED = dict(block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5, refine_lim=32, refine_keep=16)
+# the same solver in FP64 (FP64 products, vectors and projections): the
+# precision-only baseline, run to the same tolerance
+FP64_SAME = dict(block=8, lim=64, keep=32, algorithm=1, precond=1)
 # Iterations the reference algorithm (block 10, limit 30) runs on this problem:
 # its 400-iteration cap (max(40 * nstates, 200)), which it reaches without
 # converging all 10 pairs to 1e-5 (measured with the same algorithm in FP64 on
@@ -221,6 +226,16 @@ def spmm_roofline(cg, h, b: int, reps: int = 20, warm: int = 3, fp64: bool = Fal
     return ms * 1e-3, alg
 
 
+def per_state_errors(cg, basis, eig_mixed, vecs_mixed, r64, twom: int):
+    """Eigenvalue and <J-J+> error of every mixed-precision state against the
+    FP64 solve (states paired in energy order)."""
+    jm, _ = cg.jt_expectations(basis, vecs_mixed)
+    j6, _ = cg.jt_expectations(basis, r64.vecs)
+    return [{"E_fp64": float(r64.eig[i]), "dE": float(eig_mixed[i] - r64.eig[i]), "JJ_fp64": float(j6[i]),
+             "dJJ": float(jm[i] - j6[i]), "twoJ": cg.jj_spin(j6[i], twom), "resid_fp64": float(r64.resid[i])}
+            for i in range(len(r64.eig))]
+
+
 def run_ours(args):
     import torch
     import cosmo_gb300 as cg
@@ -275,7 +290,7 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - s0)
         h2d = int(p2.info.n_one_body) * 16 + int(p2.info.n_two_body) * 24
         d2h = r2.vecs.nbytes + 3 * 8 * NSTATES
-        mixed_vecs = r2.vecs
+        mixed_vecs, mixed_eig = r2.vecs, r2.eig
         del h2, b2, p2
     e2e = statistics.median(e2e_times)
 
@@ -299,34 +314,46 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / spmm_s / 1e9
 
-    # plain FP64 GPU Davidson (the reference algorithm) on an FP64 matrix
+    # FP64 GPU Davidson on an FP64 matrix: (1) the same solver in FP64 to the
+    # same tolerance (the precision-only baseline), (2) the reference control
+    # flow (block 10, limit 30, one-vector Gram-Schmidt) to its iteration cap
     fp64 = None
     if not args.skip_fp64:
         H64 = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP64)
         torch.cuda.synchronize()
         s0 = time.perf_counter()
         r64 = cg.davidson_diagonalization(H64, NSTATES, want_vectors=True, precision=cg.CG_PREC_FP64,
-                                          tol_resid=TOL, maxiter=args.fp64_maxiter)
+                                          tol_resid=TOL, **FP64_SAME)
         torch.cuda.synchronize()
-        fp64 = dict(seconds=time.perf_counter() - s0, iterations=int(r64.stats.iterations),
-                    converged=int(r64.stats.converged), spmm_seconds=r64.stats.spmm_seconds,
-                    max_abs_dE_vs_mixed=float(np.abs(r64.eig - last.eig).max()))
-        # per-state eigenvalue and <J-J+> error of the mixed solve against the FP64 one
-        # (states the FP64 reference algorithm converged)
-        jj_mixed, _ = cg.jt_expectations(basis, mixed_vecs)
-        jj64, _ = cg.jt_expectations(basis, r64.vecs)
-        ok = r64.resid <= TOL
-        fp64["per_state"] = [{"E_fp64": float(r64.eig[i]), "dE": float(last.eig[i] - r64.eig[i]),
-                              "JJ_fp64": float(jj64[i]), "dJJ": float(jj_mixed[i] - jj64[i]),
-                              "twoJ": cg.jj_spin(jj64[i], 0)} for i in range(NSTATES) if ok[i]]
-        fp64["max_abs_dJJ_vs_mixed"] = max((abs(x["dJJ"]) for x in fp64["per_state"]), default=None)
-        del H64, r64
+        t64 = time.perf_counter() - s0
+        fp64 = dict(workload="same matrix stored in FP64, same solver (block 8, limit 64, keep 32, residual-driven) "
+                             "with FP64 products, vectors and projections, to the same tolerance",
+                    seconds=t64, iterations=int(r64.stats.iterations), converged=int(r64.stats.converged),
+                    spmm_seconds=r64.stats.spmm_seconds, max_resid=float(r64.resid.max()),
+                    precision_only_speedup=t64 / per_solve,
+                    per_state=per_state_errors(cg, basis, mixed_eig, mixed_vecs, r64, 0))
+        fp64["max_abs_dE"] = max(abs(x["dE"]) for x in fp64["per_state"])
+        fp64["max_abs_dJJ"] = max(abs(x["dJJ"]) for x in fp64["per_state"])
+        del r64
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        r0 = cg.davidson_diagonalization(H64, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64,
+                                         tol_resid=TOL, maxiter=args.fp64_maxiter)
+        torch.cuda.synchronize()
+        t0r = time.perf_counter() - s0
+        fp64["reference_control_flow"] = dict(
+            seconds=t0r, iterations=int(r0.stats.iterations), converged=int(r0.stats.converged),
+            spmm_seconds=r0.stats.spmm_seconds, speedup=t0r / per_solve,
+            max_abs_dE_converged=float(np.abs(r0.eig - last.eig)[r0.resid <= TOL].max(initial=0.0)),
+            note="the reference algorithm (block 10, limit 30, one-vector Gram-Schmidt, critc stall test) in FP64; "
+                 "it stops at its iteration cap with the converged count shown")
+        del H64, r0
 
     # CPU baseline: the reference algorithm restated in C (oracle), FP64 CSB, on
     # this host's cores, bounded sample scaled to a full solve
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline_from_gpu_matrix(H, fp64["iterations"] if fp64 else None, args.cpu_budget)
+        cpu = cpu_baseline_from_gpu_matrix(H, fp64["reference_control_flow"]["iterations"] if fp64 else None)
 
     hinfo = {"n": int(H.n), "nnz_full": int(H.info.nnz_full), "nnz_upper": int(H.info.nnz_upper),
              "build_seconds": H.info.build_seconds, "device_bytes": int(H.info.device_bytes)}
@@ -337,7 +364,7 @@ def run_ours(args):
     if rank == 0 and not args.skip_virtual:
         del H
         torch.cuda.empty_cache()
-        virtual = virtual_subbench(cg, fp64["iterations"] if fp64 else None)
+        virtual = virtual_subbench(cg, fp64["reference_control_flow"]["iterations"] if fp64 else None)
 
     if rank != 0:
         if dist:
@@ -377,6 +404,7 @@ def run_ours(args):
     }
     if fp64:
         line["speedup_vs_fp64_gpu"] = fp64["seconds"] / per_solve
+        line["speedup_vs_fp64_gpu_reference_control_flow"] = fp64["reference_control_flow"]["seconds"] / per_solve
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -466,14 +494,27 @@ def virtual_subbench(cg, fp64_iters):
     kw = dict(precision=cg.CG_PREC_FP32, tol_resid=TOL, **MIXED)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    r = cg.davidson_diagonalization(hv, NSTATES, want_vectors=False, **kw)
+    r = cg.davidson_diagonalization(hv, NSTATES, want_vectors=True, **kw)
     torch.cuda.synchronize()
     mixed = time.perf_counter() - t0
-    # plain FP64 on-the-fly Davidson: a bounded sample of iterations
-    t0 = time.perf_counter()
-    r64 = cg.davidson_diagonalization(hv, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64, maxiter=4)
+    # the same solver in FP64 on the FP64 on-the-fly product, to the same tolerance
     torch.cuda.synchronize()
-    per_it = (time.perf_counter() - t0) / max(1, int(r64.stats.iterations))
+    t0 = time.perf_counter()
+    r64 = cg.davidson_diagonalization(hv, NSTATES, want_vectors=True, precision=cg.CG_PREC_FP64, tol_resid=TOL,
+                                      **FP64_SAME)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    states = per_state_errors(cg, basis, r.eig, r.vecs, r64, 0)
+    fp64_same = {"seconds": t64, "iterations": int(r64.stats.iterations), "converged": int(r64.stats.converged),
+                 "spmm_seconds": r64.stats.spmm_seconds, "max_resid": float(r64.resid.max()),
+                 "precision_only_speedup": t64 / mixed, "per_state": states,
+                 "max_abs_dE": max(abs(x["dE"]) for x in states), "max_abs_dJJ": max(abs(x["dJJ"]) for x in states)}
+    del r64
+    # the reference control flow in FP64 on the on-the-fly product: a bounded sample of iterations
+    t0 = time.perf_counter()
+    rr = cg.davidson_diagonalization(hv, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64, maxiter=4)
+    torch.cuda.synchronize()
+    per_it = (time.perf_counter() - t0) / max(1, int(rr.stats.iterations))
     its = fp64_iters or REF_ITERS_DEFAULT
     return {"workload": "fp-shell 5p+5n M=0, lowest 10 eigenpairs, resid<=1e-5, on-the-fly product",
             "n": int(n), "connections_per_product": conn, "table_bytes": int(hv.info.device_bytes),
@@ -485,62 +526,94 @@ def virtual_subbench(cg, fp64_iters):
             "mixed_solve_seconds": mixed, "mixed_iterations": int(r.stats.iterations),
             "mixed_refine_iterations": int(r.stats.refine_iterations), "mixed_converged": int(r.stats.converged),
             "mixed_max_resid": float(r.resid.max()), "eig": [round(float(x), 8) for x in r.eig],
-            "fp64_seconds_per_iteration": per_it,
-            "fp64_estimated_seconds": per_it * its,
-            "fp64_sample": f"{int(r64.stats.iterations)} iterations of the reference algorithm (block 10, lim 30) "
-                           f"in FP64 on the on-the-fly product, scaled to {its} iterations",
-            "speedup_vs_fp64_estimate": per_it * its / mixed}
+            "fp64_same_solver": fp64_same,
+            "fp64_reference_control_flow": {
+                "seconds_per_iteration": per_it, "estimated_seconds": per_it * its,
+                "sample": f"{int(rr.stats.iterations)} iterations of the reference algorithm (block 10, lim 30) in "
+                          f"FP64 on the on-the-fly product, scaled to {its} iterations (its cap, reached without "
+                          f"convergence on fp 4+4)",
+                "speedup_estimate": per_it * its / mixed}}
 
 
-def cpu_baseline_from_gpu_matrix(H, ref_iters, budget):
+REF_ALGO = ("the reference control flow (DavidsonDiagonalization defaults: block 10, basis limit 30, "
+            "thresholds 1e-15/1e-12/1e-8) on an FP64 CSB pull-form product")
+
+
+def reference_davidson_sample(csb, warm: int, timed: int, cores: int, budget: float = 600.0):
+    """One continuous run of the reference Davidson (oracle restatement, all
+    host threads) for warm + timed iterations; the mean duration of the timed
+    iterations (after the first `warm`), with the counts actually run."""
+    r = csb.davidson(NSTATES, nthreads=cores, maxiter=warm + timed, time_budget=budget)
+    ends = np.asarray(r["iter_end"])
+    k = len(ends)
+    if k == 0:
+        raise RuntimeError("reference Davidson sample ran no iteration")
+    w = min(warm, k - 1)
+    dur = np.diff(np.concatenate([[0.0], ends]))[w:]
+    return float(dur.mean()), {"iterations_run": k, "timed_iterations": int(len(dur)), "warmup_iterations": w,
+                               "collapses": int(r["collapses"]), "sample_seconds": float(dur.sum())}
+
+
+def sample_text(per: float, info: dict, its: int, cores: int) -> str:
+    return (f"one continuous run of {REF_ALGO}, {cores} host threads: iterations {info['warmup_iterations'] + 1}.."
+            f"{info['iterations_run']} ({info['timed_iterations']} iterations, {info['collapses']} basis collapses "
+            f"in the run) measured at {per:.3f} s/iteration; value = that x {its}, the iteration cap at which this "
+            f"algorithm stops on this problem without converging all 10 pairs to resid<=1e-5 (GPU FP64 run of the "
+            f"same control flow), so a lower bound of its time to tolerance")
+
+
+def cpu_baseline_from_gpu_matrix(H, ref_iters, warm: int = 3, timed: int = 12):
+    """The bench line's cpu_baseline: the oracle's reference Davidson on the
+    GPU-built matrix (its upper triangle copied to the host)."""
     from oracle import oracle as O
     rp, c, v = H.upper_rows()
     csb = O.CSB(rp, c, v)
     del rp, c, v
     cores = os.cpu_count() or 1
-    r = csb.davidson(NSTATES, critr=TOL, nthreads=cores, time_budget=budget)
+    per, info = reference_davidson_sample(csb, warm, timed, cores)
     its = ref_iters if ref_iters else REF_ITERS_DEFAULT
-    per = r["seconds_per_iteration"]
-    return {"value": per * its if its else None, "unit": "s", "cores": cores, "kind": "port",
-            "sample": f"{r['iterations']} Davidson iterations (block 10, lim 30, FP64 CSB pull-form SpMM) "
-                      f"at {per:.3f} s/iteration, scaled to the {its} iterations the same algorithm takes to "
-                      f"resid<=1e-5 on the GPU FP64 run",
-            "seconds_per_iteration": per}
+    return {"value": per * its, "unit": "s", "cores": cores, "kind": "port", "sample": sample_text(per, info, its, cores),
+            "seconds_per_iteration": per, **info}
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores, with nothing from the
+    product library: the oracle's own XML/interaction restatement, the oracle
+    basis and row builder (C, OpenMP), the reference-layout CSB and the
+    reference Davidson.  Each step is one Davidson iteration of one continuous
+    run (warm-up iterations untimed)."""
     rank, world, local = env_rank()
     if rank != 0:
         return
-    import cosmo_gb300.synthetic as syn  # noqa: F401 (input generation only)
+    from oracle import interaction as OI
     from oracle import oracle as O
-    import cosmo_gb300 as cg
     tmp = tempfile.mkdtemp(prefix="cg_ref_")
-    xml = make_inputs(tmp)
-    prob = cg.Problem(xml)  # host-side XML/interaction parsing only (no GPU)
-    inf = prob.info
+    xml = make_inputs(tmp, args.config)
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    z = O.basis(prob.sps(), inf.nv + inf.zv, inf.twom, inf.nv - inf.zv, inf.parity)
-    k1, v1 = prob.one_body()
-    k2, v2 = prob.two_body()
-    rp, c, v = O.build_upper(inf.n_sps, k1, v1, k2, v2, z, nthreads=cores)
+    sysd, k1, v1, k2, v2 = OI.operator_terms(xml)
+    t1 = time.perf_counter()
+    z = O.basis(sysd.sps, sysd.nv + sysd.zv, sysd.twom, sysd.nv - sysd.zv, sysd.parity)
+    t2 = time.perf_counter()
+    rp, c, v = O.build_upper(len(sysd.sps), k1, v1, k2, v2, z, nthreads=cores)
     csb = O.CSB(rp, c, v)
-    setup = time.perf_counter() - t0
-    per = []
-    for i in range(args.warmup + args.steps):
-        r = csb.davidson(NSTATES, critr=TOL, nthreads=cores, time_budget=args.cpu_budget / max(1, args.steps))
-        if i >= args.warmup:
-            per.append(r["seconds_per_iteration"])
+    t3 = time.perf_counter()
+    nnz = int(rp[-1])
+    del rp, c, v, z
+    per, info = reference_davidson_sample(csb, args.warmup, args.steps, cores)
     its = args.ref_iters
-    value = statistics.median(per) * its
+    value = per * its
+    loaded = sorted({ln.split()[-1] for ln in open("/proc/self/maps") if ln.rstrip().endswith(".so")
+                     and HERE in ln})
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "config": WORKLOAD,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": False,
+            "config": WORKLOAD,
             "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port",
-                             "sample": f"Davidson iterations (block 10, lim 30) of the C restatement of the "
-                                       f"reference on {cores} host threads, median s/iteration x {its} iterations"},
+                             "sample": sample_text(per, info, its, cores)},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "setup_seconds": setup, "seconds_per_iteration": statistics.median(per)}
+            "seconds_per_iteration": per, **info,
+            "setup_seconds": {"interaction": t1 - t0, "basis": t2 - t1, "csb_build": t3 - t2},
+            "nnz_upper": nnz, "repo_libraries_loaded": [os.path.relpath(x, HERE) for x in loaded]}
     print(json.dumps(line))
 
 
@@ -553,7 +626,6 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--fp64-maxiter", type=int, default=400)
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-virtual", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)

@@ -73,7 +73,7 @@ def lib() -> C.CDLL:
         L.oracle_davidson.restype = C.c_int
         L.oracle_davidson.argtypes = [_P, _P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.c_double, _P, _P, _P, _P, _P, _P, C.c_int,
-                                      C.c_double, _P, _P]
+                                      C.c_double, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -189,18 +189,22 @@ class CSB:
     def davidson(self, nume: int = 10, block: int | None = None, lim: int | None = None, maxiter: int = 0,
                  crite=1e-15, critc=1e-12, critr=1e-8, ortho=1e-9, nthreads: int = 0, time_budget: float = 0.0,
                  want_vectors: bool = False):
+        """dvdrvr2 restated.  Besides the eigenpairs, returns the end time of
+        every iteration (iter_end, seconds from the start of the first) and the
+        number of basis collapses."""
         block = block or nume
         lim = lim or nume + 20
         maxiter = maxiter or max(40 * nume, 200)
         d = self.diagonal()
         eig = np.zeros(nume); de = np.zeros(nume); res = np.zeros(nume)
         vecs = np.zeros((nume, self.n)) if want_vectors else None
-        it = C.c_int(0); nmv = C.c_int64(0); per = C.c_double(0); t0 = C.c_double(0)
+        ends = np.zeros(maxiter)
+        it = C.c_int(0); nmv = C.c_int64(0); per = C.c_double(0); t0 = C.c_double(0); ncol = C.c_int(0)
         ierr = lib().oracle_davidson(self._h, _p(d), self.n, nume, block, lim, maxiter, crite, critc, critr, ortho,
                                      _p(eig), _p(de), _p(res), _p(vecs), C.byref(it), C.byref(nmv), nthreads,
-                                     time_budget, C.byref(per), C.byref(t0))
+                                     time_budget, C.byref(per), C.byref(t0), _p(ends), C.byref(ncol))
         return dict(eig=eig, de=de, resid=res, vecs=vecs, iterations=it.value, matvecs=nmv.value, ierr=ierr,
-                    seconds_per_iteration=per.value)
+                    seconds_per_iteration=per.value, iter_end=ends[:it.value].copy(), collapses=ncol.value)
 
 
 def full_from_upper(rp, cols, vals):

@@ -192,11 +192,14 @@ static int ortho_seq(vecs_t* V, int basis_dim, int* nncv, double ortho) {
 
 /* Returns ierr (reference codes); fills eig/de/resid (nume) and vectors
  * (nume x n, may be NULL).  time_budget > 0 stops after that many seconds
- * (ierr 4096 marks a budget stop); *iters and *per_iter report the work done. */
+ * (ierr 4096 marks a budget stop); *iters and *per_iter report the work done.
+ * iter_end (maxiter entries, may be NULL) receives the wall time of the end of
+ * every iteration, from the start of the first one; *collapses (may be NULL)
+ * the number of basis collapses (restarts at the basis limit). */
 int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int nume, int mblock, int lim, int maxiter,
                     double crite, double critc, double critr, double ortho, double* eig, double* de, double* resid,
                     double* vout, int* iters, int64_t* matvecs, int nthreads, double time_budget, double* per_iter,
-                    double* first_iter_start) {
+                    double* first_iter_start, double* iter_end, int* collapses) {
   if (nthreads > 0) omp_set_num_threads(nthreads);
   vecs_t V = {n, lim, nume, (double**)malloc(sizeof(double*) * lim), (double**)malloc(sizeof(double*) * lim)};
   for (int k = 0; k < lim; ++k) {
@@ -226,6 +229,7 @@ int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int num
     free(used);
   }
   int kpass = nume, nncv = kpass, nloops = 0, ierr = 0, done = 0, first = 1, hit_cap = 1;
+  if (collapses) *collapses = 0;
   add_ab_s(M, &V, 0, kpass, S, nthreads, &nmv);
   double t_start = wall();
   if (first_iter_start) *first_iter_start = t_start;
@@ -322,6 +326,7 @@ int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int num
     if (!restart) first = 1;
     else if (first) {
       first = 0;
+      if (collapses) ++*collapses;
       combine(n, V.b, kpass, zv, kz, nume);
       combine(n, V.ab, kpass, zv, kz, nume);
       memset(S, 0, sizeof(double) * lim * lim);
@@ -335,6 +340,7 @@ int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int num
     if (done || nncv == 0) { hit_cap = 0; break; }
     add_ab_s(M, &V, kpass, nncv, S, nthreads, &nmv);
     kpass += nncv;
+    if (iter_end) iter_end[nloops] = wall() - t_start;
     ++nloops;
     if (time_budget > 0 && wall() - t_start > time_budget) { ierr += 4096; break; }
   } while (nloops < maxiter);

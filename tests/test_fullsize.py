@@ -3,9 +3,12 @@ through size-independent properties, since the oracle cannot run them in
 seconds: basis sizes, the block-tiled product against the row-wise product,
 symmetry (x . H y = y . H x, dots accumulated in FP64) and linearity of the
 stored and on-the-fly products, the on-the-fly product against the stored
-one, and the mixed solve's residuals under the FP64 product.  Tolerances: 2e-6 of max|y| between the two FP32 stored kernels (same
-values, different summation order), 1e-5 for FP32 products against each other
-or in linear combinations, 1e-6 relative for the FP32 symmetry defect."""
+one, the mixed solve's residuals under the FP64 product, and the mixed
+solve's 10 eigenpairs against the same solver run entirely in FP64.
+Tolerances: 2e-6 of max|y| between the two FP32 stored kernels (same values,
+different summation order), 1e-5 for FP32 products against each other or in
+linear combinations, 1e-6 relative for the FP32 symmetry defect, 1e-4 MeV per
+eigenvalue and 1e-6 per <J-J+> between the mixed and the FP64 solves."""
 import numpy as np
 import pytest
 
@@ -97,3 +100,42 @@ def test_fp44_mixed_solve_true_residuals(gpu_available, tmp_path):
     res = np.linalg.norm(hv.times_matrix(V, cg.CG_PREC_FP64) - V * r.eig, axis=0)
     assert np.all(res <= 1e-5), res
     np.testing.assert_allclose(res, r.resid, rtol=1e-3, atol=1e-8)
+
+
+MIXED = dict(precision=cg.CG_PREC_FP32, tol_resid=1e-5, block=8, lim=64, keep=32, algorithm=1, precond=1,
+             switch_resid=3e-5, refine_lim=32, refine_keep=16)
+FP64_SAME = dict(precision=cg.CG_PREC_FP64, tol_resid=1e-5, block=8, lim=64, keep=32, algorithm=1, precond=1)
+
+
+def _compare_states(b, rm, r64):
+    """Mixed vs FP64 solve, state by state in energy order: eigenvalues within
+    1e-4 MeV and <J-J+> within 1e-6 (a missed or swapped state fails)."""
+    assert rm.stats.converged == 10 and r64.stats.converged == 10, (rm.resid, r64.resid)
+    np.testing.assert_allclose(rm.eig, r64.eig, rtol=0, atol=1e-4)
+    jm, _ = cg.jt_expectations(b, rm.vecs)
+    j6, _ = cg.jt_expectations(b, r64.vecs)
+    np.testing.assert_allclose(jm, j6, rtol=0, atol=1e-6)
+
+
+def test_fp44_mixed_matches_fp64_solve(gpu_available, tmp_path):
+    """The headline workload: the 10 lowest eigenpairs of the mixed solve (FP32
+    stored H and vectors) against the same solver run entirely in FP64 (FP64
+    stored H) to the same tolerance."""
+    p, b = _system(tmp_path, "fp", 4, 4, 7)
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    rm = cg.davidson_diagonalization(h, 10, want_vectors=True, **MIXED)
+    del h
+    h64 = cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
+    r64 = cg.davidson_diagonalization(h64, 10, want_vectors=True, **FP64_SAME)
+    _compare_states(b, rm, r64)
+
+
+def test_fp55_mixed_matches_fp64_on_the_fly_solve(gpu_available, tmp_path):
+    """fp 5+5 (n = 18,600,516, H never stored): the mixed solve on the FP32
+    on-the-fly product against the same solver on the FP64 on-the-fly product
+    (about two minutes of FP64 products)."""
+    p, b = _system(tmp_path, "fp", 5, 5, 8)
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
+    rm = cg.davidson_diagonalization(hv, 10, want_vectors=True, **MIXED)
+    r64 = cg.davidson_diagonalization(hv, 10, want_vectors=True, **FP64_SAME)
+    _compare_states(b, rm, r64)

@@ -60,6 +60,55 @@ def test_host_operator_usdb_matches_reference(tmp_path):
     assert np.array_equal(k1, g["esp_keys"]) and np.array_equal(v1, g["esp_vals"])
 
 
+@pytest.mark.parametrize("name", SMALL)
+def test_oracle_interaction_matches_reference(name, tmp_path):
+    """The oracle's own XML/Oxbash/AddPPVsp/J-J+ restatement (no product
+    library) against the reference's operator terms: keys identical, values
+    within 1e-13."""
+    from oracle import interaction as OI
+    g = golden(name)
+    sysd, k1, v1, k2, v2 = OI.operator_terms(synthetic_xml(name, str(tmp_path)))
+    assert np.array_equal(sysd.sps, g["sps"])
+    assert np.array_equal(k1, g["esp_keys"]) and np.array_equal(k2, g["vspx_keys"])
+    np.testing.assert_allclose(v1, g["esp_vals"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(v2, g["vspx_vals"], rtol=0, atol=1e-13)
+
+
+def test_oracle_interaction_usdb_matches_reference(tmp_path):
+    """usdb with its mass scaling through the oracle's restatement (needs the
+    reference interaction file; skipped without the reference checkout)."""
+    from oracle import interaction as OI
+    from cosmo_gb300.synthetic import SyntheticSystem, write_xml
+    root = O.reference_root()
+    usdb = os.path.join(root, "interactions", "sd", "usdb.int") if root else ""
+    if not os.path.exists(usdb):
+        pytest.skip("reference checkout not given (COSMO_REFERENCE)")
+    orbits = [("0d3", 0, 2, 3), ("0d5", 0, 2, 5), ("1s1", 1, 0, 1)]
+    xml = str(tmp_path / "mg24.xml")
+    write_xml(xml, SyntheticSystem("sd", 4, 4, 0, "+", 0.0, 0, name="mg24usdb"), usdb, orbits, hname="usdb")
+    txt = open(xml).read().replace('<matrix JJ="0.0"/>', "")
+    open(xml, "w").write(txt)
+    g = golden("mg24usdb")
+    sysd, k1, v1, k2, v2 = OI.operator_terms(xml)
+    assert np.array_equal(k1, g["esp_keys"]) and np.array_equal(k2, g["vspx_keys"])
+    np.testing.assert_allclose(v1, g["esp_vals"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(v2, g["vspx_vals"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["sd32m1s2", "fp21m3s6", "fp22m0s3"])
+def test_oracle_only_pipeline_matches_reference(name, tmp_path):
+    """The CPU baseline's pipeline, with nothing from the product library:
+    oracle interaction -> oracle basis -> oracle rows reproduce the reference's
+    basis and connectivity hashes."""
+    from oracle import interaction as OI
+    m = manifest()[name]
+    sysd, k1, v1, k2, v2 = OI.operator_terms(synthetic_xml(name, str(tmp_path)))
+    z = O.basis(sysd.sps, sysd.nv + sysd.zv, sysd.twom, sysd.nv - sysd.zv, sysd.parity)
+    assert mbs_sha(z) == m["mbs_sha256"]
+    rp, c, v = O.build_upper(len(sysd.sps), k1, v1, k2, v2, z)
+    assert int(rp[-1]) == m["nnz_upper"] and conn_hash(rp, c) == m["conn_sha256"]
+
+
 @pytest.mark.parametrize("name", SMALL + MEDIUM + ["sd66m0s5", "fp44m0s7"])
 def test_oracle_basis_matches_reference(name, tmp_path):
     m = manifest()[name]
