@@ -180,7 +180,8 @@ def run_spmm_only(args):
         spmm_s, alg = spmm_roofline(cg, H, args.nvec, reps=args.steps, warm=args.warmup, fp64=True)
     peak, kind = measured_peaks()
     print(json.dumps({"mode": "spmm", "config": args.config, "precision": args.precision, "nvec": args.nvec,
-                      "n": H.n, "nnz_full": int(H.info.nnz_full), "launch_ms": spmm_s * 1e3, "alg_bytes": alg,
+                      "n": H.n, "nnz_full": int(H.info.nnz_full), "build_seconds": H.info.build_seconds,
+                      "launch_ms": spmm_s * 1e3, "alg_bytes": alg,
                       "achieved_gbs": alg / spmm_s / 1e9, "peak_gbs": peak, "frac": alg / spmm_s / 1e9 / peak,
                       "tuning": tune}))
 
@@ -359,8 +360,11 @@ def run_ours(args):
              "build_seconds": H.info.build_seconds, "device_bytes": int(H.info.device_bytes)}
     batched = None
     virtual = None
+    sd66 = None
     if rank == 0 and not args.skip_batched:
         batched = batched_subbench(cg)
+    if rank == 0 and not args.skip_sd66:
+        sd66 = sd66_subbench(cg)
     if rank == 0 and not args.skip_virtual:
         del H
         torch.cuda.empty_cache()
@@ -400,6 +404,7 @@ def run_ours(args):
         "fp64_gpu_davidson": fp64,
         "cpu_baseline": cpu,
         "batched_sd64": batched,
+        "sd66_fp64_block4": sd66,
         "virtual_fp55": virtual,
     }
     if fp64:
@@ -447,10 +452,88 @@ def batched_subbench(cg):
             "build_seconds": build, "solve_seconds": min(times), "build_plus_solve_seconds": build + min(times),
             "iterations_fp32": int(st.iterations_fp32), "iterations_fp64": int(st.iterations_fp64),
             "graph_launches": int(st.graph_launches), "kernels_per_graph": int(st.graph_kernels),
+            "spmm_autotuned_shape": {"warps_per_cta": int(st.spmm_warps), "ctas_per_sm": int(st.spmm_ctas_per_sm),
+                                     "tune_seconds": float(st.spmm_tune_seconds)},
             "launches": int(st.launches), "states_converged": int(nconv.sum()), "states_wanted": wanted,
             "max_resid": float(np.nanmax(res)),
             "sequential_build_plus_solve_seconds": seq,
             "speedup_vs_sequential": seq / (build + min(times))}
+
+
+def sd66_subbench(cg):
+    """sd-shell 6p+6n M=0 (n = 93,710): plain FP64 stored H and block Davidson
+    for the 10 lowest eigenpairs with block 4 and basis limit 40, as the
+    reference control flow on the GPU, as the residual-driven solver in FP64,
+    and the mixed solve; the same reference control flow on the host cores
+    (oracle restatement, all threads) run to its own stop, not sampled."""
+    import torch
+    from oracle import oracle as O
+    tmp = tempfile.mkdtemp(prefix="cg_sd66_")
+    xml = make_inputs(tmp, "sd66")
+    prob = cg.Problem(xml)
+    basis = cg.ManyBodyStates(prob)
+    out = {"workload": "sd-shell 6p+6n M=0, FP64 CSB, lowest 10 eigenpairs, block 4, basis limit 40",
+           "n": int(basis.n)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h64 = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP64)
+    torch.cuda.synchronize()
+    out["gpu_build_seconds"] = time.perf_counter() - t0
+    runs = {}
+    for name, kw in (("fp64_reference_control_flow", dict(algorithm=0)),
+                     ("fp64_residual_driven", dict(algorithm=1, keep=20, precond=1))):
+        cg.davidson_diagonalization(h64, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64, tol_resid=TOL,
+                                    block=4, lim=40, **kw)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = cg.davidson_diagonalization(h64, NSTATES, want_vectors=False, precision=cg.CG_PREC_FP64, tol_resid=TOL,
+                                        block=4, lim=40, **kw)
+        torch.cuda.synchronize()
+        runs[name] = r
+        out[name] = {"seconds": time.perf_counter() - t0, "iterations": int(r.stats.iterations),
+                     "converged": int(r.stats.converged), "max_resid": float(r.resid.max())}
+    h32 = cg.Hamiltonian(prob, basis, cg.CG_PREC_FP32)
+    kw = dict(precision=cg.CG_PREC_FP32, tol_resid=TOL, **MIXED)
+    cg.davidson_diagonalization(h32, NSTATES, want_vectors=False, **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rm = cg.davidson_diagonalization(h32, NSTATES, want_vectors=False, **kw)
+    torch.cuda.synchronize()
+    ref = runs["fp64_residual_driven"]
+    out["mixed"] = {"seconds": time.perf_counter() - t0, "iterations": int(rm.stats.iterations),
+                    "converged": int(rm.stats.converged), "max_abs_dE_vs_fp64": float(np.abs(rm.eig - ref.eig).max())}
+
+    def nearest(eig, resid):
+        """converged pairs matched to the nearest FP64 eigenvalue (a control
+        flow that stalls a state can converge a higher one in its place), and
+        how many of the 10 lowest FP64 states no converged pair matches"""
+        ok = np.asarray(resid) <= TOL
+        e = np.asarray(eig)[ok]
+        if not len(e):
+            return 0.0, NSTATES
+        d = np.abs(e[:, None] - ref.eig[None, :])
+        return float(d.min(axis=1).max()), int(NSTATES - len(set(d.argmin(axis=1).tolist())))
+    r0 = runs["fp64_reference_control_flow"]
+    dmax, miss = nearest(r0.eig, r0.resid)
+    out["fp64_reference_control_flow"].update(max_abs_dE_converged_vs_nearest_fp64=dmax,
+                                              lowest_states_not_found=miss)
+    out["eig"] = [round(float(x), 8) for x in ref.eig]
+    # the reference control flow on the host cores, run to its own stop
+    rp, c, v = h64.upper_rows()
+    csb = O.CSB(rp, c, v)
+    del rp, c, v
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    rc = csb.davidson(NSTATES, block=4, lim=40, critr=TOL, nthreads=cores)
+    cpu_s = time.perf_counter() - t0
+    dmax, miss = nearest(rc["eig"], rc["resid"])
+    out["cpu_reference_control_flow"] = {
+        "seconds": cpu_s, "iterations": int(rc["iterations"]), "converged": int((rc["resid"] <= TOL).sum()),
+        "cores": cores, "kind": "port", "max_abs_dE_converged_vs_nearest_fp64": dmax,
+        "lowest_states_not_found": miss}
+    out["speedup_gpu_reference_control_flow_vs_cpu"] = cpu_s / out["fp64_reference_control_flow"]["seconds"]
+    out["speedup_mixed_vs_cpu"] = cpu_s / out["mixed"]["seconds"]
+    return out
 
 
 def virtual_subbench(cg, fp64_iters):
@@ -628,6 +711,7 @@ def main():
     ap.add_argument("--fp64-maxiter", type=int, default=400)
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-virtual", action="store_true")
+    ap.add_argument("--skip-sd66", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
     ap.add_argument("--mode", default="solve", choices=["solve", "spmm"])
     ap.add_argument("--config", default="fp44", choices=sorted(CONFIGS))

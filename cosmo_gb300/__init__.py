@@ -85,7 +85,8 @@ class BatchParams(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("iterations_fp32", C.c_int32), ("iterations_fp64", C.c_int32), ("graph_launches", C.c_uint64),
                 ("graph_kernels", C.c_int32), ("launches", C.c_uint64), ("seconds", C.c_double),
-                ("build_seconds", C.c_double)]
+                ("build_seconds", C.c_double), ("spmm_warps", C.c_int32), ("spmm_ctas_per_sm", C.c_int32),
+                ("spmm_tune_seconds", C.c_double)]
 
 
 class DavidsonStats(C.Structure):

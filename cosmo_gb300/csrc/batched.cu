@@ -967,6 +967,19 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
   }
   CG_CUDA(cudaGetLastError());
   CG_CUDA(cudaStreamSynchronize(s));
+  // launch shape of the block-diagonal product (warps per CTA x resident CTAs
+  // per SM), timed on this matrix with the solve's 8-vector rows; the iteration
+  // graphs capture the chosen shape
+  if (H.n > 0) {
+    const auto ta = std::chrono::steady_clock::now();
+    struct StreamLoan {  // H destroys its own stream; the batch's is only lent
+      Hamiltonian& h;
+      ~StreamLoan() { h.stream = nullptr; }
+    } loan{H};
+    H.stream = s;
+    spmm_autotune(H, kMaxB, 3);
+    bs.tune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
+  }
   bs.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 

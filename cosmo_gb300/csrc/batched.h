@@ -31,6 +31,7 @@ struct BatchSet {
   DBuf<double> dense;             // nd x 64 x 64 FP64 matrices of the small problems
   std::vector<int> ddim;
   double build_seconds = 0;
+  double tune_seconds = 0;        // launch-shape autotuning of H inside build_seconds
   cudaStream_t stream = nullptr;
   ~BatchSet();
 };

@@ -538,6 +538,9 @@ cg_status cg_batch_solve(cg_batch* b, const cg_batch_params* prm, double* eig, d
       stats->launches = r.launches;
       stats->seconds = r.seconds;
       stats->build_seconds = b->bs.build_seconds;
+      stats->spmm_warps = b->bs.H.tuning.warps;
+      stats->spmm_ctas_per_sm = b->bs.H.tuning.ctas_per_sm;
+      stats->spmm_tune_seconds = b->bs.tune_seconds;
     }
   });
 }

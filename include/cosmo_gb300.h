@@ -350,6 +350,9 @@ typedef struct {
   int32_t graph_kernels;     /* kernels in the largest iteration graph */
   uint64_t launches;         /* kernel launches of the solve, graph replays included */
   double seconds, build_seconds;
+  int32_t spmm_warps;        /* launch shape the autotuner chose for the block-diagonal product at */
+  int32_t spmm_ctas_per_sm;  /* cg_batch_create (warps per CTA, resident CTAs per SM) */
+  double spmm_tune_seconds;  /* time the autotuner took (inside build_seconds) */
 } cg_batch_stats;
 cg_status cg_batch_create(const cg_problem* const* problems, int32_t count, cg_batch** out);
 void cg_batch_destroy(cg_batch* b);

@@ -270,6 +270,7 @@ int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int num
     }
     if (done || (uint64_t)kpass >= n) { hit_cap = 0; break; }
     if (kpass == lim) {
+      if (collapses) ++*collapses;
       combine(n, V.b, lim, zv, kz, nume);
       combine(n, V.ab, lim, zv, kz, nume);
       memset(S, 0, sizeof(double) * lim * lim);
@@ -326,7 +327,6 @@ int oracle_davidson(const oracle_csb* M, const double* diag, uint64_t n, int num
     if (!restart) first = 1;
     else if (first) {
       first = 0;
-      if (collapses) ++*collapses;
       combine(n, V.b, kpass, zv, kz, nume);
       combine(n, V.ab, kpass, zv, kz, nume);
       memset(S, 0, sizeof(double) * lim * lim);

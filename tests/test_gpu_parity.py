@@ -345,3 +345,22 @@ def test_davidson_mixed_iteration_cap_residuals(gpu_available, tmp_path):
     res = np.linalg.norm(h64.times_matrix(V) - V * r.eig, axis=0)
     np.testing.assert_allclose(res, r.resid, rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(V.T @ V, np.eye(nst), rtol=0, atol=1e-8)
+
+
+def test_sd66_fp64_block4_lim40(gpu_available, tmp_path):
+    """sd 6+6 (n = 93,710) as the FP64 stored-H workload with block 4 and basis
+    limit 40: the residual-driven solver in FP64 converges all 10 pairs to the
+    exact spectrum (1e-6 MeV), and the reference control flow's converged
+    pairs are exact eigenpairs too (it may stall some, like the reference)."""
+    nst = 10
+    exact = _exact("sd66m0s5", str(tmp_path), nst)
+    _, _, h = _gpu("sd66m0s5", str(tmp_path))
+    r1 = cg.davidson_diagonalization(h, nst, want_vectors=False, precision=cg.CG_PREC_FP64, tol_resid=1e-5,
+                                     block=4, lim=40, algorithm=1, keep=20, precond=1)
+    assert r1.stats.converged == nst, (r1.resid, r1.stats.ierr)
+    np.testing.assert_allclose(r1.eig, exact, rtol=0, atol=1e-6)
+    r0 = cg.davidson_diagonalization(h, nst, want_vectors=False, precision=cg.CG_PREC_FP64, tol_resid=1e-5,
+                                     block=4, lim=40, algorithm=0)
+    ok = r0.resid <= 1e-5
+    assert ok.sum() >= nst // 2, r0.resid
+    assert np.all(np.min(np.abs(r0.eig[ok][:, None] - exact[None, :]), axis=1) < 1e-6)
