@@ -120,18 +120,81 @@ __global__ void k_tfill(uint64_t n, const uint64_t* __restrict__ rowptr, const u
   }
 }
 
-// Reorder each row's entries inside its run so that, step by step, the 32
-// lanes' row reads of x spread over the shared-memory bank groups: lane l at
-// step j reads its first 16 bytes from group (2 col + (l & 1)) mod 8, and a
-// step costs as many wavefronts as its most used group.  Lane l aims at step j
-// for group 2 ((l / 2 + j) mod 4) + (l & 1), which puts four lanes on every
-// group, and takes the first entry of its next 8 with that group (else a
-// padding entry, which issues no read, else the next entry).  One warp per
-// run, each lane reordering its own entries; only a row's summation order
-// changes.
+// Bank-group balancing of the staged-x row reads.  A row read is two 16-byte
+// loads, lane l taking half (l & 1) first; the half of x row c read first sits
+// in bank group 2 (c mod 4) + (l & 1), the second one in its partner group.
+// When in every quarter warp (8 lanes) of a step the four even lanes read four
+// different column classes (c mod 4) and so do the four odd lanes, both loads
+// touch 8 distinct groups per quarter: no extra wavefront.  The entries of a
+// row may be taken in any order (only its summation order changes) and a row
+// shorter than its run may place its padding at any step, so the classes are
+// matched greedily step by step: one thread per (run, quarter); lanes with the
+// least slack choose first, each taking its first entry whose class is still
+// free among the lanes of its parity, else padding when it has slack, else its
+// next entry.
 __global__ void k_tbalance(uint64_t nruns, const uint32_t* __restrict__ roff, uint16_t* __restrict__ col,
                            float* __restrict__ val) {
-  const int lane = threadIdx.x & 31, p = lane & 1;
+  const uint64_t t0 = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  const uint64_t nt = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t t = t0; t < nruns * 4; t += nt) {
+    const uint64_t r = t >> 2;
+    const int lq = int(t & 3) * 8;  // first lane of this quarter
+    const uint64_t g0 = roff[r];
+    const uint32_t w = roff[r + 1] - roff[r];
+    if (w < 2) continue;
+    uint32_t rem[8];
+    for (int i = 0; i < 8; ++i) {
+      rem[i] = 0;
+      for (uint32_t q = 0; q < w; ++q) rem[i] += val[(g0 + q) * 32 + lq + i] != 0.f;
+    }
+    for (uint32_t j = 0; j < w; ++j) {
+      uint32_t used = 0;  // bit (4 parity + class): taken in this step
+      uint32_t done = 0;
+      for (int pick = 0; pick < 8; ++pick) {
+        int i = -1;
+        uint32_t bslack = 0;
+        for (int c = 0; c < 8; ++c) {
+          if ((done >> c) & 1u) continue;
+          const uint32_t slack = (w - j) - rem[c];
+          if (i < 0 || slack < bslack) { i = c; bslack = slack; }
+        }
+        done |= 1u << i;
+        if (rem[i] == 0) continue;  // only padding left in this row
+        const uint32_t par = uint32_t(i & 1) * 4;
+        const uint64_t ej = (g0 + j) * 32 + lq + i;
+        uint32_t take = w;
+        for (uint32_t q = j; q < w && take == w; ++q) {
+          const uint64_t e = (g0 + q) * 32 + lq + i;
+          if (val[e] != 0.f && !((used >> (par + (col[e] & 3u))) & 1u)) take = q;
+        }
+        if (take == w && bslack > 0)  // pad now: bring a padding entry to step j
+          for (uint32_t q = j; q < w && take == w; ++q)
+            if (val[(g0 + q) * 32 + lq + i] == 0.f) take = q;
+        if (take == w)
+          for (uint32_t q = j; q < w && take == w; ++q)
+            if (val[(g0 + q) * 32 + lq + i] != 0.f) take = q;
+        if (take != j) {
+          const uint64_t eb = (g0 + take) * 32 + lq + i;
+          const uint16_t tc = col[ej]; col[ej] = col[eb]; col[eb] = tc;
+          const float tv = val[ej]; val[ej] = val[eb]; val[eb] = tv;
+        }
+        if (val[ej] != 0.f) {
+          used |= 1u << (par + (col[ej] & 3u));
+          --rem[i];
+        }
+      }
+    }
+  }
+}
+
+// Padding entries (value 0) still issue the row read: each points at the
+// column of a real lane of the same parity and step (the same addresses in
+// both loads: no extra access), in its own quarter warp when one has a real
+// entry, else anywhere in the warp.  One warp per run.
+__global__ void k_tpadaddr(uint64_t nruns, const uint32_t* __restrict__ roff, uint16_t* __restrict__ col,
+                           const float* __restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t pmask = (lane & 1) ? 0xaaaaaaaau : 0x55555555u;
   const uint64_t w0 = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
   const uint64_t nw = (uint64_t(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t r = w0; r < nruns; r += nw) {
@@ -139,32 +202,13 @@ __global__ void k_tbalance(uint64_t nruns, const uint32_t* __restrict__ roff, ui
     const uint32_t w = roff[r + 1] - roff[r];
     for (uint32_t j = 0; j < w; ++j) {
       const uint64_t ej = (g0 + j) * 32 + lane;
-      if (j + 1 < w) {
-        const uint32_t target = 2 * (((lane >> 1) + j) & 3) + p;
-        const uint32_t jw = min(w, j + 8);
-        uint32_t hit = jw, pad = jw;
-        for (uint32_t q = j; q < jw && hit == jw; ++q) {
-          const uint64_t e = (g0 + q) * 32 + lane;
-          if (val[e] == 0.f) {
-            if (pad == jw) pad = q;
-          } else if (((2u * col[e] + p) & 7u) == target) {
-            hit = q;
-          }
-        }
-        const uint32_t best = hit < jw ? hit : (pad < jw ? pad : j);
-        if (best != j) {
-          const uint64_t eb = (g0 + best) * 32 + lane;
-          const uint16_t tc = col[ej]; col[ej] = col[eb]; col[eb] = tc;
-          const float tv = val[ej]; val[ej] = val[eb]; val[eb] = tv;
-        }
-      }
-      // padding (value 0) still reads a row: point it at the row a real lane
-      // of the same parity reads in this step (same address, no extra access)
       const bool real = val[ej] != 0.f;
-      const uint32_t same = __ballot_sync(0xffffffffu, real) & (p ? 0xaaaaaaaau : 0x55555555u);
       const uint32_t mine = col[ej];
-      const uint32_t other = __shfl_sync(0xffffffffu, mine, same ? __ffs(same) - 1 : lane);
-      if (!real && same) col[ej] = uint16_t(other);
+      const uint32_t same = __ballot_sync(0xffffffffu, real) & pmask;
+      const uint32_t inq = same & (0xffu << (lane & 24));
+      const int src = inq ? __ffs(inq) - 1 : (same ? __ffs(same) - 1 : lane);
+      const uint32_t other = __shfl_sync(0xffffffffu, mine, src);
+      if (!real) col[ej] = uint16_t(other);
     }
   }
 }
@@ -537,7 +581,11 @@ void tiled_build(Hamiltonian& h, const std::vector<uint64_t>& bs) {
   CG_CUDA(cudaGetLastError());
   count_launch();
   if (nruns) {
-    k_tbalance<<<unsigned(std::min<uint64_t>((nruns * 32 + 255) / 256, 152ull * 64)), 256, 0, s>>>(
+    k_tbalance<<<unsigned(std::min<uint64_t>((nruns * 4 + 255) / 256, 152ull * 64)), 256, 0, s>>>(
+        nruns, t.roff.p, t.col.p, t.val.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    k_tpadaddr<<<unsigned(std::min<uint64_t>((nruns * 32 + 255) / 256, 152ull * 64)), 256, 0, s>>>(
         nruns, t.roff.p, t.col.p, t.val.p);
     CG_CUDA(cudaGetLastError());
     count_launch();
