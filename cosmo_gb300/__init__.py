@@ -138,6 +138,8 @@ _SIGS = {
     "cg_batch_solve": (C.c_int32, [_P, C.POINTER(BatchParams), _P, _P, _P, C.POINTER(BatchStats)]),
     "cg_jt_expectations": (C.c_int32, [_P, _P, C.c_int32, _P, _P]),
     "cg_jj_spin": (C.c_int32, [C.c_double, C.c_int32]),
+    "cg_sf_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "cg_xshlsf": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -238,6 +240,26 @@ def jt_expectations(basis: "ManyBodyStates", vecs) -> tuple[np.ndarray, np.ndarr
     return jj, tt
 
 
+def sf_amplitudes(parent: "ManyBodyStates", vp, daughter: "ManyBodyStates", vd) -> np.ndarray:
+    """amp[q, p, s] = <D_q| a_s |P_p> for one-particle removal from the parent
+    states (rows of vp) to the daughter states (rows of vd, at most 16),
+    computed on the GPU (the overlaps of XSHLSF, xmlshell/XSHLSF.cpp:150-175)."""
+    vp = np.ascontiguousarray(np.asarray(vp, dtype=np.float64).reshape(-1, parent.n))
+    vd = np.ascontiguousarray(np.asarray(vd, dtype=np.float64).reshape(-1, daughter.n))
+    amp = np.zeros((vd.shape[0], vp.shape[0], parent.n_sps))
+    _check(lib().cg_sf_amplitudes(parent._h, _ptr(vp), vp.shape[0], daughter._h, _ptr(vd), vd.shape[0], _ptr(amp)))
+    return amp
+
+
+def xshlsf(parent_xml: str, out: str | None = None, daughter_xml: str | None = None, parent_system: str | None = None,
+           daughter_system: str | None = None, full: bool = False) -> None:
+    """The XSHLSF tool: spectroscopic factors between the parent's and the
+    daughter's <state>s, table written to `out` (xmlshell/XSHLSF.cpp)."""
+    enc = lambda x: x.encode() if x is not None else None  # noqa: E731
+    _check(lib().cg_xshlsf(enc(parent_xml), enc(parent_system), enc(daughter_xml), enc(daughter_system), enc(out),
+                           int(full)))
+
+
 def jj_spin(x: float, two_m: int) -> int:
     """2J from <J-J+> and 2M (SM::JJSpin); -1 if not a valid spin."""
     return int(lib().cg_jj_spin(float(x), int(two_m)))
@@ -329,6 +351,7 @@ class ManyBodyStates:
         _check(lib().cg_basis_dims(h, C.byref(n), C.byref(N)))
         self.n = int(n.value)
         self.N = int(N.value)
+        self.n_sps = int(problem.info.n_sps)
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -22,7 +22,7 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcosmo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu"]
+SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu", "sf.cu", "xshlsf.cpp"]
 
 
 def nvcc() -> str:
@@ -58,7 +58,7 @@ def _stale() -> bool:
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(ROOT, "include", "cosmo_gb300.h"),
                                                                 os.path.abspath(__file__)]
     deps += [os.path.join(PKG, "cli", f) for f in os.listdir(os.path.join(PKG, "cli"))]
-    if not all(os.path.exists(os.path.join(PKG, "bin", c)) for c in ("cg_dexhvjt", "cg_xshljt")):
+    if not all(os.path.exists(os.path.join(PKG, "bin", c)) for c in CLIS):
         return True
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
@@ -84,7 +84,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
 
 CLI_DIR = os.path.join(PKG, "cli")
 BIN_DIR = os.path.join(PKG, "bin")
-CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt"]
+CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf"]
 
 
 def build_cli() -> list[str]:

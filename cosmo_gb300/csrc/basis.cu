@@ -133,7 +133,6 @@ void enumerate_species(SpeciesTables& sp, int norb, int k, const int* m2, const 
 }  // namespace
 
 void basis_build(const System& sys, Basis& b) {
-  refuse_truncated(sys);
   CG_CUDA(cudaGetDevice(&b.device));
   if (!b.stream) CG_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
   cudaStream_t s = b.stream;
@@ -183,16 +182,99 @@ void basis_build(const System& sys, Basis& b) {
   std::vector<uint64_t> bstart;
   std::vector<uint32_t> bmask, bclass;
   uint64_t off = 0;
-  for (uint64_t i = 0; i < b.neut.nconf; ++i) {
-    auto it = cls_id.find({b.twom - b.neut.lex_m2[i], b.parity ^ b.neut.lex_par[i]});
-    if (it == cls_id.end()) continue;
-    uint64_t cnt = cls[{b.twom - b.neut.lex_m2[i], b.parity ^ b.neut.lex_par[i]}].size();
-    uint32_t nm = b.neut.lex_mask[i];
-    b.h_noff[colex_host(nm, b.h_binom)] = off;
-    bstart.push_back(off);
-    bmask.push_back(nm);
-    bclass.push_back(it->second);
-    off += cnt;
+  const Truncation& tr = sys.trunc;
+  b.truncated = tr.active();
+  if (!b.truncated) {
+    for (uint64_t i = 0; i < b.neut.nconf; ++i) {
+      auto it = cls_id.find({b.twom - b.neut.lex_m2[i], b.parity ^ b.neut.lex_par[i]});
+      if (it == cls_id.end()) continue;
+      uint64_t cnt = cls[{b.twom - b.neut.lex_m2[i], b.parity ^ b.neut.lex_par[i]}].size();
+      uint32_t nm = b.neut.lex_mask[i];
+      b.h_noff[colex_host(nm, b.h_binom)] = off;
+      bstart.push_back(off);
+      bmask.push_back(nm);
+      bclass.push_back(it->second);
+      off += cnt;
+    }
+  } else {
+    // the truncated basis keeps the untruncated order (XsysmbsOMP writes its
+    // determinants from a sorted map, xmlshell/xmbs/XsysmbsOMP.cpp:405-428):
+    // neutron configurations in lexicographic order, each followed by the
+    // allowed proton configurations of its class in lexicographic order
+    const int R = int(tr.rejections.size());
+    std::vector<int> q(b.ns);
+    for (int i = 0; i < b.ns; ++i) q[i] = sp_quanta(sys.sps[i]);
+    int ncore = 0, pcore = 0;  // SM::CoreQuanta: the first Nv (Zv) s.p. states in list order
+    for (int i = 0; i < std::min(b.kn, b.nn); ++i) ncore += q[i];
+    for (int i = 0; i < std::min(b.kp, b.np); ++i) pcore += q[b.nn + i];
+    auto quanta = [&](uint64_t gmask) {
+      int Q = 0;
+      for (uint64_t m = gmask; m; m &= m - 1) Q += q[__builtin_ctzll(m)];
+      return Q;
+    };
+    // per proton configuration (lexicographic index): quanta above the core and rejection counts
+    std::vector<int> pq(b.prot.nconf), pc(b.prot.nconf * std::max(R, 1));
+    for (uint64_t i = 0; i < b.prot.nconf; ++i) {
+      const uint64_t gm = uint64_t(b.prot.lex_mask[i]) << b.nn;
+      pq[i] = quanta(gm) - pcore;
+      for (int r = 0; r < R; ++r) pc[i * R + r] = __builtin_popcountll(gm & tr.rejections[r].mask);
+    }
+    // lexicographic index of each proton class member (cls holds them in rank order)
+    std::map<std::vector<int>, uint32_t> list_id;
+    std::vector<std::vector<uint32_t>> lists;  // lexicographic proton indices
+    b.npc = b.prot.nconf;
+    b.h_nlist.assign(std::max<uint64_t>(b.neut.nconf, 1), ~0u);
+    for (uint64_t i = 0; i < b.neut.nconf; ++i) {
+      const std::pair<int, int> ckey{b.twom - b.neut.lex_m2[i], b.parity ^ b.neut.lex_par[i]};
+      auto it = cls_id.find(ckey);
+      if (it == cls_id.end()) continue;
+      const uint64_t gm = b.neut.lex_mask[i];
+      const int qn = quanta(gm) - ncore;
+      if (tr.hw && (qn < 0 || qn > tr.hwmax)) continue;
+      std::vector<int> key{int(it->second), qn};
+      for (int r = 0; r < R; ++r) key.push_back(__builtin_popcountll(gm & tr.rejections[r].mask));
+      auto lit = list_id.find(key);
+      if (lit == list_id.end()) {
+        std::vector<uint32_t> keep;
+        for (uint32_t li : cls[ckey]) {
+          const int qp = pq[li];
+          if (tr.hw && (qp < 0 || qp > tr.hwmax || qn + qp < tr.hwmin || qn + qp > tr.hwmax)) continue;
+          bool ok = true;
+          for (int r = 0; r < R && ok; ++r) {
+            const int c = key[2 + r] + pc[li * R + r];
+            ok = c >= tr.rejections[r].nmin && c <= tr.rejections[r].nmax;
+          }
+          if (ok) keep.push_back(li);
+        }
+        lit = list_id.emplace(key, uint32_t(lists.size())).first;
+        lists.push_back(std::move(keep));
+      }
+      const std::vector<uint32_t>& lst = lists[lit->second];
+      if (lst.empty()) continue;
+      const uint32_t nm = b.neut.lex_mask[i];
+      const uint64_t cn = colex_host(nm, b.h_binom);
+      b.h_noff[cn] = off;
+      b.h_nlist[cn] = lit->second;
+      bstart.push_back(off);
+      bmask.push_back(nm);
+      bclass.push_back(lit->second);
+      off += lst.size();
+    }
+    // the lists take the place of the classes; per-list ranks by proton colex rank
+    cstart.clear();
+    cmasks.clear();
+    b.h_lrank.assign(std::max<uint64_t>(lists.size() * b.npc, 1), ~0u);
+    for (size_t L = 0; L < lists.size(); ++L) {
+      cstart.push_back(uint32_t(cmasks.size()));
+      uint32_t r = 0;
+      for (uint32_t li : lists[L]) {
+        const uint32_t pm = b.prot.lex_mask[li];
+        cmasks.push_back(pm);
+        b.h_lrank[L * b.npc + colex_host(pm, b.h_binom)] = r++;
+      }
+    }
+    b.nlist.upload(b.h_nlist, s);
+    b.lrank.upload(b.h_lrank, s);
   }
   b.n = off;
   cstart.push_back(uint32_t(cmasks.size()));
@@ -250,8 +332,13 @@ uint64_t basis_locate_host(const Basis& b, const uint16_t* t) {
     else { pmask |= 1ull << (x - b.nn); ++kp; m2p += b.sp_m2[x]; pp ^= b.sp_par[x]; }
   }
   if (kn != b.kn || kp != b.kp || m2n + m2p != b.twom || (pn ^ pp) != b.parity) return miss;
-  uint64_t no = b.h_noff[colex_host(nmask, b.h_binom)];
+  const uint64_t cn = colex_host(nmask, b.h_binom);
+  uint64_t no = b.h_noff[cn];
   if (no == ~0ull) return miss;
+  if (b.truncated) {
+    const uint32_t r = b.h_lrank[uint64_t(b.h_nlist[cn]) * b.npc + colex_host(pmask, b.h_binom)];
+    return r == ~0u ? miss : no + r;
+  }
   return no + b.h_pcrank[colex_host(pmask, b.h_binom)];
 }
 

@@ -977,7 +977,7 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
       ~StreamLoan() { h.stream = nullptr; }
     } loan{H};
     H.stream = s;
-    spmm_autotune(H, kMaxB, 3);
+    spmm_autotune(H, kMaxB, 2);
     bs.tune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
   }
   bs.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

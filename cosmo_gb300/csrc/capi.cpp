@@ -219,7 +219,6 @@ cg_status cg_basis_build(const cg_problem* p, cg_basis** out) {
     CG_NOT_NULL(p);
     CG_NOT_NULL(out);
     *out = nullptr;
-    cg::refuse_truncated(p->sys);
     require_device();
     auto b = std::make_unique<cg_basis>();
     b->sys = p->sys;
@@ -301,6 +300,7 @@ cg_status cg_hamiltonian_build_virtual(const cg_problem* p, const cg_basis* b, i
     CG_NOT_NULL(b);
     CG_NOT_NULL(out);
     *out = nullptr;
+    cg::refuse_truncated(b->sys, "the on-the-fly product");
     same_device(b->b.device);
     if (p->sys.sps.size() != b->sys.sps.size() || p->sys.nv != b->sys.nv || p->sys.zv != b->sys.zv)
       throw cg::Error(CG_ERR_ARG, "basis was built for another problem");
@@ -469,7 +469,6 @@ cg_status cg_batch_create(const cg_problem* const* problems, int32_t count, cg_b
     std::vector<const cg::Operator*> ops;
     for (int i = 0; i < count; ++i) {
       CG_NOT_NULL(problems[i]);
-      cg::refuse_truncated(problems[i]->sys);
       sys.push_back(&problems[i]->sys);
       ops.push_back(&problems[i]->op);
     }
@@ -558,6 +557,31 @@ cg_status cg_jt_expectations(const cg_basis* b, const double* vecs, int32_t nsta
 
 int32_t cg_jj_spin(double jj, int32_t two_m) { return cg::jj_spin(jj, two_m); }
 
+cg_status cg_xshlsf(const char* parent_xml, const char* parent_system, const char* daughter_xml,
+                    const char* daughter_system, const char* out_path, int32_t full) {
+  return guard([&] {
+    CG_NOT_NULL(parent_xml);
+    require_device();
+    const std::string px = parent_xml, dx = daughter_xml ? daughter_xml : parent_xml;
+    cg::xshlsf(px, parent_system ? parent_system : "", dx, daughter_system ? daughter_system : "",
+               out_path ? out_path : "", full != 0);
+  });
+}
+
+cg_status cg_sf_amplitudes(const cg_basis* parent, const double* vp, int32_t np, const cg_basis* daughter,
+                           const double* vd, int32_t nd, double* amp) {
+  return guard([&] {
+    CG_NOT_NULL(parent);
+    CG_NOT_NULL(daughter);
+    CG_NOT_NULL(vp);
+    CG_NOT_NULL(vd);
+    CG_NOT_NULL(amp);
+    same_device(parent->b.device);
+    same_device(daughter->b.device);
+    cg::sf_amplitudes(parent->sys, parent->b, vp, np, daughter->b, vd, nd, amp);
+  });
+}
+
 cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* ee_path, int32_t nstates,
                     const char* xml_out, int32_t* n_added) {
   return guard([&] {
@@ -565,7 +589,6 @@ cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* e
     CG_NOT_NULL(ee_path);
     const std::string sname = system_name ? system_name : "";
     cg::System sys = cg::load_system(xml_path, sname);
-    cg::refuse_truncated(sys);
     require_device();
     cg::Basis b;
     cg::basis_build(sys, b);

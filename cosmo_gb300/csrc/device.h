@@ -95,6 +95,16 @@ struct Basis {
   std::vector<uint32_t> h_bclass;  // proton class of each block
   std::vector<uint32_t> h_cstart;  // first position of each proton class in h_cmasks
   std::vector<uint32_t> h_cmasks;  // proton masks, class by class, rank order
+  // truncated bases: a neutron block holds the proton configurations of its
+  // class that the truncation allows with it, a list fixed by the neutron
+  // configuration's quanta and rejection counts; h_bclass then numbers these
+  // lists (h_cstart / h_cmasks hold them) and the in-block rank is
+  // lrank[list * npc + colex(p)] (~0u: not in the list)
+  bool truncated = false;
+  uint64_t npc = 0;                // proton configurations (colex ranks)
+  DBuf<uint32_t> nlist;            // by neutron colex rank: list of its block, ~0u if none
+  DBuf<uint32_t> lrank;            // lists x npc
+  std::vector<uint32_t> h_nlist, h_lrank;
   // host copies used for locate and .mbs output
   std::vector<uint64_t> h_noff;
   std::vector<uint32_t> h_pcrank;
@@ -108,6 +118,9 @@ uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom);
 
 // <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nst host vectors (state k at vecs + k*n).
 void jt_expectations(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt);
+// amp[(q * np + p) * ns + s] = <D_q| a_s |P_p> (sf.cu)
+void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
+                   const double* vd, int nd, double* amp);
 // twice the spin from <J-J+> and twice the projection; -1 if not (half-)integer within 0.1
 int jj_spin(double x, int two_m);
 void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);

@@ -78,6 +78,9 @@ struct Ctx {
   const uint64_t* state;
   const uint64_t* noff;
   const uint32_t* pcrank;
+  const uint32_t* nlist;  // truncated basis: list of each neutron block (null when not truncated)
+  const uint32_t* lrank;  // truncated basis: rank inside a list by proton colex rank, ~0u if absent
+  uint64_t npc;
   const double* e1;
   const double* v2;
   const uint64_t* mmask;
@@ -107,11 +110,21 @@ __device__ __forceinline__ uint64_t colex(uint64_t mask, const uint64_t* binom) 
   return r;
 }
 
-// Index of determinant K; ~0 if K is outside the basis (never for an M- and
-// parity-conserving operator: the caller flags it as an internal error).
+// Index of determinant K.  In an untruncated basis an M- and parity-conserving
+// operator never leaves it, so ~0 marks an internal error the caller flags; a
+// truncated basis drops the determinants outside it (kOutside: the matrix is
+// the operator projected on the basis, as the reference's PPMatrix2CSBBlk
+// skips a ket that SM::locate does not find, include/sm/PPMatrix.cxx:571-656).
+constexpr uint64_t kOutside = ~0ull - 1;
 __device__ __forceinline__ uint64_t ket_index(const Ctx& c, const Shared& sh, uint64_t K) {
   uint64_t kn = K & c.nall, kp = K >> c.nn;
-  uint64_t off = c.noff[colex(kn, sh.binom)];
+  const uint64_t cn = colex(kn, sh.binom);
+  uint64_t off = c.noff[cn];
+  if (c.nlist) {
+    if (off == ~0ull) return kOutside;
+    const uint32_t r = c.lrank[uint64_t(c.nlist[cn]) * c.npc + colex(kp, sh.binom)];
+    return r == ~0u ? kOutside : off + r;
+  }
   if (off == ~0ull) return ~0ull;
   uint64_t idx = off + c.pcrank[colex(kp, sh.binom)];
   return idx < c.n ? idx : ~0ull;
@@ -243,6 +256,7 @@ __global__ void k_count(Ctx c, const uint64_t* binom64, uint32_t* __restrict__ c
     uint32_t k = 0;
     visit_row(c, sh, row, [&](uint64_t col, double v, bool) {
       if (col == ~0ull) { atomicOr(err, 1); return; }
+      if (col == kOutside) return;
       k += (fabs(v) >= kDrop);
     });
     counts[row] = k;
@@ -258,7 +272,7 @@ __global__ void k_fill(Ctx c, const uint64_t* binom64, const uint64_t* __restric
     uint64_t p = rowptr[row];
     double dv = 0.0;
     visit_row(c, sh, row, [&](uint64_t k, double v, bool isdiag) {
-      if (k == ~0ull) return;
+      if (k >= kOutside) return;
       if (fabs(v) >= kDrop) {
         col[p] = uint32_t(k);
         val[p] = v;
@@ -475,6 +489,9 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   c.state = b.state.p;
   c.noff = b.noff.p;
   c.pcrank = b.pcrank.p;
+  c.nlist = b.truncated ? b.nlist.p : nullptr;
+  c.lrank = b.truncated ? b.lrank.p : nullptr;
+  c.npc = b.npc;
   c.e1 = dop.e1.p;
   c.v2 = dop.v2.p;
   c.mmask = dop.mmask.p;

@@ -45,6 +45,9 @@ struct RaiseArgs {
   uint64_t ns_src;           // source dimension
   const uint64_t* noff;      // source basis: neutron block offsets by colex rank
   const uint32_t* pcrank;    // source basis: proton rank by colex rank
+  const uint32_t* nlist;     // truncated source basis: list of each neutron block (null otherwise)
+  const uint32_t* lrank;     // truncated source basis: rank inside a list by proton colex rank
+  uint64_t npc;
   const uint64_t* binom;
   const int8_t* partner;     // per s.p. y: the x that O moves into y, -1 if none
   const double* coef;        // per s.p. y: the operator value for x -> y
@@ -68,8 +71,17 @@ __global__ void k_raise_norm(RaiseArgs a, double* __restrict__ part, int* __rest
       const int x = a.partner[y];
       if (x < 0 || ((K >> x) & 1)) continue;
       const uint64_t S = K ^ (1ull << y) ^ (1ull << x);
-      const uint64_t off = a.noff[colex_d(S & a.nall, a.binom)];
-      const uint64_t idx = off == ~0ull ? ~0ull : off + a.pcrank[colex_d(S >> a.nn, a.binom)];
+      const uint64_t cn = colex_d(S & a.nall, a.binom);
+      const uint64_t off = a.noff[cn];
+      uint64_t idx;
+      if (a.nlist) {  // truncated source basis: a source outside it has amplitude 0
+        if (off == ~0ull) continue;
+        const uint32_t r = a.lrank[uint64_t(a.nlist[cn]) * a.npc + colex_d(S >> a.nn, a.binom)];
+        if (r == ~0u) continue;
+        idx = off + r;
+      } else {
+        idx = off == ~0ull ? ~0ull : off + a.pcrank[colex_d(S >> a.nn, a.binom)];
+      }
       if (idx >= a.ns_src) { atomicOr(err, 1); continue; }
       const int p = __popcll(S & bel(x)) + __popcll((S & ~(1ull << x)) & bel(y));
       const double c = (p & 1) ? -a.coef[y] : a.coef[y];
@@ -120,6 +132,9 @@ void raise_norms(const Basis& src, const Basis& tb, const std::vector<int8_t>& p
   a.ns_src = src.n;
   a.noff = src.noff.p;
   a.pcrank = src.pcrank.p;
+  a.nlist = src.truncated ? src.nlist.p : nullptr;
+  a.lrank = src.truncated ? src.lrank.p : nullptr;
+  a.npc = src.npc;
   a.binom = src.binom.p;
   a.partner = dpart.p;
   a.coef = dcoef.p;

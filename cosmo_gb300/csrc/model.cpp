@@ -275,10 +275,49 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   if (const std::string* ft = sn->attr("T")) sys.filter_twoT = parse_spin2(*ft);
   if (!sn->attr("P")) throw Error(CG_ERR_PARSE, "system needs P");
   sys.parity = ((*sn->attr("P"))[0] == '-') ? 1 : 0;
-  // getXMLData (include/xmlParser.cxx:129) takes hwmax from an attribute or a child element
-  if (sn->attr("hwmax") || sn->child("hwmax")) sys.truncation += "hwmax ";
-  if (sn->count("hwrejection")) sys.truncation += "<hwrejection> ";
-  if (sn->count("rejection")) sys.truncation += "<rejection> ";
+  // basis truncation (XsysmbsOMP, xmlshell/xmbs/XsysmbsOMP.cpp:214-300); the
+  // reference's getXMLData (include/xmlParser.cxx:129) reads a value from an
+  // attribute or from the text of a child element
+  auto xml_value = [](const XmlNode& nd, const char* k) -> const std::string* {
+    if (const std::string* a = nd.attr(k)) return a;
+    if (const XmlNode* c = nd.child(k)) return &c->text;
+    return nullptr;
+  };
+  auto xml_int = [&](const XmlNode& nd, const char* k) {
+    const std::string* v = xml_value(nd, k);
+    if (!v) throw Error(CG_ERR_PARSE, std::string("missing ") + k + " on <" + nd.tag + ">");
+    return std::atoi(v->c_str());
+  };
+  if (const std::string* hm = xml_value(*sn, "hwmax")) {
+    sys.trunc.hw = true;
+    sys.trunc.hwmax = std::atoi(hm->c_str());
+    sys.trunc.hwmin = 0;
+    sys.truncation += "hwmax ";
+  }
+  if (const XmlNode* hr = sn->child("hwrejection")) {  // only the first one counts, as in the reference
+    sys.trunc.hw = true;
+    sys.trunc.hwmax = xml_int(*hr, "HWMAX");
+    sys.trunc.hwmin = xml_int(*hr, "HWMIN");
+    sys.truncation += "<hwrejection> ";
+  }
+  for (int r = 0; r < sn->count("rejection"); ++r) {
+    const XmlNode* rj = sn->child("rejection", r);
+    Truncation::Rejection rej;
+    rej.nmin = xml_int(*rj, "NMIN");
+    rej.nmax = xml_int(*rj, "NMAX");
+    for (int o = 0; o < rj->count("orbital"); ++o) {
+      const XmlNode* ob = rj->child("orbital", o);
+      const int level = xml_int(*ob, "index") - 1;
+      const std::string type = ob->attr("type") ? *ob->attr("type") : std::string("n");
+      for (size_t i = 0; i < sys.sps.size(); ++i) {
+        const bool neut = sys.sps[i].tz2 > 0;
+        if (sys.sps[i].level == level && ((neut && (type == "pn" || type == "n")) || (!neut && (type == "pn" || type == "p"))))
+          rej.mask |= 1ull << i;
+      }
+    }
+    sys.trunc.rejections.push_back(rej);
+    if (r == 0) sys.truncation += "<rejection> ";
+  }
   if (const XmlNode* mb = sn->child("ManyBodyStates"))
     if (mb->attr("name")) sys.mbs_name = *mb->attr("name");
   if (const XmlNode* mx = sn->child("matrix")) {
@@ -311,11 +350,10 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   return sys;
 }
 
-void refuse_truncated(const System& sys) {
-  if (!sys.truncation.empty())
-    throw Error(CG_ERR_UNSUPPORTED, "truncated bases (" + sys.truncation +
-                                        "on the system) are not built; the full basis would differ from the "
-                                        "reference's");
+void refuse_truncated(const System& sys, const char* route) {
+  if (sys.trunc.active())
+    throw Error(CG_ERR_UNSUPPORTED, std::string(route) + " does not take truncated bases (" + sys.truncation +
+                                        "on the system)");
 }
 
 // ----------------------------------------------------- Oxbash reader

@@ -52,6 +52,27 @@ struct Orbit {
   std::string type;  // "pn", "p" or "n"
 };
 
+// Basis truncation of a system (XsysmbsOMP, xmlshell/xmbs/XsysmbsOMP.cpp:
+// 214-300): oscillator quanta Q = sum of 2n + l over the occupied states,
+// counted above the core quanta Ncore / Pcore (the quanta of the first Nv
+// neutron / Zv proton s.p. states in list order, SM::CoreQuanta,
+// include/sm/SingleParticleStates.cxx:155-168); a neutron configuration is
+// kept when Qn - Ncore is in [0, hwmax], a proton one when Qp - Pcore is, a
+// determinant when (Qn - Ncore) + (Qp - Pcore) is in [hwmin, hwmax]
+// (PartitionClass.cxx:151-190, 390-413); and for each rejection the number
+// of particles in its flagged s.p. states is in [nmin, nmax]
+// (TestRestriction, PartitionClass.cxx:23-40).
+struct Truncation {
+  bool hw = false;
+  int hwmin = 0, hwmax = 0;
+  struct Rejection {
+    int nmin = 0, nmax = 0;
+    uint64_t mask = 0;  // flagged s.p. states (global index, neutrons first)
+  };
+  std::vector<Rejection> rejections;
+  bool active() const { return hw || !rejections.empty(); }
+};
+
 // A CI problem: valence space, particle numbers, M sector and interaction files.
 struct System {
   std::string name;
@@ -69,18 +90,20 @@ struct System {
   int filter_twoJ = -1;          // system J / T attributes: XSHLJT keeps only these states
   int filter_twoT = -1;
   std::string xml_dir;
-  // basis truncations of the system node (hwmax attribute, <hwrejection>,
-  // <rejection>, xmlshell/xmbs/XsysmbsOMP.cpp:214-300), listed; the basis
-  // builder refuses a truncated system instead of building the full basis
+  // basis truncations of the system node (hwmax, <hwrejection>, <rejection>),
+  // listed in `truncation` and given in `trunc`
   std::string truncation;
+  Truncation trunc;
 };
 
 System load_system(const std::string& xml_path, const std::string& system_name);
 
-// Throws CG_ERR_UNSUPPORTED for a system with a basis truncation: every route
-// that builds a basis (single problem, batch, XSHLJT) calls it before any
-// device work, so no truncated system is ever solved on the full basis.
-void refuse_truncated(const System& sys);
+// Throws CG_ERR_UNSUPPORTED for a system with a basis truncation, on routes
+// that do not take truncated bases (the on-the-fly product), before any
+// device work.
+void refuse_truncated(const System& sys, const char* route);
+// Oscillator quanta 2n + l of s.p. state i.
+inline int sp_quanta(const SPState& s) { return 2 * s.n + s.l; }
 
 // ------------------------------------------------------------ operators
 // Forward-ordered m-scheme operator terms.  Keys follow the reference's

@@ -30,4 +30,11 @@ std::vector<NewState> xshljt_states(const System& sys, const Basis& b, const std
                                     const std::string& file_attr, std::vector<double>* jj_out,
                                     std::vector<double>* tt_out);
 
+// XSHLSF (xmlshell/XSHLSF.cpp:40-222): spectroscopic factors between the
+// states of a parent system and a daughter system with one particle less
+// (overlaps when the particle numbers are equal), table written to out_path
+// (none when empty), per orbital l or, with full, per s.p. state.
+void xshlsf(const std::string& parent_xml, const std::string& parent_system, const std::string& daughter_xml,
+            const std::string& daughter_system, const std::string& out_path, bool full);
+
 }  // namespace cg

@@ -374,6 +374,26 @@ cg_status cg_jt_expectations(const cg_basis* b, const double* vecs, int32_t nsta
 /* 2J from <J-J+> and 2M (SM::JJSpin, include/sm/QN.cxx:40-60): -1 when J + M is
  * not an integer within 0.1. */
 int32_t cg_jj_spin(double jj, int32_t two_m);
+
+/* ------------------------------------------------ spectroscopic factors */
+/* One-particle removal amplitudes <D_q| a_s |P_p> for every s.p. state s, the
+ * overlaps of XSHLSF (xmlshell/XSHLSF.cpp:150-175: PPMatrix::OverlapNH,
+ * include/sm/PPMatrix.cxx:275-302, of the one-body operator a_s).  parent: a
+ * basis with one neutron or one proton more than daughter, same valence space;
+ * vp: np parent vectors, vd: nd daughter vectors (1..16), host, vector k at
+ * v + k*n (the .EE layout).  amp: nd * np * n_sps values, amp[(q*np + p)*n_sps
+ * + s]; 0 for the states s that cannot connect the two (M, charge, parity)
+ * sectors.  Computed on the GPU in FP64. */
+cg_status cg_sf_amplitudes(const cg_basis* parent, const double* vp, int32_t np, const cg_basis* daughter,
+                           const double* vd, int32_t nd, double* amp);
+/* The XSHLSF tool (xmlshell/XSHLSF.cpp:40-222): every <state> of the parent
+ * system (parent_xml; parent_system may be NULL when the file holds one system)
+ * against every <state> of the daughter system (daughter_xml, NULL: the same
+ * file), the vectors read from the .EE files their <wavefunction file id>
+ * names; spectroscopic factors written to out_path (NULL: none) per orbital l,
+ * or per s.p. state (2j, A, SF) when full is nonzero; a report on stdout. */
+cg_status cg_xshlsf(const char* parent_xml, const char* parent_system, const char* daughter_xml,
+                    const char* daughter_system, const char* out_path, int32_t full);
 /* XSHLJT (xmlshell/XSHLJT.cpp, include/xsm/XSHLJT.cxx:38-142): the first nstates
  * (all when <= 0) eigenpairs of ee_path get 2J and 2T from <J-J+> / <T-T+>
  * computed on the GPU, E minus lambda*(J-M)(J+M+2)/4 when the system's matrix

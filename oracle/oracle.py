@@ -215,3 +215,30 @@ def full_from_upper(rp, cols, vals):
     U = sp.csr_matrix((vals, (rows, cols.astype(np.int64))), shape=(n, n))
     D = sp.diags(U.diagonal())
     return (U + U.T - D).tocsr()
+
+
+def annihilation_amplitudes(zp: np.ndarray, vp: np.ndarray, zd: np.ndarray, vd: np.ndarray, ns: int) -> np.ndarray:
+    """amp[q, p, s] = <D_q| a_s |P_p> for every s.p. state s: the overlap the
+    reference's XSHLSF takes with PPMatrix::OverlapNH and the one-body
+    operator a_s (xmlshell/XSHLSF.cpp:150-175, include/sm/PPMatrix.cxx:
+    275-302).  zp, zd: parent and daughter bases (sorted tuples), vp, vd:
+    their vectors (states x dimension).  For each daughter determinant D and
+    each s outside it, P = D + s; SM::Annihilation removes s from P with the
+    phase of the number of states of P below s (include/sm/operators.cxx:
+    121-150)."""
+    index = {tuple(int(x) for x in t): i for i, t in enumerate(zp)}
+    vp = np.asarray(vp, dtype=np.float64).reshape(-1, len(zp))
+    vd = np.asarray(vd, dtype=np.float64).reshape(-1, len(zd))
+    amp = np.zeros((len(vd), len(vp), ns))
+    for di, D in enumerate(zd):
+        d = tuple(int(x) for x in D)
+        for s in range(ns):
+            if s in d:
+                continue
+            P = tuple(sorted(d + (s,)))
+            i = index.get(P)
+            if i is None:
+                continue
+            sign = -1.0 if P.index(s) & 1 else 1.0
+            amp[:, :, s] += sign * np.outer(vd[:, di], vp[:, i])
+    return amp

@@ -189,6 +189,61 @@ def jt_case(name: str, work: str, xml: str, nstates: int, manifest: dict, keep_v
     print(name, "jt", manifest[name]["ref_twoJ"])
 
 
+# spectroscopic factors (XSHLSF): parent sd 2n+2p, daughter sd 2n+1p, same
+# seed (same TBMEs); the systems carry Tz so that the reference's XSHLJT
+# records it in the <wavefunction> nodes XSHLSF reads
+SF_PAIR = (("sd22m0s1", SyntheticSystem("sd", 2, 2, 0, "+", 0.5, 1)),
+           ("sd21m1s1", SyntheticSystem("sd", 2, 1, 1, "+", 0.5, 1)))
+SF_STATES = 5
+
+
+def spin_text(t2: int) -> str:
+    return str(t2 // 2) if t2 % 2 == 0 else f"{t2}/2"
+
+
+def sf_xml(work: str, name: str, sysd) -> str:
+    """The synthetic system XML with a Tz attribute on the system node."""
+    sysd.name = name
+    _, xml = make_system(work, sysd)
+    txt = open(xml).read().replace("<system ", f'<system Tz="{spin_text(sysd.nv - sysd.zv)}" ', 1)
+    open(xml, "w").write(txt)
+    return xml
+
+
+def sf_case(work: str, manifest: dict) -> None:
+    """The reference's XSHLSF tables (per l, and per s.p. state with -of) for
+    the SF_PAIR systems, after the reference's Davidson (ref_dump) and XSHLJT
+    recorded their states; stores the <state> nodes, the .EE files and the
+    tables."""
+    arrays = {}
+    entry = {}
+    xjs = []
+    for name, sysd in SF_PAIR:
+        xml = sf_xml(work, name, sysd)
+        run_ref("ref_dump", xml, name, work, SF_STATES, 0)
+        txt = open(xml).read()
+        jj = re.search(r'<matrix JJ="([^"]*)"/>', txt)
+        txt = txt.replace(jj.group(0), f'<matrix name="{name}" format="pp" JJ="{jj.group(1)}"/>')
+        xj = os.path.join(work, name + ".sf.xml")
+        open(xj, "w").write(txt)
+        with open(os.path.join(work, name + ".sf.log"), "w") as log:
+            subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLJT"), xj, "-n", str(SF_STATES)], cwd=work,
+                           stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+        out = open(xj).read()
+        entry[name] = {"states": re.findall(r"<state [^>]*>\s*<wavefunction[^>]*/>\s*</state>", out)}
+        arrays[name + "_EE"] = np.fromfile(os.path.join(work, name + ".EE"), np.uint8)
+        xjs.append(xj)
+    for key, flags in (("table", []), ("table_full", ["-of"])):
+        outp = os.path.join(work, key + ".txt")
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLSF"), xjs[0], "-f", xjs[1], "-o", outp] + flags,
+                       cwd=work, stdin=subprocess.DEVNULL, stdout=subprocess.DEVNULL, stderr=subprocess.STDOUT,
+                       check=True)
+        entry[key] = [ln for ln in open(outp).read().splitlines() if ln and not ln.startswith("#")]
+    manifest["sf_sd22_sd21"] = entry
+    np.savez_compressed(os.path.join(HERE, "sf_sd22_sd21.npz"), **arrays)
+    print("sf", len(entry["table"]), "lines per l,", len(entry["table_full"]), "per s.p. state")
+
+
 def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) -> None:
     """The reference's .HH file (XHH+JJ, PPMatrix::Write): sha256, and the bytes
     for one small case so the .HH reader can be pinned on a GPU."""
@@ -221,6 +276,8 @@ def main() -> None:
     manifest = json.load(open(mpath)) if os.path.exists(mpath) else {}
     work = tempfile.mkdtemp(prefix="cg_golden_")
     try:
+        if not skip("sf_sd22_sd21"):
+            sf_case(work, manifest)
         for name, (sysd, full, nst, it) in CASES.items():
             if skip(name):
                 continue

@@ -295,43 +295,21 @@ def test_oracle_truncated_basis_matches_reference(name, tmp_path):
     assert 0 < len(z) < len(full)
 
 
-def test_truncated_system_refused_by_basis_builder(tmp_path):
-    """A system with a basis truncation loads (its s.p. table is usable), but
-    the basis builder refuses it with CG_ERR_UNSUPPORTED on the host, before
-    any device work, instead of building the full basis."""
+def test_truncated_system_loads_and_parses(tmp_path):
+    """Systems with basis truncations (hwmax as an attribute or as a child
+    element, <hwrejection>, <rejection>) load; a malformed <hwrejection>
+    without HWMAX is a parse error.  The truncated bases themselves are built
+    and checked on the GPU (tests/test_truncated.py)."""
     import sys
     import cosmo_gb300 as cg
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
     import truncated as T
-    for name in ("psd22m0_hw2", "psd32m1_hwr13", "psd21m1_rej"):
+    for name in T.CASES:
         p = cg.Problem(T.write_case(str(tmp_path), name))
         assert len(p.sps()) == 36
-        with pytest.raises(cg.CosmoError) as e:
-            cg.ManyBodyStates(p)
-        assert e.value.status == -6 and "truncated bases" in str(e.value)
-
-
-def test_truncated_system_refused_by_every_basis_route(tmp_path):
-    """The batched solver and the XSHLJT tool build bases too: both refuse a
-    truncated system on the host with CG_ERR_UNSUPPORTED (no device needed),
-    and hwmax given as a child element (<hwmax>2</hwmax>, which the
-    reference's getXMLData also reads) counts as a truncation."""
-    import sys
-    import cosmo_gb300 as cg
-    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
-    import truncated as T
-    xml = T.write_case(str(tmp_path), "psd22m0_hw2")
+    xml = T.write_case(str(tmp_path), "psd32m1_hwr13")
+    bad = tmp_path / "bad.xml"
+    bad.write_text(open(xml).read().replace(' HWMAX="3"', "", 1))
     with pytest.raises(cg.CosmoError) as e:
-        cg.Batch([cg.Problem(xml)])
-    assert e.value.status == -6 and "truncated bases" in str(e.value)
-    ee = tmp_path / "none.EE"
-    ee.write_bytes(b"")
-    with pytest.raises(cg.CosmoError) as e:
-        cg.xshljt(xml, str(ee), out=str(tmp_path / "out.xml"))
-    assert e.value.status == -6 and "truncated bases" in str(e.value)
-    txt = open(xml).read().replace(' hwmax="2"', "", 1).replace("<matrix JJ", "<hwmax>2</hwmax><matrix JJ", 1)
-    child = tmp_path / "child.xml"
-    child.write_text(txt)
-    with pytest.raises(cg.CosmoError) as e:
-        cg.ManyBodyStates(cg.Problem(str(child)))
-    assert e.value.status == -6 and "hwmax" in str(e.value)
+        cg.Problem(str(bad))
+    assert e.value.status == -3 and "HWMAX" in str(e.value)
