@@ -319,6 +319,8 @@ __global__ void __launch_bounds__(1024) k_tiled(TArgs a, const float* __restrict
     // S before, writes the unit's bounds and starts its four copies
     int issued = 0;
     bool stop = false;
+    // entries are read once; x blocks are staged again by the CTAs of other row blocks
+    const uint64_t once = bulk::policy_evict_first(), again = bulk::policy_evict_last();
     for (int base = 0; base < I && !stop; base += 32) {
       TItem d{};
       if (base + lane < I) d = a.items[i0 + base + lane];
@@ -345,9 +347,9 @@ __global__ void __launch_bounds__(1024) k_tiled(TArgs a, const float* __restrict
             const uint32_t ng = g1 - g0, xb = xrows * 32u;
             bulk::expect_tx(bar, rcb + xb + ng * 192u);
             bulk::copy(st + 16, a.rcopy + rc, rcb, bar);
-            bulk::copy(st + kTiledSlotHead, x + uint64_t(xrow) * 8, xb, bar);
-            bulk::copy(st + kTiledSlotHead + xbytes, a.col + uint64_t(g0) * 32, ng * 64u, bar);
-            bulk::copy(st + kTiledSlotHead + xbytes + cbytes, a.val + uint64_t(g0) * 32, ng * 128u, bar);
+            bulk::copy_hint(st + kTiledSlotHead, x + uint64_t(xrow) * 8, xb, bar, again);
+            bulk::copy_hint(st + kTiledSlotHead + xbytes, a.col + uint64_t(g0) * 32, ng * 64u, bar, once);
+            bulk::copy_hint(st + kTiledSlotHead + xbytes + cbytes, a.val + uint64_t(g0) * 32, ng * 128u, bar, once);
             issued = i + 1;
           }
         }
