@@ -141,6 +141,11 @@ _SIGS = {
     "cg_sf_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P]),
     "cg_xshlsf": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
+    "cg_transition_terms": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, _P, _P, _P,
+                                        C.c_int32, C.POINTER(C.c_int32)]),
+    "cg_onebody_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, _P, _P, C.c_int32, _P]),
+    "cg_xshlemb": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32,
+                               C.c_char_p]),
     "cg_gather_ceiling": (C.c_int32, [C.c_uint64, C.c_int32, C.POINTER(C.c_double)]),
     "cg_spmm_get_tuning": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cg_spmm_set_format": (C.c_int32, [_P, C.c_int32]),
@@ -258,6 +263,56 @@ def xshlsf(parent_xml: str, out: str | None = None, daughter_xml: str | None = N
     enc = lambda x: x.encode() if x is not None else None  # noqa: E731
     _check(lib().cg_xshlsf(enc(parent_xml), enc(parent_system), enc(daughter_xml), enc(daughter_system), enc(out),
                            int(full)))
+
+
+CG_EMB_WEISSKOPF, CG_EMB_UNITS, CG_EMB_LOGFT, CG_EMB_PHASE_INFINITY = 1, 2, 4, 8
+
+
+def transition_terms(xml: str, system: str | None = None, operator: str | None = None, kappa: int = 0,
+                     phase_infinity: bool = False) -> list:
+    """[(i, f, v)]: the m-scheme terms v a+_f a_i of the <operator> node of an
+    XML file (XSHLEMB's operators, include/sm/EMspherical2sp.cxx) for the
+    projection kappa, on the system's s.p. states.  Host computation."""
+    enc = lambda x: x.encode() if x is not None else None  # noqa: E731
+    flags = CG_EMB_PHASE_INFINITY if phase_infinity else 0
+    n = C.c_int32()
+    _check(lib().cg_transition_terms(enc(xml), enc(system), enc(operator), kappa, flags, None, None, None, 0,
+                                     C.byref(n)))
+    i = np.zeros(max(n.value, 1), np.int32)
+    f = np.zeros(max(n.value, 1), np.int32)
+    v = np.zeros(max(n.value, 1), np.float64)
+    _check(lib().cg_transition_terms(enc(xml), enc(system), enc(operator), kappa, flags, _ptr(i), _ptr(f), _ptr(v),
+                                     n.value, C.byref(n)))
+    return [(int(i[k]), int(f[k]), float(v[k])) for k in range(n.value)]
+
+
+def onebody_amplitudes(parent: "ManyBodyStates", vp, daughter: "ManyBodyStates", vd, terms) -> np.ndarray:
+    """amp[q, p] = <D_q| sum v a+_f a_i |P_p> for the (i, f, v) terms, parent
+    states the rows of vp, daughter states the rows of vd (at most 16), on the
+    GPU (the overlaps of XSHLEMB, PPMatrix::OverlapNH)."""
+    vp = np.ascontiguousarray(np.asarray(vp, dtype=np.float64).reshape(-1, parent.n))
+    vd = np.ascontiguousarray(np.asarray(vd, dtype=np.float64).reshape(-1, daughter.n))
+    ti = np.ascontiguousarray([t[0] for t in terms] or [0], dtype=np.int32)
+    tf = np.ascontiguousarray([t[1] for t in terms] or [0], dtype=np.int32)
+    tv = np.ascontiguousarray([t[2] for t in terms] or [0.0], dtype=np.float64)
+    amp = np.zeros((vd.shape[0], vp.shape[0]))
+    _check(lib().cg_onebody_amplitudes(parent._h, _ptr(vp), vp.shape[0], daughter._h, _ptr(vd), vd.shape[0],
+                                       _ptr(ti), _ptr(tf), _ptr(tv), len(terms), _ptr(amp)))
+    return amp
+
+
+def xshlemb(parent_xml: str, out: str | None = None, daughter_xml: str | None = None,
+            parent_system: str | None = None, daughter_system: str | None = None, operator: str | None = None,
+            weisskopf: bool = False, units: bool = False, logft: bool = False,
+            phase_infinity: bool = False) -> None:
+    """The XSHLEMB tool: B values of the parent XML's <operator> between the
+    parent's and the daughter's <state>s, written as <transition>/<moment>
+    children of the parent's states into `out` (the parent XML when None)."""
+    enc = lambda x: x.encode() if x is not None else None  # noqa: E731
+    flags = ((CG_EMB_WEISSKOPF if weisskopf else 0) | (CG_EMB_UNITS if units else 0) | (CG_EMB_LOGFT if logft else 0)
+             | (CG_EMB_PHASE_INFINITY if phase_infinity else 0))
+    _check(lib().cg_xshlemb(enc(parent_xml), enc(parent_system), enc(daughter_xml), enc(daughter_system), enc(out),
+                            flags, enc(operator)))
 
 
 def jj_spin(x: float, two_m: int) -> int:

@@ -22,7 +22,7 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcosmo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu", "sf.cu", "xshlsf.cpp"]
+SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu", "sf.cu", "xshlsf.cpp", "em.cpp", "xshlemb.cpp"]
 
 
 def nvcc() -> str:
@@ -84,7 +84,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
 
 CLI_DIR = os.path.join(PKG, "cli")
 BIN_DIR = os.path.join(PKG, "bin")
-CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf"]
+CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb"]
 
 
 def build_cli() -> list[str]:

@@ -568,6 +568,69 @@ cg_status cg_xshlsf(const char* parent_xml, const char* parent_system, const cha
   });
 }
 
+cg_status cg_transition_terms(const char* xml_path, const char* system_name, const char* op_name, int32_t kappa,
+                              int32_t flags, int32_t* i, int32_t* f, double* v, int32_t cap, int32_t* count) {
+  return guard([&] {
+    CG_NOT_NULL(xml_path);
+    CG_NOT_NULL(count);
+    const cg::System sys = cg::load_system(xml_path, system_name ? system_name : "");
+    const cg::XmlNode root = cg::parse_xml_file(xml_path);
+    const cg::TransitionOp op = cg::read_transition_operator(root, op_name ? op_name : "",
+                                                             (flags & CG_EMB_PHASE_INFINITY) != 0, nullptr, nullptr);
+    const std::vector<cg::OneBodyTerm> t = cg::transition_terms(sys, op, kappa);
+    *count = int32_t(t.size());
+    if (cap == 0 && !i && !f && !v) return;
+    CG_NOT_NULL(i);
+    CG_NOT_NULL(f);
+    CG_NOT_NULL(v);
+    if (cap < int32_t(t.size())) throw cg::Error(CG_ERR_ARG, "cap below the number of terms");
+    for (size_t k = 0; k < t.size(); ++k) {
+      i[k] = t[k].i;
+      f[k] = t[k].f;
+      v[k] = t[k].v;
+    }
+  });
+}
+
+cg_status cg_onebody_amplitudes(const cg_basis* parent, const double* vp, int32_t np, const cg_basis* daughter,
+                                const double* vd, int32_t nd, const int32_t* i, const int32_t* f, const double* v,
+                                int32_t nterms, double* amp) {
+  return guard([&] {
+    CG_NOT_NULL(parent);
+    CG_NOT_NULL(daughter);
+    CG_NOT_NULL(vp);
+    CG_NOT_NULL(vd);
+    CG_NOT_NULL(amp);
+    if (nterms < 0) throw cg::Error(CG_ERR_ARG, "negative term count");
+    if (nterms) {
+      CG_NOT_NULL(i);
+      CG_NOT_NULL(f);
+      CG_NOT_NULL(v);
+    }
+    same_device(parent->b.device);
+    same_device(daughter->b.device);
+    std::vector<cg::OneBodyTerm> t(nterms);
+    for (int32_t k = 0; k < nterms; ++k) t[k] = {i[k], f[k], v[k]};
+    cg::onebody_amplitudes(parent->sys, parent->b, vp, np, daughter->b, vd, nd, t, amp);
+  });
+}
+
+cg_status cg_xshlemb(const char* parent_xml, const char* parent_system, const char* daughter_xml,
+                     const char* daughter_system, const char* out_xml, int32_t flags, const char* op_name) {
+  return guard([&] {
+    CG_NOT_NULL(parent_xml);
+    require_device();
+    cg::XshlembOptions o;
+    o.weisskopf = flags & CG_EMB_WEISSKOPF;
+    o.units = flags & CG_EMB_UNITS;
+    o.logft = flags & CG_EMB_LOGFT;
+    o.phase_infinity = flags & CG_EMB_PHASE_INFINITY;
+    o.op_name = op_name ? op_name : "";
+    cg::xshlemb(parent_xml, parent_system ? parent_system : "", daughter_xml ? daughter_xml : "",
+                daughter_system ? daughter_system : "", out_xml ? out_xml : "", o);
+  });
+}
+
 cg_status cg_sf_amplitudes(const cg_basis* parent, const double* vp, int32_t np, const cg_basis* daughter,
                            const double* vd, int32_t nd, double* amp) {
   return guard([&] {

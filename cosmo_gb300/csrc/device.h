@@ -121,6 +121,10 @@ void jt_expectations(const System& sys, const Basis& b, const double* vecs, int 
 // amp[(q * np + p) * ns + s] = <D_q| a_s |P_p> (sf.cu)
 void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                    const double* vd, int nd, double* amp);
+// amp[q * np + p] = <D_q| sum_t v_t a+_f a_i |P_p> (sf.cu); nd <= 16
+struct OneBodyTerm;
+void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
+                        const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp);
 // twice the spin from <J-J+> and twice the projection; -1 if not (half-)integer within 0.1
 int jj_spin(double x, int two_m);
 void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);

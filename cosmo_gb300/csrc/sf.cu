@@ -1,7 +1,10 @@
-// Spectroscopic amplitudes on the GPU: <D_q| a_s |P_p> for one-particle
-// removal, the overlaps the reference's XSHLSF takes (xmlshell/XSHLSF.cpp:
-// 150-175) with PPMatrix::OverlapNH and the one-body operator a_s
-// (include/sm/PPMatrix.cxx:275-302).
+// Overlaps of one-body operators between two bases on the GPU:
+// spectroscopic amplitudes <D_q| a_s |P_p> for one-particle removal, the
+// overlaps the reference's XSHLSF takes (xmlshell/XSHLSF.cpp:150-175) with
+// PPMatrix::OverlapNH and the one-body operator a_s (include/sm/
+// PPMatrix.cxx:275-302); and transition amplitudes <D_q| sum v a+_f a_i |P_p>
+// of XSHLEMB's electromagnetic and beta operators (xmlshell/XSHLEMB.cpp:
+// 248-270).
 //
 // The reference applies a_s to every parent determinant (SM::Annihilation,
 // include/sm/operators.cxx:121-150: phase of the number of states below s),
@@ -15,6 +18,7 @@
 #include <cmath>
 
 #include "device.h"
+#include "em.h"
 
 namespace cg {
 
@@ -105,7 +109,159 @@ __global__ void k_rows_sf(uint64_t n, int nst, const double* __restrict__ src, d
   dst[i] = src[uint64_t(k) * n + r];
 }
 
+// <D_q| sum_t v_t a+_f a_i |P> for one parent vector: one thread per
+// daughter determinant D and every term t whose f is occupied in D and whose
+// i is free in D - f (or i = f); the parent determinant P = D - f + i is
+// located by the colex tables of the parent basis and the phase is that of
+// a+_f a_i acting on P (states below i in P, then below f in P - i).
+struct ObArgs {
+  uint64_t nd;
+  const uint64_t* dstate;
+  const double* psid;
+  int nq;
+  int nn;
+  uint64_t nall;
+  uint64_t np_;
+  const uint64_t* noff;
+  const uint32_t* pcrank;
+  const uint32_t* nlist;
+  const uint32_t* lrank;
+  uint64_t npc;
+  const uint64_t* binom;
+  const double* psip;
+  const int2* tif;  // per term: i, f
+  const double* tv;  // per term: value
+  int nt;
+};
+
+__global__ void k_onebody_amplitudes(ObArgs a, double* __restrict__ part, int* __restrict__ err) {
+  __shared__ double red[kMaxDaughter][256 / 32];
+  double acc[kMaxDaughter];
+#pragma unroll
+  for (int q = 0; q < kMaxDaughter; ++q) acc[q] = 0.0;
+  for (uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; row < a.nd;
+       row += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t D = a.dstate[row];
+    double w = 0.0;
+    for (int t = 0; t < a.nt; ++t) {
+      const int2 e = a.tif[t];
+      if (!((D >> e.y) & 1)) continue;
+      const uint64_t Df = D & ~(1ull << e.y);
+      if (e.x != e.y && ((Df >> e.x) & 1)) continue;
+      const uint64_t P = Df | (1ull << e.x);
+      const uint64_t cn = colex_sf(P & a.nall, a.binom);
+      const uint64_t off = a.noff[cn];
+      if (off == ~0ull) continue;
+      uint64_t idx;
+      if (a.nlist) {
+        const uint32_t r = a.lrank[uint64_t(a.nlist[cn]) * a.npc + colex_sf(P >> a.nn, a.binom)];
+        if (r == ~0u) continue;
+        idx = off + r;
+      } else {
+        idx = off + a.pcrank[colex_sf(P >> a.nn, a.binom)];
+      }
+      if (idx >= a.np_) { atomicOr(err, 1); continue; }
+      const int ph = __popcll(P & below_sf(e.x)) + __popcll(Df & below_sf(e.y));
+      const double v = a.tv[t] * a.psip[idx];
+      w += (ph & 1) ? -v : v;
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxDaughter; ++q)
+      if (q < a.nq) acc[q] += w * a.psid[row * a.nq + q];
+  }
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kMaxDaughter; ++q) {
+    double v = acc[q];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+    if (lane == 0) red[q][wi] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kMaxDaughter) {
+    double v = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) v += red[threadIdx.x][i];
+    part[size_t(blockIdx.x) * kMaxDaughter + threadIdx.x] = v;
+  }
+}
+
 }  // namespace
+
+void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
+                        const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp) {
+  if (np < 1 || nd < 1 || nd > kMaxDaughter) throw Error(CG_ERR_ARG, "1..16 daughter states, at least one parent state");
+  if (parent.ns != daughter.ns || parent.nn != daughter.nn)
+    throw Error(CG_ERR_ARG, "parent and daughter bases have different valence spaces");
+  if (parent.kn + parent.kp != daughter.kn + daughter.kp)
+    throw Error(CG_ERR_ARG, "a one-body operator keeps the number of particles");
+  const int ns = parent.ns;
+  for (size_t i = 0; i < size_t(nd) * np; ++i) amp[i] = 0.0;
+  // the terms that take the daughter's sector into the parent's (species
+  // change, m and parity), so that P = D - f + i is always in the parent's
+  // sector and its colex ranks cannot alias another sector's
+  const int dn = parent.kn - daughter.kn;  // +1: a neutron becomes a proton
+  std::vector<int2> tif;
+  std::vector<double> tv;
+  for (const OneBodyTerm& t : terms) {
+    if (t.i < 0 || t.i >= ns || t.f < 0 || t.f >= ns) throw Error(CG_ERR_ARG, "one-body term outside the s.p. states");
+    const bool in_ = t.i < parent.nn, fn = t.f < parent.nn;
+    if (int(in_) - int(fn) != dn) continue;
+    const SPState &si = psys.sps[t.i], &sf = psys.sps[t.f];
+    if (sf.m2 - si.m2 != daughter.twom - parent.twom) continue;
+    if ((sf.parity ^ si.parity) != (daughter.parity ^ parent.parity)) continue;
+    if (t.v == 0.0) continue;
+    tif.push_back(make_int2(t.i, t.f));
+    tv.push_back(t.v);
+  }
+  if (tif.empty() || daughter.n == 0 || parent.n == 0) return;
+  cudaStream_t st = parent.stream;
+  DBuf<double> dcm(daughter.n * nd), psid(daughter.n * nd), pv(parent.n);
+  dcm.upload(vd, daughter.n * nd, st);
+  k_rows_sf<<<unsigned((daughter.n * nd + 255) / 256), 256, 0, st>>>(daughter.n, nd, dcm.p, psid.p);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
+  DBuf<int2> dtif;
+  DBuf<double> dtv;
+  DBuf<int> err(1);
+  dtif.upload(tif, st);
+  dtv.upload(tv, st);
+  CG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  ObArgs a;
+  a.nd = daughter.n;
+  a.dstate = daughter.state.p;
+  a.psid = psid.p;
+  a.nq = nd;
+  a.nn = parent.nn;
+  a.nall = parent.nn ? ((parent.nn == 64) ? ~0ull : ((1ull << parent.nn) - 1)) : 0;
+  a.np_ = parent.n;
+  a.noff = parent.noff.p;
+  a.pcrank = parent.pcrank.p;
+  a.nlist = parent.truncated ? parent.nlist.p : nullptr;
+  a.lrank = parent.truncated ? parent.lrank.p : nullptr;
+  a.npc = parent.npc;
+  a.binom = parent.binom.p;
+  a.tif = dtif.p;
+  a.tv = dtv.p;
+  a.nt = int(tif.size());
+  const int T = 256;
+  const unsigned gx = unsigned(std::min<uint64_t>((daughter.n + T - 1) / T, 152ull * 4));
+  DBuf<double> part(size_t(gx) * kMaxDaughter);
+  std::vector<double> h(part.n);
+  for (int p = 0; p < np; ++p) {
+    pv.upload(vp + uint64_t(p) * parent.n, parent.n, st);
+    a.psip = pv.p;
+    k_onebody_amplitudes<<<gx, T, 0, st>>>(a, part.p, err.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    CG_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+    CG_CUDA(cudaStreamSynchronize(st));
+    for (unsigned g = 0; g < gx; ++g)
+      for (int q = 0; q < nd; ++q) amp[size_t(q) * np + p] += h[size_t(g) * kMaxDaughter + q];
+  }
+  int herr = 0;
+  CG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CG_CUDA(cudaStreamSynchronize(st));
+  if (herr) throw Error(CG_ERR_INTERNAL, "a one-body move left the parent basis");
+}
 
 void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                    const double* vd, int nd, double* amp) {

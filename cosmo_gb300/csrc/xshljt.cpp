@@ -115,6 +115,102 @@ std::string spin_text(int twice) {
   return b;
 }
 
+std::string num_text(double x) { return num_str(x); }
+
+namespace {
+
+// [start, end) of the system element's start tag and the position of its
+// end tag (npos for a self-closed system)
+void find_system(const std::string& text, const std::string& system_name, size_t& start, size_t& stag_end,
+                 size_t& close) {
+  size_t p = 0;
+  start = std::string::npos;
+  while ((p = find_tag(text, "system", p, text.size())) != std::string::npos) {
+    const size_t e = tag_end(text, p);
+    Attrs a = parse_attrs(text, p + 1, e);
+    const std::string* nm = get(a, "name");
+    if (system_name.empty() || (nm && *nm == system_name)) {
+      start = p;
+      break;
+    }
+    p = e;
+  }
+  if (start == std::string::npos) throw Error(CG_ERR_PARSE, "xml: system " + system_name + " not found");
+  stag_end = tag_end(text, start);
+  close = text[stag_end - 1] == '/' ? std::string::npos : text.find("</system>", stag_end);
+}
+
+std::string line_indent(const std::string& text, size_t p) {
+  const size_t ls = text.rfind('\n', p);
+  const size_t b = ls == std::string::npos ? 0 : ls + 1;
+  std::string in = text.substr(b, p - b);
+  for (char& c : in)
+    if (!is_space(c)) c = ' ';
+  return in;
+}
+
+}  // namespace
+
+std::string xml_state_children(const std::string& text, const std::string& system_name,
+                               const std::vector<std::vector<std::string>>& front,
+                               const std::vector<std::vector<std::string>>& back) {
+  size_t sys, stag_end, close;
+  find_system(text, system_name, sys, stag_end, close);
+  if (close == std::string::npos) {
+    if (!front.empty() || !back.empty()) throw Error(CG_ERR_PARSE, "xml: the system has no <state> children");
+    return text;
+  }
+  std::string out = text.substr(0, stag_end + 1);
+  size_t q = stag_end + 1;
+  size_t k = 0;
+  while (true) {
+    const size_t st = find_tag(text, "state", q, close);
+    if (st == std::string::npos) break;
+    const size_t e = tag_end(text, st);
+    const std::string in = line_indent(text, st) + "\t";
+    std::string fr, bk;
+    if (k < front.size())
+      for (const std::string& c : front[k]) fr += "\n" + in + c;
+    if (k < back.size())
+      for (const std::string& c : back[k]) bk += "\n" + in + c;
+    if (text[e - 1] == '/') {  // <state .../>
+      out += text.substr(q, e - 1 - q);
+      if (fr.empty() && bk.empty()) {
+        out += "/>";
+      } else {
+        out += ">" + fr + bk + "\n" + line_indent(text, st) + "</state>";
+      }
+      q = e + 1;
+    } else {
+      const size_t end = text.find("</state>", e);
+      if (end == std::string::npos || end > close) throw Error(CG_ERR_PARSE, "xml: </state> missing");
+      size_t tail = end;  // before the whitespace that precedes </state>
+      while (tail > e + 1 && is_space(text[tail - 1])) --tail;
+      out += text.substr(q, e + 1 - q) + fr + text.substr(e + 1, tail - (e + 1)) + bk + text.substr(tail, end + 8 - tail);
+      q = end + 8;
+    }
+    ++k;
+  }
+  if (k < front.size() || k < back.size()) throw Error(CG_ERR_INTERNAL, "xml: fewer <state> children than records");
+  return out + text.substr(q);
+}
+
+std::string xml_append_attrs(const std::string& text, const std::string& tag, int index,
+                             const std::vector<std::pair<std::string, std::string>>& attrs) {
+  size_t p = 0;
+  for (int i = 0;; ++i) {
+    p = find_tag(text, tag, p, text.size());
+    if (p == std::string::npos) throw Error(CG_ERR_PARSE, "xml: no <" + tag + "> number " + std::to_string(index));
+    if (i == index) break;
+    p = tag_end(text, p);
+  }
+  size_t e = tag_end(text, p);
+  if (text[e - 1] == '/') --e;
+  std::string add;
+  for (auto& kv : attrs) add += " " + kv.first + "=\"" + kv.second + "\"";
+  return text.substr(0, e) + add + text.substr(e);
+}
+
 std::string xml_add_states(const std::string& text, const std::string& system_name,
                            const std::vector<NewState>& add) {
   // the system element

@@ -25,17 +25,8 @@
 
 namespace cg {
 
-namespace {
-
-struct SfState {
-  std::string name, ex;
-  int twoJ = 0, twoT = 0, parity = 0, twoJz = 0, twoTz = 0, id = 0;
-  double E = 0;
-  std::string file;
-};
-
 // the <state> children of the system node (ReadXMLState, include/xsm/xState.cxx:38-46)
-std::vector<SfState> read_states(const std::string& xml_path, const std::string& system_name) {
+std::vector<StateRecord> read_states(const std::string& xml_path, const std::string& system_name) {
   XmlNode root = parse_xml_file(xml_path);
   const XmlNode* sn = nullptr;
   const int ns = root.count("system");
@@ -47,14 +38,15 @@ std::vector<SfState> read_states(const std::string& xml_path, const std::string&
     }
   }
   if (!sn) throw Error(CG_ERR_ARG, "no system " + system_name + " in " + xml_path);
-  std::vector<SfState> out;
+  std::vector<StateRecord> out;
   for (int i = 0; i < sn->count("state"); ++i) {
     const XmlNode* st = sn->child("state", i);
     const XmlNode* wf = st->child("wavefunction");
     if (!wf || !wf->attr("file") || !wf->attr("id")) throw Error(CG_ERR_PARSE, "a <state> without its wave function");
-    SfState s;
+    StateRecord s;
     s.name = st->attr("name") ? *st->attr("name") : std::string();
     s.ex = st->attr("Ex") ? *st->attr("Ex") : std::string();
+    s.e_text = st->attr("E") ? *st->attr("E") : std::string();
     if (!st->attr("J")) throw Error(CG_ERR_PARSE, "a <state> without J");
     s.twoJ = parse_spin2(*st->attr("J"));
     s.twoT = st->attr("T") ? parse_spin2(*st->attr("T")) : -1;
@@ -70,9 +62,10 @@ std::vector<SfState> read_states(const std::string& xml_path, const std::string&
   return out;
 }
 
-// vector `id` of an .EE file (SM::EnergyStateRead), looked up as given, then
-// beside the XML file
-std::vector<double> read_vector(const std::string& file, const std::string& xml_dir, int id, uint64_t n) {
+// vector `id` of an .EE file and its energy (SM::EnergyStateRead), looked up
+// as given, then beside the XML file
+std::vector<double> read_vector(const std::string& file, const std::string& xml_dir, int id, uint64_t n,
+                                double* energy) {
   std::ifstream f(file, std::ios::binary);
   if (!f && !xml_dir.empty()) f.open(xml_dir + "/" + file, std::ios::binary);
   if (!f) throw Error(CG_ERR_IO, "cannot open " + file);
@@ -86,6 +79,7 @@ std::vector<double> read_vector(const std::string& file, const std::string& xml_
     f.read(reinterpret_cast<char*>(e), 24);
     f.read(reinterpret_cast<char*>(&m), 8);
     if (!f || m != n) throw Error(CG_ERR_IO, ".EE vector dimension does not match the basis: " + file);
+    if (energy) *energy = e[0];
     if (k < id) f.seekg(std::streamoff(8 * m), std::ios::cur);
     else f.read(reinterpret_cast<char*>(v.data()), std::streamsize(8 * n));
   }
@@ -98,15 +92,13 @@ std::string dir_of(const std::string& p) {
   return s == std::string::npos ? std::string() : p.substr(0, s);
 }
 
-}  // namespace
-
 void xshlsf(const std::string& pxml, const std::string& psys_name, const std::string& dxml,
             const std::string& dsys_name, const std::string& out_path, bool full) {
   const System ps = load_system(pxml, psys_name);
   const System ds = load_system(dxml, dsys_name);
   if (ps.sps.size() != ds.sps.size() || ps.n_neutron_states != ds.n_neutron_states)
     throw Error(CG_ERR_ARG, "parent and daughter systems have different valence spaces");
-  const std::vector<SfState> pst = read_states(pxml, ps.name), dst = read_states(dxml, ds.name);
+  const std::vector<StateRecord> pst = read_states(pxml, ps.name), dst = read_states(dxml, ds.name);
   const int NP = ps.nv + ps.zv, ND = ds.nv + ds.zv;
   if (NP != ND && NP - ND != 1)
     throw Error(CG_ERR_ARG, "the number of particles in the final system must be less by one than in the initial");
@@ -114,12 +106,12 @@ void xshlsf(const std::string& pxml, const std::string& psys_name, const std::st
   basis_build(ps, pb);
   basis_build(ds, db);
   std::vector<double> pv, dv;
-  for (const SfState& s : pst) {
-    const auto v = read_vector(s.file, dir_of(pxml), s.id, pb.n);
+  for (const StateRecord& s : pst) {
+    const auto v = read_vector(s.file, dir_of(pxml), s.id, pb.n, nullptr);
     pv.insert(pv.end(), v.begin(), v.end());
   }
-  for (const SfState& s : dst) {
-    const auto v = read_vector(s.file, dir_of(dxml), s.id, db.n);
+  for (const StateRecord& s : dst) {
+    const auto v = read_vector(s.file, dir_of(dxml), s.id, db.n, nullptr);
     dv.insert(dv.end(), v.begin(), v.end());
   }
   const int np = int(pst.size()), nd = int(dst.size()), ns = int(ps.sps.size());
@@ -144,9 +136,9 @@ void xshlsf(const std::string& pxml, const std::string& psys_name, const std::st
     of << (full ? "#parent Ex(p) daugther Ex(d) L J A SF=|A|^2 \n" : "#parent Ex(p) daugther Ex(d) L SF=|A|^2 \n");
   }
   for (int p = 0; p < np; ++p) {
-    const SfState& P = pst[p];
+    const StateRecord& P = pst[p];
     for (int q = 0; q < nd; ++q) {
-      const SfState& D = dst[q];
+      const StateRecord& D = dst[q];
       const int jz = P.twoJz - D.twoJz, tz = P.twoTz - D.twoTz, par = P.parity ^ D.parity;
       std::cout << "Parent: " << P.name << " Ex=" << P.ex << " E=" << P.E << "\n";
       std::cout << "Daughter: " << D.name << " Ex=" << D.ex << " E=" << D.E << "\n";

@@ -394,6 +394,38 @@ cg_status cg_sf_amplitudes(const cg_basis* parent, const double* vp, int32_t np,
  * or per s.p. state (2j, A, SF) when full is nonzero; a report on stdout. */
 cg_status cg_xshlsf(const char* parent_xml, const char* parent_system, const char* daughter_xml,
                     const char* daughter_system, const char* out_path, int32_t full);
+
+/* --------------------------------------- electromagnetic / beta transitions */
+/* Flags of cg_xshlemb / cg_transition_terms. */
+#define CG_EMB_WEISSKOPF 1      /* -w: B also in Weisskopf units (E, M) */
+#define CG_EMB_UNITS 2          /* -u: B in e^2 fm^2L / mu_N^2 fm^(2L-2), oscillator length on moments */
+#define CG_EMB_LOGFT 4          /* -ft: log ft (6145 s, g_A = 1.27) */
+#define CG_EMB_PHASE_INFINITY 8 /* -p: oscillator radial functions positive at infinity */
+/* The m-scheme terms v a+_f a_i of the transition operator of the
+ * <operator> node (op_name, or the first one when NULL) of an XML file, for the
+ * projection kappa (m_f = m_i + 2 kappa in doubled units), on the s.p. states
+ * of system_name: ElectricSPMultipole / MagneticSPMultipole / BetaJAMultipole
+ * with oscillator radial integrals, SPTPlus + Hermitian2FullOperator for F
+ * (include/sm/EMspherical2sp.cxx, include/xsm/xmlemb.cxx:121-206).  Writes up
+ * to cap terms into (i, f, v) and their number into *count (CG_ERR_ARG when
+ * cap is too small; NULL arrays with cap 0 only count).  Host only. */
+cg_status cg_transition_terms(const char* xml_path, const char* system_name, const char* op_name, int32_t kappa,
+                              int32_t flags, int32_t* i, int32_t* f, double* v, int32_t cap, int32_t* count);
+/* Transition amplitudes <D_q| sum_t v_t a+_f a_i |P_p> of a one-body operator
+ * between two bases with the same number of particles (the overlaps XSHLEMB
+ * takes with PPMatrix::OverlapNH, include/sm/PPMatrix.cxx:275-302): vp, vd
+ * host vectors (.EE layout), nd 1..16; amp[q*np + p].  On the GPU in FP64. */
+cg_status cg_onebody_amplitudes(const cg_basis* parent, const double* vp, int32_t np, const cg_basis* daughter,
+                                const double* vd, int32_t nd, const int32_t* i, const int32_t* f, const double* v,
+                                int32_t nterms, double* amp);
+/* The XSHLEMB tool (xmlshell/XSHLEMB.cpp:116-372): B(op) of the <operator>
+ * node of parent_xml (op_name, or the first one when NULL) from every <state>
+ * of the parent system to every <state> of the daughter system (daughter_xml,
+ * NULL: the parent file), written as <transition> and <moment> children of the
+ * parent's states into out_xml (NULL: parent_xml itself); flags CG_EMB_*;
+ * a report on stdout.  Radial overlaps from files are refused (CG_ERR_UNSUPPORTED). */
+cg_status cg_xshlemb(const char* parent_xml, const char* parent_system, const char* daughter_xml,
+                     const char* daughter_system, const char* out_xml, int32_t flags, const char* op_name);
 /* XSHLJT (xmlshell/XSHLJT.cpp, include/xsm/XSHLJT.cxx:38-142): the first nstates
  * (all when <= 0) eigenpairs of ee_path get 2J and 2T from <J-J+> / <T-T+>
  * computed on the GPU, E minus lambda*(J-M)(J+M+2)/4 when the system's matrix

@@ -244,6 +244,71 @@ def sf_case(work: str, manifest: dict) -> None:
     print("sf", len(entry["table"]), "lines per l,", len(entry["table_full"]), "per s.p. state")
 
 
+# electromagnetic and beta transitions (XSHLEMB): parent sd 2n+2p, and for the
+# beta operators a daughter sd 1n+3p; both with the mass number A (Weisskopf
+# units) and Tz, their states from the reference's Davidson and XSHLJT, their
+# .mbs from the reference's XsysmbsOMP
+EM_SYSTEMS = (("sd22m0s1", SyntheticSystem("sd", 2, 2, 0, "+", 0.5, 1)),
+              ("sd13m0s1", SyntheticSystem("sd", 1, 3, 0, "+", 0.5, 1)))
+EM_STATES = 5
+# run name: (operator node, daughter system or None for the parent itself, flags)
+EM_RUNS = {
+    "E2": ('<operator name="E2" J="2" en="0.5" ep="1.5"/>', None, ["-w", "-u"]),
+    "E2p": ('<operator name="E2" J="2" en="0.5" ep="1.5"/>', None, ["-p"]),
+    "M1": ('<operator name="M1" J="1"/>', None, ["-w", "-u"]),
+    "GT-": ('<operator name="GT-" J="1"/>', "sd13m0s1", ["-ft"]),
+    "F": ('<operator name="F" J="0"/>', "sd13m0s1", []),
+}
+
+
+def em_xml(work: str, name: str, sysd) -> str:
+    """A system with its reference basis (.mbs, XsysmbsOMP), eigenvectors
+    (.EE, ref_dump) and <state> nodes (XSHLJT); returns the XML path."""
+    xml = sf_xml(work, name, sysd)
+    txt = open(xml).read().replace("<system ", f'<system A="{16 + sysd.nv + sysd.zv}" ', 1)
+    open(xml, "w").write(txt)
+    run_ref("ref_dump", xml, name, work, EM_STATES, 0)
+    txt = open(xml).read()
+    jj = re.search(r'<matrix JJ="([^"]*)"/>', txt)
+    txt = txt.replace(jj.group(0), f'<matrix name="{name}" format="pp" JJ="{jj.group(1)}"/>')
+    open(xml, "w").write(txt)
+    run_ref("XsysmbsOMP", xml, name + ".x", work, 0, 0)
+    with open(os.path.join(work, name + ".jt.log"), "w") as log:
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLJT"), xml, "-n", str(EM_STATES)], cwd=work,
+                       stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+    return xml
+
+
+def em_case(work: str, manifest: dict) -> None:
+    """The <transition> and <moment> nodes the reference XSHLEMB adds to the
+    parent's states for every EM_RUNS operator, with the systems' <state>
+    nodes and .EE files they were computed from."""
+    arrays, entry, xmls = {}, {"runs": {}}, {}
+    for name, sysd in EM_SYSTEMS:
+        xmls[name] = em_xml(work, name, sysd)
+        arrays[name + "_EE"] = np.fromfile(os.path.join(work, name + ".EE"), np.uint8)
+        entry[name] = {"states": re.findall(r"<state [^>]*>\s*<wavefunction[^>]*/>\s*</state>",
+                                            open(xmls[name]).read())}
+    parent = EM_SYSTEMS[0][0]
+    for run, (op, daughter, flags) in EM_RUNS.items():
+        xin = os.path.join(work, f"em_{run}.xml")
+        open(xin, "w").write(open(xmls[parent]).read().replace("</cosmo>", op + "\n</cosmo>", 1))
+        xout = os.path.join(work, f"em_{run}.out.xml")
+        cmd = [os.path.join(ROOT, "oracle", "_ref", "XSHLEMB"), xin, "-o", xout] + flags
+        if daughter:
+            cmd += ["-f", xmls[daughter]]
+        with open(os.path.join(work, f"em_{run}.log"), "w") as log:
+            subprocess.run(cmd, cwd=work, stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+        out = open(xout).read()
+        entry["runs"][run] = {
+            "operator": op, "daughter": daughter, "flags": flags,
+            "operator_out": re.search(r"<operator [^>]*/>", out).group(0),
+            "states": re.findall(r"<state [^>]*>.*?</state>", out, re.S)}
+    manifest["em_sd22"] = entry
+    np.savez_compressed(os.path.join(HERE, "em_sd22.npz"), **arrays)
+    print("em", {r: sum(s.count("<transition") for s in v["states"]) for r, v in entry["runs"].items()})
+
+
 def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) -> None:
     """The reference's .HH file (XHH+JJ, PPMatrix::Write): sha256, and the bytes
     for one small case so the .HH reader can be pinned on a GPU."""
@@ -278,6 +343,8 @@ def main() -> None:
     try:
         if not skip("sf_sd22_sd21"):
             sf_case(work, manifest)
+        if not skip("em_sd22"):
+            em_case(work, manifest)
         for name, (sysd, full, nst, it) in CASES.items():
             if skip(name):
                 continue

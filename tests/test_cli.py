@@ -1,6 +1,7 @@
 """The command-line drop-ins (C++ over the C ABI) against the reference's
 tools' outputs: cg_xsysmbs (Xsysmbs), cg_xhhjj (XHH+JJ), cg_dexhvjt
-(DEXHVJTcsb incl. XSHLJT), cg_davidson_vfile (davidson_vfile), cg_xshljt."""
+(DEXHVJTcsb incl. XSHLJT), cg_davidson_vfile (davidson_vfile), cg_xshljt; cg_xshlsf and
+cg_xshlemb are run against the reference tools' outputs in test_sf.py / test_em.py."""
 import hashlib
 import os
 import re
@@ -13,7 +14,7 @@ import cosmo_gb300 as cg
 from conftest import ROOT, golden, manifest, synthetic_xml
 
 BIN = os.path.join(ROOT, "cosmo_gb300", "bin")
-TOOLS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt"]
+TOOLS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb"]
 
 
 def _run(args, cwd):
