@@ -84,8 +84,8 @@ constexpr size_t jac_smem() {
 template <class R>
 __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain, const int* __restrict__ kdim,
                                                  int kconst, double* __restrict__ w, double* Zout,
-                                                 const int* __restrict__ fz, int kprev) {
-  constexpr R kConv = sizeof(R) == 4 ? R(1e-12) : R(1e-30);   // (off / total)^2 at convergence
+                                                 const int* __restrict__ fz, int kprev, int ortho) {
+  constexpr R kConv = sizeof(R) == 4 ? R(1e-12) : R(1e-24);   // (off / total)^2 at convergence
   constexpr R kTiny = sizeof(R) == 4 ? R(1e-30) : R(1e-300);
   constexpr R kSkip = sizeof(R) == 4 ? R(1e-7) : R(1e-17);
   if (fz && fz[blockIdx.x]) return;
@@ -104,12 +104,40 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
   const int b = blockIdx.x, tid = threadIdx.x;
   const int k = kdim ? kdim[b] : kconst;
   const double* Ab = Ain + size_t(b) * kJac * kJac;
-  const int kp = (kprev > 0 && kprev < k) ? kprev : 0;
+  const int kp = (kprev > 0 && kprev <= k) ? kprev : 0;
   const double* Zp = Zout + size_t(b) * kJac * kJac;
   for (int i = tid; i < kJac * kJac; i += blockDim.x) {
     const int r = i / kJac, c = i % kJac;
-    A[r][c] = (r < k && c < k) ? R(Ab[r * kJac + c]) : R(0);
     Z[r][c] = (r < kp && c < kp) ? R(Zp[r * kJac + c]) : (r == c && r >= kp ? R(1) : R(0));
+  }
+  __syncthreads();
+  if (ortho && kp > 0) {
+    // vectors from a lower-precision solve: one Newton-Schulz step,
+    // P <- P (3 I - P^T P) / 2, squares their deviation from orthonormality
+    // (A's storage holds the new P until A is loaded)
+    for (int i = tid; i < kp * kp; i += blockDim.x) {
+      const int r = i / kp, c = i % kp;
+      R v = 0;
+      for (int t = 0; t < kp; ++t) v += Z[t][r] * Z[t][c];
+      Tm[r][c] = (r == c ? R(1.5) : R(0)) - R(0.5) * v;
+    }
+    __syncthreads();
+    for (int i = tid; i < kp * kp; i += blockDim.x) {
+      const int r = i / kp, c = i % kp;
+      R v = 0;
+      for (int t = 0; t < kp; ++t) v += Z[r][t] * Tm[t][c];
+      A[r][c] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < kp * kp; i += blockDim.x) {
+      const int r = i / kp, c = i % kp;
+      Z[r][c] = A[r][c];
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < kJac * kJac; i += blockDim.x) {
+    const int r = i / kJac, c = i % kJac;
+    A[r][c] = (r < k && c < k) ? R(Ab[r * kJac + c]) : R(0);
   }
   __syncthreads();
   if (kp > 0) {
@@ -155,21 +183,24 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
       tot += v;
       if (r != c) off += v;
     }
-    red[tid] = off;
-    __syncthreads();
-    for (int s = 128; s; s >>= 1) {
-      if (tid < s) red[tid] += red[tid + s];
-      __syncthreads();
+    // warp sums, then the 8 warps' in a fixed order
+    for (int o = 16; o; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
     }
-    const R offs = red[0];
-    __syncthreads();
-    red[tid] = tot;
-    __syncthreads();
-    for (int s = 128; s; s >>= 1) {
-      if (tid < s) red[tid] += red[tid + s];
-      __syncthreads();
+    if ((tid & 31) == 0) {
+      red[tid >> 5] = off;
+      red[8 + (tid >> 5)] = tot;
     }
-    if (tid == 0) done = offs <= kConv * red[0] || offs == R(0);
+    __syncthreads();
+    if (tid == 0) {
+      R offs = 0, tots = 0;
+      for (int w8 = 0; w8 < int(blockDim.x >> 5); ++w8) {
+        offs += red[w8];
+        tots += red[8 + w8];
+      }
+      done = offs <= kConv * tots || offs == R(0);
+    }
     __syncthreads();
     if (done) break;
     for (int round = 0; round < kk - 1; ++round) {
@@ -179,7 +210,6 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
         int p = player(tid), q = player(kk - 1 - tid);
         if (p > q) { int t = p; p = q; q = t; }
         R c = 1, s = 0;
-        bool rot = false;
         if (q < k) {
           const R apq = A[p][q];
           if (fabs(apq) > kTiny && fabs(apq) > kSkip * sqrt(fabs(A[p][p] * A[q][q]))) {
@@ -187,39 +217,44 @@ __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain,
             const R t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
             c = R(1) / sqrt(R(1) + t * t);
             s = t * c;
-            rot = true;
           }
         }
         rp[tid] = p;
-        rq[tid] = rot ? q : kJac;  // kJac: no rotation this round
-        rc[tid] = c;
+        rq[tid] = q;  // >= k: the idle player of an odd k
+        rc[tid] = c;  // (1, 0) when this pair is not rotated
         rs[tid] = s;
       }
       __syncthreads();
-      // rows: A <- J^T A
-      for (int i = tid; i < (kk / 2) * k; i += blockDim.x) {
-        const int pr = i / k, j = i % k;
-        const int p = rp[pr], q = rq[pr];
-        if (q < k) {
-          const R c = rc[pr], s = rs[pr];
-          const R ap = A[p][j], aq = A[q][j];
-          A[p][j] = c * ap - s * aq;
-          A[q][j] = s * ap + c * aq;
-        }
-      }
-      __syncthreads();
-      // columns: A <- A J, Z <- Z J
-      for (int i = tid; i < (kk / 2) * k; i += blockDim.x) {
-        const int pr = i / k, j = i % k;
-        const int p = rp[pr], q = rq[pr];
-        if (q < k) {
-          const R c = rc[pr], s = rs[pr];
-          const R ap = A[j][p], aq = A[j][q];
-          A[j][p] = c * ap - s * aq;
-          A[j][q] = s * ap + c * aq;
-          const R zp = Z[j][p], zq = Z[j][q];
-          Z[j][p] = c * zp - s * zq;
-          Z[j][q] = s * zp + c * zq;
+      // A <- J^T A J and Z <- Z J in one pass: the pairs of a round are
+      // disjoint and cover every index, so each 2 x 2 block (pair a rows,
+      // pair b columns) is rotated from both sides by one thread; the rows of
+      // Z's column pairs go to the threads after the blocks
+      const int np2 = kk / 2;
+      for (int i = tid; i < np2 * np2 + k * np2; i += blockDim.x) {
+        if (i < np2 * np2) {
+          const int a = i / np2, bb = i - a * np2;
+          const int pa = rp[a], qa = rq[a], pb = rp[bb], qb = rq[bb];
+          const bool va = qa < k, vb = qb < k;
+          const R ca = rc[a], sa = rs[a], cb = rc[bb], sb = rs[bb];
+          if ((sa == R(0)) && (sb == R(0))) continue;
+          const R x00 = A[pa][pb], x01 = vb ? A[pa][qb] : R(0);
+          const R x10 = va ? A[qa][pb] : R(0), x11 = (va && vb) ? A[qa][qb] : R(0);
+          // rows p, q of the block: J_a^T
+          const R y00 = ca * x00 - sa * x10, y01 = ca * x01 - sa * x11;
+          const R y10 = sa * x00 + ca * x10, y11 = sa * x01 + ca * x11;
+          // columns p, q: J_b
+          A[pa][pb] = cb * y00 - sb * y01;
+          if (vb) A[pa][qb] = sb * y00 + cb * y01;
+          if (va) A[qa][pb] = cb * y10 - sb * y11;
+          if (va && vb) A[qa][qb] = sb * y10 + cb * y11;
+        } else {
+          const int t = i - np2 * np2, bb = t / k, r = t - bb * k;
+          const int pb = rp[bb], qb = rq[bb];
+          const R cb = rc[bb], sb = rs[bb];
+          if (qb >= k || sb == R(0)) continue;
+          const R zp = Z[r][pb], zq = Z[r][qb];
+          Z[r][pb] = cb * zp - sb * zq;
+          Z[r][qb] = sb * zp + cb * zq;
         }
       }
       __syncthreads();
@@ -792,8 +827,16 @@ struct BEngine {
     xty(V.p, lim, 0, k, AV.p, lim, k - b, b);
     k_bset_proj<<<Q, 128, 0, s>>>(k, b, k - b, G.p, S.p, fz.p);
     // warm start from the previous step's eigenvectors (size k - b; after a
-    // restart the kept block is diagonal and Z's leading block the identity)
-    k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p, k - b);
+    // restart the kept block is diagonal and Z's leading block the identity).
+    // FP32 phase: FP32 sweeps first, then FP64 sweeps from their
+    // (re-orthonormalized) vectors, which leave only ~1e-7 couplings, so the
+    // FP64 pipe does one or two sweeps instead of a full solve
+    if (sizeof(T) == 4) {
+      k_bjacobi<float><<<Q, 256, jac_smem<float>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p, k - b, 0);
+      k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p, k, 1);
+    } else {
+      k_bjacobi<double><<<Q, 256, jac_smem<double>(), s>>>(S.p, nullptr, k, w.p, Z.p, fz.p, k - b, 0);
+    }
     k_bresid<T><<<unsigned(bs.nchunks), 256, 0, s>>>(bs.chunks.p, V.p, AV.p, lim, k, w.p, Z.p, R.p, 8, b, fz.p);
     xty(R.p, 8, 0, b, R.p, 8, 0, b);
     k_bconv<<<1, 256, 0, s>>>(Q, nev, b, G.p, tol, rnorm.p, fz.p, kfreeze.p, k, nconv.p);
@@ -938,7 +981,6 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
     for (uint64_t i = 0; i < h.n; ++i) rowprob[row + i] = uint32_t(q);
     row += h.n;
     e += h.nnz;
-    CG_CUDA(cudaStreamSynchronize(s));  // h is released after its copy
   }
   pchunk[nq] = uint32_t(chunks.size());
   bs.qrow0[nq] = row;
@@ -963,10 +1005,9 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
     k_dense_fill<<<unsigned(h.n), 64, 0, s>>>(int(h.n), 0, h.rowptr.p, h.col.p, h.hi.p, h.lo.p,
                                                bs.dense.p + size_t(d) * kJac * kJac);
     count_launch();
-    CG_CUDA(cudaStreamSynchronize(s));
   }
   CG_CUDA(cudaGetLastError());
-  CG_CUDA(cudaStreamSynchronize(s));
+  CG_CUDA(cudaStreamSynchronize(s));  // the per-problem matrices (hs) are released after their copies
   // launch shape of the block-diagonal product (warps per CTA x resident CTAs
   // per SM), timed on this matrix with the solve's 8-vector rows; the iteration
   // graphs capture the chosen shape
@@ -984,8 +1025,11 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
 }
 
 void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
+  // (also loads both Jacobi kernels before any iteration is captured into a graph)
   CG_CUDA(cudaFuncSetAttribute(k_bjacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(jac_smem<double>())));
+  CG_CUDA(cudaFuncSetAttribute(k_bjacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(jac_smem<float>())));
   if (prm.nev < 1 || prm.nev > kMaxB) throw Error(CG_ERR_ARG, "batched solve: nstates must be in 1..8");
   if (prm.block < prm.nev || prm.block > kMaxB) throw Error(CG_ERR_ARG, "batched solve: block must be in nstates..8");
   if (prm.lim > kMaxLim || prm.keep < prm.block || prm.keep + prm.block > prm.lim)
@@ -1004,7 +1048,7 @@ void batch_solve(BatchSet& bs, const BatchParams& prm, BatchResult& res) {
     DBuf<double> w(size_t(bs.nd) * kJac), Z(size_t(bs.nd) * kJac * kJac);
     DBuf<int> kd;
     kd.upload(bs.ddim, s);
-    k_bjacobi<double><<<bs.nd, 256, jac_smem<double>(), s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr, 0);
+    k_bjacobi<double><<<bs.nd, 256, jac_smem<double>(), s>>>(bs.dense.p, kd.p, 0, w.p, Z.p, nullptr, 0, 0);
     CG_CUDA(cudaGetLastError());
     count_launch();
     dw.resize(size_t(bs.nd) * kJac);

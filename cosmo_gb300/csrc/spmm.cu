@@ -489,7 +489,11 @@ void spmm_host(const Hamiltonian& h, int precision, const double* x, double* y, 
 // this matrix and, for up to 8 vectors, the block-tiled product (CUDA events
 // on the handle's stream, median of `reps`); keep the fastest in h.tuning /
 // h.use_tiled.  Returns the per-candidate times (the tiled candidate carries
-// ctas_per_sm = 0).
+// ctas_per_sm = 0).  Shapes with fewer than 16 resident warps per SM are not
+// tried (the gathers of the row-wise product need more in flight; they were
+// 2-6x slower than the best on every matrix measured), and a candidate whose
+// warm-up launch takes more than twice the best median so far is not
+// repeated.
 std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   if (h.virt) throw Error(CG_ERR_UNSUPPORTED, "launch-shape tuning applies to stored matrices");
   if (h.precision != CG_PREC_FP32) throw Error(CG_ERR_ARG, "autotuning applies to FP32 matrices");
@@ -500,8 +504,15 @@ std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   cudaEvent_t e0, e1;
   CG_CUDA(cudaEventCreate(&e0));
   CG_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
   auto time_once = [&]() {
+    CG_CUDA(cudaEventRecord(e0, s));
     spmm_f32_padded(h, x.p, ld, y.p, ld, m, s);  // warm
+    CG_CUDA(cudaEventRecord(e1, s));
+    CG_CUDA(cudaEventSynchronize(e1));
+    float warm = 0;
+    CG_CUDA(cudaEventElapsedTime(&warm, e0, e1));
+    if (warm > 2.0f * best) return warm;
     std::vector<float> ts;
     for (int r = 0; r < reps; ++r) {
       CG_CUDA(cudaEventRecord(e0, s));
@@ -517,13 +528,12 @@ std::vector<SpmmCandidate> spmm_autotune(Hamiltonian& h, int m, int reps) {
   };
   std::vector<SpmmCandidate> out;
   const SpmmTuning keep = h.tuning;
-  float best = 1e30f;
   SpmmTuning bt = keep;
   bool tiled_best = false;
   h.use_tiled = false;
   for (int w : {4, 8, 16, 32})
     for (int c : {1, 2, 4, 8}) {
-      if (w * c > 64) continue;  // at most 64 resident warps per SM
+      if (w * c > 64 || w * c < 16) continue;  // 16..64 resident warps per SM
       h.tuning.warps = w;
       h.tuning.ctas_per_sm = c;
       const float med = time_once();
