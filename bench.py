@@ -186,6 +186,31 @@ def run_spmm_only(args):
                       "tuning": tune}))
 
 
+def run_batched_only(args):
+    """The 64-problem batched solve alone (for profiling): build the batch,
+    then --steps solves; prints build and per-solve times."""
+    import torch
+    import cosmo_gb300 as cg
+    from cosmo_gb300.synthetic import batched_sd_systems, make_system
+    torch.cuda.set_device(0)
+    tmp = tempfile.mkdtemp(prefix="cg_batch_")
+    probs = [cg.Problem(make_system(tmp, s)[1]) for s in batched_sd_systems()]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = cg.Batch(probs)
+    torch.cuda.synchronize()
+    build = time.perf_counter() - t0
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        eig, res, nconv, st = b.solve(5)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    print(json.dumps({"mode": "batched", "problems": len(probs), "build_seconds": build, "solve_seconds": times,
+                      "iterations_fp32": int(st.iterations_fp32), "iterations_fp64": int(st.iterations_fp64),
+                      "states_converged": int(nconv.sum()), "max_resid": float(np.nanmax(res))}))
+
+
 def spmm_roofline(cg, h, b: int, reps: int = 20, warm: int = 3, fp64: bool = False):
     """Average device time of one SpMM launch (b vectors) from CUDA events on the
     library's stream, and its algorithmic bytes per launch: stored entries x
@@ -713,7 +738,7 @@ def main():
     ap.add_argument("--skip-virtual", action="store_true")
     ap.add_argument("--skip-sd66", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=REF_ITERS_DEFAULT)
-    ap.add_argument("--mode", default="solve", choices=["solve", "spmm"])
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmm", "batched"])
     ap.add_argument("--config", default="fp44", choices=sorted(CONFIGS))
     ap.add_argument("--nvec", type=int, default=10)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
@@ -723,6 +748,8 @@ def main():
     args = ap.parse_args()
     if args.mode == "spmm":
         run_spmm_only(args)
+    elif args.mode == "batched":
+        run_batched_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -29,6 +29,10 @@ using Attrs = std::vector<std::pair<std::string, std::string>>;
 struct StateNode {
   Attrs attrs;
   std::vector<Attrs> wfs;
+  // the children in document order: an empty string stands for the next
+  // <wavefunction> of wfs, anything else is another child element kept as
+  // written (<transition>, <moment>, ... of other tools)
+  std::vector<std::string> kids;
 };
 
 std::string num_str(double x) {
@@ -273,10 +277,26 @@ std::string xml_add_states(const std::string& text, const std::string& system_na
         size_t close = body.find("</state>", e);
         if (close == std::string::npos) throw Error(CG_ERR_PARSE, "xml: </state> missing");
         size_t w = e + 1;
-        while ((w = find_tag(body, "wavefunction", w, close)) != std::string::npos) {
-          const size_t we = tag_end(body, w);
-          sn.wfs.push_back(parse_attrs(body, w + 1, we));
-          w = we + 1;
+        while (true) {
+          const size_t c0 = body.find('<', w);
+          if (c0 == std::string::npos || c0 >= close) break;
+          const size_t ce = tag_end(body, c0);
+          size_t n0 = c0 + 1;
+          while (n0 < ce && !is_space(body[n0]) && body[n0] != '/' && body[n0] != '>') ++n0;
+          const std::string name = body.substr(c0 + 1, n0 - c0 - 1);
+          size_t end = ce + 1;  // past the child element
+          if (body[ce - 1] != '/' && name[0] != '!' && name[0] != '?') {
+            const size_t cl = body.find("</" + name + ">", ce);
+            if (cl == std::string::npos || cl > close) throw Error(CG_ERR_PARSE, "xml: </" + name + "> missing");
+            end = cl + name.size() + 3;
+          }
+          if (name == "wavefunction") {
+            sn.wfs.push_back(parse_attrs(body, c0 + 1, ce));
+            sn.kids.emplace_back();
+          } else {
+            sn.kids.push_back(body.substr(c0, end - c0));
+          }
+          w = end;
         }
         next = close + 8;
       }
@@ -317,6 +337,7 @@ std::string xml_add_states(const std::string& text, const std::string& system_na
       update(wf, "file", ns.file);
       update(wf, "id", std::to_string(ns.id));
       hit->wfs.push_back(wf);
+      hit->kids.emplace_back();
     }
     update(hit->attrs, "dE", num_str(ns.dE));
   }
@@ -340,11 +361,13 @@ std::string xml_add_states(const std::string& text, const std::string& system_na
     update(sn.attrs, "name", j + pp.substr(0, 1) + "(" + std::to_string(k) + ")");
     update(sn.attrs, "Ex", num_str(o.first - order.front().first));
     emitted += "\n" + in1 + "<state" + attrs_text(sn.attrs);
-    if (sn.wfs.empty()) {
+    if (sn.kids.empty()) {
       emitted += "/>";
     } else {
       emitted += ">";
-      for (auto& wf : sn.wfs) emitted += "\n" + in2 + "<wavefunction" + attrs_text(wf) + "/>";
+      size_t wi = 0;
+      for (const std::string& kid : sn.kids)
+        emitted += "\n" + in2 + (kid.empty() ? "<wavefunction" + attrs_text(sn.wfs[wi++]) + "/>" : kid);
       emitted += "\n" + in1 + "</state>";
     }
   }

@@ -209,3 +209,11 @@ def test_gpu_transition_amplitudes_and_tool(gpu_available, tmp_path, run):
              for st in states]
     moms = [[{"m": float(_attrs(m)["m"])} for m in re.findall(r"<moment [^>]*/>", st)] for st in states]
     _check_records(run, trans, moms, parent["sys"].A + 16)
+    if run == "E2":
+        # XSHLJT run again on the result keeps the states' other children
+        ntr = txt.count("<transition"), txt.count("<moment")
+        cg.xshljt(out, os.path.join(str(tmp_path), "sd22m0s1.EE"), nstates=5)
+        again = open(out).read()
+        assert (again.count("<transition"), again.count("<moment")) == ntr
+        for st0, st1 in zip(states, re.findall(r"<state [^>]*>.*?</state>", again, re.S)):
+            assert re.findall(r"<(?:transition|moment) [^>]*/>", st0) == re.findall(r"<(?:transition|moment) [^>]*/>", st1)
