@@ -249,15 +249,21 @@ def sf_case(work: str, manifest: dict) -> None:
 # units) and Tz, their states from the reference's Davidson and XSHLJT, their
 # .mbs from the reference's XsysmbsOMP
 EM_SYSTEMS = (("sd22m0s1", SyntheticSystem("sd", 2, 2, 0, "+", 0.5, 1)),
-              ("sd13m0s1", SyntheticSystem("sd", 1, 3, 0, "+", 0.5, 1)))
+              ("sd13m0s1", SyntheticSystem("sd", 1, 3, 0, "+", 0.5, 1)),
+              ("sd22m2s1", SyntheticSystem("sd", 2, 2, 2, "+", 0.5, 1)))
 EM_STATES = 5
-# run name: (operator node, daughter system or None for the parent itself, flags)
+# run name: (operator node, daughter system or None for the parent itself, flags[, parent system])
 EM_RUNS = {
     "E2": ('<operator name="E2" J="2" en="0.5" ep="1.5"/>', None, ["-w", "-u"]),
     "E2p": ('<operator name="E2" J="2" en="0.5" ep="1.5"/>', None, ["-p"]),
     "M1": ('<operator name="M1" J="1"/>', None, ["-w", "-u"]),
     "GT-": ('<operator name="GT-" J="1"/>', "sd13m0s1", ["-ft"]),
     "F": ('<operator name="F" J="0"/>', "sd13m0s1", []),
+    # projection kappa = 1 (daughter 2M = 2), explicit moments
+    "M1k": ('<operator name="M1" J="1" mu_n="-1.5" mu_p="2.5" gl_n="0.1" gl_p="0.9"/>', "sd22m2s1", ["-u"]),
+    "E2k": ('<operator name="E2" J="2" en="0.6" ep="1.4"/>', "sd22m2s1", ["-w"]),
+    # beta plus from the sd 1n+3p states to the sd 2n+2p ones
+    "GT+": ('<operator name="GT+" J="1"/>', "sd22m0s1", ["-ft"], "sd13m0s1"),
 }
 
 
@@ -289,8 +295,9 @@ def em_case(work: str, manifest: dict) -> None:
         arrays[name + "_EE"] = np.fromfile(os.path.join(work, name + ".EE"), np.uint8)
         entry[name] = {"states": re.findall(r"<state [^>]*>\s*<wavefunction[^>]*/>\s*</state>",
                                             open(xmls[name]).read())}
-    parent = EM_SYSTEMS[0][0]
-    for run, (op, daughter, flags) in EM_RUNS.items():
+    for run, spec in EM_RUNS.items():
+        op, daughter, flags = spec[:3]
+        parent = spec[3] if len(spec) > 3 else EM_SYSTEMS[0][0]
         xin = os.path.join(work, f"em_{run}.xml")
         open(xin, "w").write(open(xmls[parent]).read().replace("</cosmo>", op + "\n</cosmo>", 1))
         xout = os.path.join(work, f"em_{run}.out.xml")
@@ -301,7 +308,7 @@ def em_case(work: str, manifest: dict) -> None:
             subprocess.run(cmd, cwd=work, stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
         out = open(xout).read()
         entry["runs"][run] = {
-            "operator": op, "daughter": daughter, "flags": flags,
+            "operator": op, "daughter": daughter, "flags": flags, "parent": parent,
             "operator_out": re.search(r"<operator [^>]*/>", out).group(0),
             "states": re.findall(r"<state [^>]*>.*?</state>", out, re.S)}
     manifest["em_sd22"] = entry

@@ -2,7 +2,8 @@
 xmlshell/XSHLEMB.cpp): the oracle's one-body operators, overlaps and B values
 against the <transition>/<moment> nodes the reference XSHLEMB wrote for a
 parent sd 2n+2p system (E2, E2 with radial functions positive at infinity,
-M1 with the default moments) and, for GT- and F, a daughter sd 1n+3p system
+M1 with the default moments; E2 and M1 to the 2M = 2 states, kappa = 1), for
+GT- and F a daughter sd 1n+3p system, and GT+ from that system back
 (tests/golden/make_golden.py, em_case), from the reference's own
 eigenvectors (.EE files) and <state> nodes; the library's operator terms
 against the oracle's; on the GPU the amplitudes against the oracle's and the
@@ -111,13 +112,17 @@ def _flags(run):
     return tuple(manifest()[CASE]["runs"][run]["flags"])
 
 
-RUNS = ("E2", "E2p", "M1", "GT-", "F")
+RUNS = ("E2", "E2p", "M1", "GT-", "F", "M1k", "E2k", "GT+")
+
+
+def _parent(s, run):
+    return s[manifest()[CASE]["runs"][run].get("parent", "sd22m0s1")]
 
 
 @pytest.mark.parametrize("run", RUNS)
 def test_oracle_transitions_match_reference(tmp_path, run):
     s = _systems(str(tmp_path))
-    parent = s["sd22m0s1"]
+    parent = _parent(s, run)
     d = manifest()[CASE]["runs"][run]["daughter"]
     daughter = s[d] if d else parent
     op = _op(run)
@@ -135,7 +140,7 @@ def test_library_terms_match_oracle(tmp_path, run):
     """The library's host operator construction against the oracle's, term by term."""
     import cosmo_gb300 as cg
     s = _systems(str(tmp_path))
-    parent = s["sd22m0s1"]
+    parent = _parent(s, run)
     xml = os.path.join(str(tmp_path), "op.xml")
     op_node = manifest()[CASE]["runs"][run]["operator"]
     open(xml, "w").write(open(parent["xml"]).read().replace("</cosmo>", op_node + "\n</cosmo>", 1))
@@ -165,7 +170,7 @@ def test_oracle_radial_and_6j_known_values():
 def test_gpu_transition_amplitudes_and_tool(gpu_available, tmp_path, run):
     import cosmo_gb300 as cg
     s = _systems(str(tmp_path))
-    parent = s["sd22m0s1"]
+    parent = _parent(s, run)
     d = manifest()[CASE]["runs"][run]["daughter"]
     daughter = s[d] if d else parent
     op = _op(run)
