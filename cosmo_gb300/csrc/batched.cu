@@ -64,13 +64,14 @@ __global__ void k_dense_fill(int n, uint64_t r0, const uint64_t* __restrict__ rp
 // ------------------------------------------------ batched Jacobi eigensolver
 // One CTA per matrix: A (k x k, symmetric, FP64 in, ld kJac) -> eigenvalues
 // ascending w[0..k) and eigenvectors Z (column j of the k x k block, ld kJac),
-// computed in R (FP64 here: off-diagonal norm down to 1e-15 of the Frobenius
-// norm; an FP32 Jacobi for the FP32 phase measured 0.43 instead of 1.08 ms
-// per launch but its Ritz vectors, off by ~eps32 |S| / gap, kept the phase
-// from reaching its 1e-4 residuals: 300 instead of 133 iterations).  Cyclic
-// Jacobi with the round-robin ordering: each round applies k/2 disjoint
-// rotations at once, skipping those whose |a_pq| is below 1e-17 (FP32: 1e-7)
-// of sqrt|a_pp a_qq|; at most 40 sweeps.
+// computed in R: FP64 (off-diagonal norm down to 1e-12 of the Frobenius norm)
+// or FP32 (1e-6).  FP32 vectors alone, off by ~eps32 |S| / gap, kept the
+// FP32 Davidson phase from reaching its 1e-4 residuals (300 instead of 133
+// iterations), so that phase runs the FP32 Jacobi and then the FP64 one from
+// its vectors (re-orthonormalized: ortho), which leaves the FP64 pipe only
+// one or two sweeps.  Cyclic Jacobi with the round-robin ordering: each round
+// applies k/2 disjoint rotations at once, skipping those whose |a_pq| is
+// below 1e-17 (FP32: 1e-7) of sqrt|a_pp a_qq|; at most 40 sweeps.
 template <class R>
 constexpr size_t jac_smem() {
   return (size_t(3) * kJac * (kJac + 1) + 256 + kJac) * sizeof(R) + (2 * kJac + 8) * sizeof(int);
@@ -80,7 +81,8 @@ constexpr size_t jac_smem() {
 // previous step's projected matrix, whose eigenvectors Zout still holds; the
 // sweeps start from A' = P^T A P, P = diag(Z_prev, I), whose leading block is
 // already diagonal, with Z = P, so only the coupling to the newest rows is
-// left to rotate away.
+// left to rotate away.  kprev = k takes Zout as approximate eigenvectors of
+// the whole matrix (from the FP32 solve of the same A).
 template <class R>
 __global__ void __launch_bounds__(256) k_bjacobi(const double* __restrict__ Ain, const int* __restrict__ kdim,
                                                  int kconst, double* __restrict__ w, double* Zout,
