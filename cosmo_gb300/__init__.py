@@ -141,6 +141,7 @@ _SIGS = {
     "cg_sf_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P]),
     "cg_xshlsf": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
+    "cg_dense_eigensolve": (C.c_int32, [_P, _P, _P]),
     "cg_transition_terms": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, _P, _P, _P,
                                         C.c_int32, C.POINTER(C.c_int32)]),
     "cg_onebody_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, _P, _P, C.c_int32, _P]),
@@ -473,6 +474,14 @@ class Hamiltonian:
         d = np.zeros(self.n)
         _check(lib().cg_hamiltonian_diagonal(self._h, _ptr(d)))
         return d
+
+    def dense_eigensolve(self, want_vectors: bool = True):
+        """Every eigenpair of the stored matrix by exact FP64 diagonalization
+        (the reference DXHV's path for small dimensions): (eig, vecs[n, n])."""
+        eig = np.zeros(max(self.n, 1))
+        vecs = np.zeros((self.n, self.n)) if want_vectors else None
+        _check(lib().cg_dense_eigensolve(self._h, _ptr(eig), _ptr(vecs) if want_vectors else None))
+        return eig[:self.n], vecs
 
     def upper_rows(self, row0: int = 0, nrows: int | None = None):
         nrows = self.n - row0 if nrows is None else nrows

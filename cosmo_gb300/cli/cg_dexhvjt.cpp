@@ -8,8 +8,10 @@
 // (in place unless -o).  Default: stored FP32 (hi + lo) matrix and the mixed
 // solve (resid <= 1e-5); --fp64: FP64 matrix and the reference's FP64 control
 // flow (block = states, limit states + 20); --virtual: on-the-fly product
-// (nothing stored); --mbs: also write <system>.mbs.  -l (the reference's Eigen
-// limit) is accepted and ignored: every size goes through Davidson.
+// (nothing stored); --mbs: also write <system>.mbs.  -l limit (default 1000,
+// 0: never): a stored matrix of at most that dimension is diagonalized
+// exactly in FP64 instead, and the .EE file then holds every state, as the
+// reference's DXHV writes it (include/xsm/DEXHVcsb.cxx:80-110).
 #include <vector>
 
 #include "cli.h"
@@ -37,6 +39,29 @@ int main(int argc, char** argv) {
   std::fprintf(stderr, "dimension %llu\n", (unsigned long long)n);
   if (a.has("--mbs")) cli::check(cg_basis_write_mbs(b, (sys + ".mbs").c_str()), "write .mbs");
   if (uint64_t(nst) > n) nst = int(n);
+  const int limit = a.geti("-l", 1000);
+  if (!virt && limit > 0 && n <= uint64_t(limit) && n > 0) {
+    // exact diagonalization: every state, FP64 matrix
+    std::fprintf(stderr, "Matrix is small for davidson. Using exact diagonalization\n");
+    cg_hamiltonian* h;
+    cli::check(cg_hamiltonian_build(p, b, CG_PREC_FP64, &h), "H");
+    std::vector<double> E(n), Z(n), V(size_t(n) * n);
+    cli::check(cg_dense_eigensolve(h, E.data(), V.data()), "exact diagonalization");
+    for (int k = 0; k < nst; ++k) std::printf("%.10f ", E[k]);
+    std::printf("\n");
+    const std::string ee = sys + ".HH.EE";
+    cli::check(cg_write_ee(ee.c_str(), int32_t(n), n, E.data(), Z.data(), Z.data(), V.data()), "write .EE");
+    int32_t added = 0;
+    const std::string out = a.gets("-o", "");
+    cli::check(cg_xshljt(xml, want.empty() ? nullptr : want.c_str(), ee.c_str(), nst,
+                         out.empty() ? nullptr : out.c_str(), &added),
+               "xshljt");
+    std::fprintf(stderr, "%d states recorded\n", added);
+    cg_hamiltonian_destroy(h);
+    cg_basis_destroy(b);
+    cg_problem_destroy(p);
+    return 0;
+  }
   const int prec = fp64 ? CG_PREC_FP64 : CG_PREC_FP32;
   cg_hamiltonian* h;
   cli::check(virt ? cg_hamiltonian_build_virtual(p, b, prec, &h) : cg_hamiltonian_build(p, b, prec, &h), "H");

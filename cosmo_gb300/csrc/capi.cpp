@@ -13,6 +13,7 @@
 
 #include "cosmo_gb300.h"
 #include "davidson.h"
+#include "dense.h"
 #include "device.h"
 #include "model.h"
 #include "batched.h"
@@ -878,6 +879,34 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
 }
 
 // ------------------------------------------------------------- file I/O
+cg_status cg_dense_eigensolve(const cg_hamiltonian* h, double* eig, double* vecs) {
+  return guard([&] {
+    CG_NOT_NULL(h);
+    CG_NOT_NULL(eig);
+    if (h->h.virt) throw cg::Error(CG_ERR_UNSUPPORTED, "exact diagonalization needs a stored matrix");
+    const uint64_t n = h->h.n;
+    if (n > 8192) throw cg::Error(CG_ERR_ARG, "exact diagonalization takes at most 8192 states");
+    if (n == 0) return;
+    same_device(h->h.device);
+    std::vector<uint64_t> rp(n + 1);
+    cg::hamiltonian_upper_rows(h->h, 0, n, rp.data(), nullptr, nullptr);
+    std::vector<uint32_t> c(rp[n]);
+    std::vector<double> v(rp[n]);
+    cg::hamiltonian_upper_rows(h->h, 0, n, rp.data(), c.data(), v.data());
+    std::vector<double> a(n * n, 0.0), w, z;
+    for (uint64_t r = 0; r < n; ++r)
+      for (uint64_t k = rp[r]; k < rp[r + 1]; ++k) {
+        a[r * n + c[k]] = v[k];
+        a[uint64_t(c[k]) * n + r] = v[k];
+      }
+    cg::sym_eig(int(n), a, w, z);
+    for (uint64_t k = 0; k < n; ++k) eig[k] = w[k];
+    if (vecs)
+      for (uint64_t k = 0; k < n; ++k)
+        for (uint64_t i = 0; i < n; ++i) vecs[k * n + i] = z[i * n + k];
+  });
+}
+
 cg_status cg_write_ee(const char* path, int32_t nstates, uint64_t n, const double* eig, const double* de,
                       const double* resid, const double* vecs) {
   return guard([&] {

@@ -437,6 +437,16 @@ cg_status cg_xshlemb(const char* parent_xml, const char* parent_system, const ch
 cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* ee_path, int32_t nstates,
                     const char* xml_out, int32_t* n_added);
 
+/* Exact diagonalization of a small stored matrix: every eigenpair of the
+ * full symmetric matrix in FP64, ascending (eig: n values; vecs: n vectors of
+ * n, state k at vecs + k*n, or NULL).  The path the reference's DXHV takes
+ * instead of Davidson when the dimension is at most its limit
+ * (include/xsm/DEXHVcsb.cxx:80-110, Eigen's SelfAdjointEigenSolver; here the
+ * Householder + implicit QL solver of the Davidson's projected problems on
+ * the host).  Stored matrices only (CG_ERR_UNSUPPORTED on the fly), n <= 8192
+ * (CG_ERR_ARG above); eigenvector signs are the solver's own. */
+cg_status cg_dense_eigensolve(const cg_hamiltonian* h, double* eig, double* vecs);
+
 /* ------------------------------------------------------------ file I/O */
 /* .EE eigenpair file: uint32 count, then per state double E, dE, resid,
  * uint64 n, double v[n] (Davidson::Save, include/kdav/cdavidson.cpp:327-368). */

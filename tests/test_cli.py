@@ -72,3 +72,31 @@ def test_cli_pipeline(gpu_available, tmp_path):
     r = _run([os.path.join(BIN, "cg_xshljt"), "out.xml", "-n", "5", "-e", name + ".HH.EE"], work)
     assert r.returncode == 0, r.stderr
     assert len(re.findall(r"<state ", open(os.path.join(work, "out.xml")).read())) == len(ref_states)
+
+
+@pytest.mark.gpu
+def test_cli_exact_path(gpu_available, tmp_path):
+    """cg_dexhvjt at or below the -l limit (default 1000) diagonalizes exactly
+    and writes every state into the .EE file, as the reference's DXHV does
+    (include/xsm/DEXHVcsb.cxx:80-110); -l 0 keeps Davidson."""
+    name = "sd22m0s1"
+    m = manifest()[name]
+    work = str(tmp_path)
+    xml = synthetic_xml(name, work)
+    r = _run([os.path.join(BIN, "cg_dexhvjt"), xml, "-n", "5", "-o", "out.xml"], work)
+    assert r.returncode == 0, r.stderr
+    assert "exact diagonalization" in r.stderr
+    E, D, R, V = cg.read_ee(os.path.join(work, name + ".HH.EE"))
+    assert len(E) == m["n"] and V.shape == (m["n"], m["n"])
+    assert np.all(D == 0) and np.all(R == 0)
+    np.testing.assert_allclose(E[:10], m["ref_eig"][:10], rtol=0, atol=1e-7)
+    assert np.all(np.diff(E) >= 0)
+    txt = open(os.path.join(work, "out.xml")).read()
+    states = [dict(re.findall(r'(\w+)="([^"]*)"', x)) for x in re.findall(r"<state ([^>]*)>", txt)]
+    assert 0 < len(states) <= 5
+    r = _run([os.path.join(BIN, "cg_dexhvjt"), xml, "-n", "5", "-l", "0", "-o", "out2.xml"], work)
+    assert r.returncode == 0, r.stderr
+    assert "exact diagonalization" not in r.stderr
+    E2, _, R2, _ = cg.read_ee(os.path.join(work, name + ".HH.EE"))
+    assert len(E2) == 5 and np.all(R2 <= 1e-5)
+    np.testing.assert_allclose(E2, E[:5], rtol=0, atol=1e-4)

@@ -79,3 +79,22 @@ def test_edge_tiny_spectra(gpu_available, tmp_path, key):
         # that default is not what this checks
         r = cg.davidson_diagonalization(h, n if n <= 16 else 16, precision=prec, tol_resid=1e-7, lim=64)
         np.testing.assert_allclose(r.eig, exact[:len(r.eig)], rtol=0, atol=1e-8 * max(1.0, np.abs(exact).max()))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", ["one", "three", "fp_one_each"])
+def test_exact_diagonalization(gpu_available, tmp_path, key):
+    """cg_dense_eigensolve (the reference DXHV's path for small dimensions):
+    every eigenvalue of the stored matrix, FP64 and FP32 (hi + lo) storage,
+    against the dense spectrum of the oracle's matrix; eigenvectors
+    orthonormal with H v = E v."""
+    import cosmo_gb300 as cg
+    p, z, H = _oracle(str(tmp_path), key)
+    exact = np.linalg.eigvalsh(H)
+    b = cg.ManyBodyStates(p)
+    for prec in (cg.CG_PREC_FP64, cg.CG_PREC_FP32):
+        h = cg.Hamiltonian(p, b, prec)
+        eig, vecs = h.dense_eigensolve()
+        np.testing.assert_allclose(eig, exact, rtol=0, atol=1e-10 * max(1.0, np.abs(exact).max()))
+        assert np.abs(vecs @ vecs.T - np.eye(len(z))).max() < 1e-12
+        assert np.abs(H @ vecs.T - vecs.T * eig[None, :]).max() < 1e-10 * max(1.0, np.abs(exact).max())
