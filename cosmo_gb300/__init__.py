@@ -142,6 +142,8 @@ _SIGS = {
     "cg_xshlsf": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "cg_xshljt": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)]),
     "cg_dense_eigensolve": (C.c_int32, [_P, _P, _P]),
+    "cg_occupations": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "cg_xshlao": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p]),
     "cg_transition_terms": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, _P, _P, _P,
                                         C.c_int32, C.POINTER(C.c_int32)]),
     "cg_onebody_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, _P, _P, C.c_int32, _P]),
@@ -314,6 +316,22 @@ def xshlemb(parent_xml: str, out: str | None = None, daughter_xml: str | None = 
              | (CG_EMB_PHASE_INFINITY if phase_infinity else 0))
     _check(lib().cg_xshlemb(enc(parent_xml), enc(parent_system), enc(daughter_xml), enc(daughter_system), enc(out),
                             flags, enc(operator)))
+
+
+def occupations(basis: "ManyBodyStates", vecs) -> np.ndarray:
+    """occ[k, s] = <psi_k| n_s |psi_k> for the rows of vecs (XSHLAO's
+    SM::occupation), on the GPU."""
+    v = np.ascontiguousarray(np.asarray(vecs, dtype=np.float64).reshape(-1, basis.n))
+    occ = np.zeros((v.shape[0], basis.n_sps))
+    _check(lib().cg_occupations(basis._h, _ptr(v), v.shape[0], _ptr(occ)))
+    return occ
+
+
+def xshlao(xml: str, out: str | None = None, system: str | None = None) -> None:
+    """The XSHLAO tool: orbital occupation numbers of the system's <state>s
+    as <occupation> nodes, into `out` (the input XML when None)."""
+    enc = lambda x: x.encode() if x is not None else None  # noqa: E731
+    _check(lib().cg_xshlao(enc(xml), enc(system), enc(out)))
 
 
 def jj_spin(x: float, two_m: int) -> int:

@@ -879,6 +879,25 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
 }
 
 // ------------------------------------------------------------- file I/O
+cg_status cg_occupations(const cg_basis* b, const double* vecs, int32_t nst, double* occ) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(occ);
+    if (nst < 0) throw cg::Error(CG_ERR_ARG, "negative state count");
+    if (nst) CG_NOT_NULL(vecs);
+    same_device(b->b.device);
+    cg::occupations(b->b, vecs, nst, occ);
+  });
+}
+
+cg_status cg_xshlao(const char* xml_path, const char* system_name, const char* out_xml) {
+  return guard([&] {
+    CG_NOT_NULL(xml_path);
+    require_device();
+    cg::xshlao(xml_path, system_name ? system_name : "", out_xml ? out_xml : "");
+  });
+}
+
 cg_status cg_dense_eigensolve(const cg_hamiltonian* h, double* eig, double* vecs) {
   return guard([&] {
     CG_NOT_NULL(h);

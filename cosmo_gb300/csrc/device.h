@@ -125,6 +125,8 @@ void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, in
 struct OneBodyTerm;
 void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                         const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp);
+// occ[k * ns + s] = <psi_k| n_s |psi_k> for nst host vectors (sf.cu)
+void occupations(const Basis& b, const double* v, int nst, double* occ);
 // twice the spin from <J-J+> and twice the projection; -1 if not (half-)integer within 0.1
 int jj_spin(double x, int two_m);
 void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);

@@ -4,7 +4,7 @@
 // PPMatrix::OverlapNH and the one-body operator a_s (include/sm/
 // PPMatrix.cxx:275-302); and transition amplitudes <D_q| sum v a+_f a_i |P_p>
 // of XSHLEMB's electromagnetic and beta operators (xmlshell/XSHLEMB.cpp:
-// 248-270).
+// 248-270); and the occupation numbers of XSHLAO.
 //
 // The reference applies a_s to every parent determinant (SM::Annihilation,
 // include/sm/operators.cxx:121-150: phase of the number of states below s),
@@ -184,7 +184,45 @@ __global__ void k_onebody_amplitudes(ObArgs a, double* __restrict__ part, int* _
   }
 }
 
+// Occupation numbers <psi| n_s |psi> = sum over determinants holding s of
+// psi_D^2 (SM::occupation, include/sm/occupation.cxx:55-70): one thread per
+// determinant adds psi_D^2 to a per-CTA shared row of s.p. states for each of
+// its set bits; the CTA rows are summed on the host.
+__global__ void k_occupations(uint64_t n, const uint64_t* __restrict__ state, const double* __restrict__ psi, int ns,
+                              double* __restrict__ part) {
+  __shared__ double occ[64];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) occ[i] = 0.0;
+  __syncthreads();
+  for (uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; row < n;
+       row += uint64_t(gridDim.x) * blockDim.x) {
+    const double p = psi[row] * psi[row];
+    for (uint64_t D = state[row]; D; D &= D - 1) atomicAdd(&occ[__ffsll((long long)D) - 1], p);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) part[size_t(blockIdx.x) * 64 + i] = occ[i];
+}
+
 }  // namespace
+
+void occupations(const Basis& b, const double* v, int nst, double* occ) {
+  const int ns = b.ns;
+  for (size_t i = 0; i < size_t(nst) * ns; ++i) occ[i] = 0.0;
+  if (b.n == 0 || nst < 1) return;
+  cudaStream_t st = b.stream;
+  const unsigned gx = unsigned(std::min<uint64_t>((b.n + 255) / 256, 152ull * 4));
+  DBuf<double> psi(b.n), part(size_t(gx) * 64);
+  std::vector<double> h(part.n);
+  for (int k = 0; k < nst; ++k) {
+    psi.upload(v + uint64_t(k) * b.n, b.n, st);
+    k_occupations<<<gx, 256, 0, st>>>(b.n, b.state.p, psi.p, ns, part.p);
+    CG_CUDA(cudaGetLastError());
+    count_launch();
+    CG_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+    CG_CUDA(cudaStreamSynchronize(st));
+    for (unsigned g = 0; g < gx; ++g)
+      for (int s = 0; s < ns; ++s) occ[size_t(k) * ns + s] += h[size_t(g) * 64 + s];
+  }
+}
 
 void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                         const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp) {

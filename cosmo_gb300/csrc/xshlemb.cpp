@@ -206,4 +206,48 @@ void xshlemb(const std::string& pxml, const std::string& psys_name, const std::s
   of << text;
 }
 
+// XSHLAO (xmlshell/XSHLAO.cpp:22-101): occupation numbers of every orbital,
+// neutrons and protons apart, for every <state> of the system, written as
+// <occupation name N Z/> children of the states (orbitals in the document
+// order of the valence space, as the reference walks them).
+void xshlao(const std::string& xml, const std::string& system_name, const std::string& out_xml) {
+  const System sys = load_system(xml, system_name);
+  const XmlNode root = parse_xml_file(xml);
+  const XmlNode* vs = root.child("valencespace");
+  if (!vs) throw Error(CG_ERR_PARSE, "no <valencespace>");
+  const std::vector<StateRecord> st = read_states(xml, sys.name);
+  Basis b;
+  basis_build(sys, b);
+  const int nst = int(st.size()), ns = int(sys.sps.size());
+  std::vector<double> v;
+  for (const StateRecord& r : st) {
+    const auto x = read_vector(r.file, dir_of(xml), r.id, b.n, nullptr);
+    v.insert(v.end(), x.begin(), x.end());
+  }
+  std::vector<double> occ(size_t(nst) * ns);
+  occupations(b, v.data(), nst, occ.data());
+  std::vector<std::vector<std::string>> front(nst), back(nst);
+  for (int k = 0; k < nst; ++k) {
+    std::cout << st[k].name << " E=" << st[k].e_text << "\n";
+    for (int o = 0; o < vs->count("orbital"); ++o) {
+      const XmlNode* orb = vs->child("orbital", o);
+      const std::string name = orb->attr("name") ? *orb->attr("name") : std::string();
+      const int level = orb->attr("index") ? std::atoi(orb->attr("index")->c_str()) - 1 : o;
+      double occN = 0.0, occZ = 0.0;
+      for (int i = 0; i < ns; ++i)
+        if (sys.sps[i].level == level) (sys.sps[i].tz2 == 1 ? occN : occZ) += occ[size_t(k) * ns + i];
+      back[k].push_back("<occupation name=\"" + name + "\" N=\"" + num_text(occN) + "\" Z=\"" + num_text(occZ) + "\"/>");
+      std::cout << "  " << name << " N=" << occN << " Z=" << occZ << "\n";
+    }
+  }
+  std::ifstream in(xml, std::ios::binary);
+  std::stringstream ss;
+  ss << in.rdbuf();
+  const std::string text = xml_state_children(ss.str(), sys.name, front, back);
+  const std::string dst = out_xml.empty() ? xml : out_xml;
+  std::ofstream of(dst, std::ios::binary);
+  if (!of) throw Error(CG_ERR_IO, "cannot write " + dst);
+  of << text;
+}
+
 }  // namespace cg

@@ -90,6 +90,10 @@ struct XshlembOptions {
 // *added: the M-operator attributes that were absent and took their defaults.
 TransitionOp read_transition_operator(const XmlNode& root, const std::string& op_name, bool phase_infinity, int* index,
                                       std::vector<std::pair<std::string, std::string>>* added);
+// XSHLAO (xmlshell/XSHLAO.cpp:22-101): orbital occupation numbers of the
+// system's <state>s as <occupation name N Z/> children, into out_xml (the
+// input when empty).
+void xshlao(const std::string& xml, const std::string& system_name, const std::string& out_xml);
 void xshlemb(const std::string& parent_xml, const std::string& parent_system, const std::string& daughter_xml,
              const std::string& daughter_system, const std::string& out_xml, const XshlembOptions& opt);
 

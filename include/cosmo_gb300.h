@@ -437,6 +437,16 @@ cg_status cg_xshlemb(const char* parent_xml, const char* parent_system, const ch
 cg_status cg_xshljt(const char* xml_path, const char* system_name, const char* ee_path, int32_t nstates,
                     const char* xml_out, int32_t* n_added);
 
+/* Occupation numbers <psi_k| n_s |psi_k> of every s.p. state (SM::occupation,
+ * include/sm/occupation.cxx:55-70) for nst host vectors (.EE layout) of a
+ * basis: occ[k * n_sps + s].  On the GPU in FP64. */
+cg_status cg_occupations(const cg_basis* b, const double* vecs, int32_t nst, double* occ);
+/* The XSHLAO tool (xmlshell/XSHLAO.cpp:22-101): per <state> of the system, the
+ * occupation of every orbital of the valence space, neutrons and protons
+ * apart, as <occupation name N Z/> children, written to out_xml (NULL: the
+ * input file); a report on stdout. */
+cg_status cg_xshlao(const char* xml_path, const char* system_name, const char* out_xml);
+
 /* Exact diagonalization of a small stored matrix: every eigenpair of the
  * full symmetric matrix in FP64, ascending (eig: n values; vecs: n vectors of
  * n, state k at vecs + k*n, or NULL).  The path the reference's DXHV takes

@@ -8,7 +8,8 @@ Hermitian2FullOperator for the Fermi operator, include/sm/spherical2sp.cxx:
 664-700, include/sm/cioperators.cxx:244-269), the overlap <D| O |P>
 (PPMatrix::OverlapNH, include/sm/PPMatrix.cxx:275-302, with ActFermiOperator's
 annihilate-then-create phases) and the B values, moments and unit conversions
-the tool writes.  Angular-momentum coefficients and oscillator radial
+the tool writes; and XSHLAO's occupation numbers (SM::occupation,
+include/sm/occupation.cxx:55-70).  Angular-momentum coefficients and oscillator radial
 integrals come from their closed forms (Racah; Lawson, Theory of the Nuclear
 Shell Model, eq. 1.11a) in exact rational arithmetic, rounded once.  Pinned
 against the reference XSHLEMB's own output (tests/golden, em_sd22).
@@ -261,3 +262,14 @@ def transitions(op: dict, P: list, D: list, amp: np.ndarray, A: int = 1, flags=(
         trans.append(tr)
         moms.append(mo)
     return trans, moms
+
+
+def occupations(z: np.ndarray, vecs: np.ndarray, ns: int) -> np.ndarray:
+    """occ[k, s] = sum over the determinants holding s of psi_k^2."""
+    vecs = np.asarray(vecs, dtype=np.float64).reshape(-1, len(z))
+    occ = np.zeros((len(vecs), ns))
+    p = vecs * vecs
+    for col in range(z.shape[1]):
+        for k in range(len(vecs)):
+            occ[k] += np.bincount(z[:, col].astype(np.int64), weights=p[k], minlength=ns)
+    return occ

@@ -311,6 +311,14 @@ def em_case(work: str, manifest: dict) -> None:
             "operator": op, "daughter": daughter, "flags": flags, "parent": parent,
             "operator_out": re.search(r"<operator [^>]*/>", out).group(0),
             "states": re.findall(r"<state [^>]*>.*?</state>", out, re.S)}
+    # occupation numbers (XSHLAO) of the same systems' states
+    entry["xshlao"] = {}
+    for name, _ in EM_SYSTEMS:
+        xout = os.path.join(work, f"ao_{name}.out.xml")
+        with open(os.path.join(work, f"ao_{name}.log"), "w") as log:
+            subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLAO"), xmls[name], "-o", xout], cwd=work,
+                           stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+        entry["xshlao"][name] = re.findall(r"<state [^>]*>.*?</state>", open(xout).read(), re.S)
     manifest["em_sd22"] = entry
     np.savez_compressed(os.path.join(HERE, "em_sd22.npz"), **arrays)
     print("em", {r: sum(s.count("<transition") for s in v["states"]) for r, v in entry["runs"].items()})

@@ -222,3 +222,70 @@ def test_gpu_transition_amplitudes_and_tool(gpu_available, tmp_path, run):
         assert (again.count("<transition"), again.count("<moment")) == ntr
         for st0, st1 in zip(states, re.findall(r"<state [^>]*>.*?</state>", again, re.S)):
             assert re.findall(r"<(?:transition|moment) [^>]*/>", st0) == re.findall(r"<(?:transition|moment) [^>]*/>", st1)
+
+
+def _ao_reference(name):
+    return [[_attrs(o) for o in re.findall(r"<occupation [^>]*/>", st)]
+            for st in manifest()[CASE]["xshlao"][name]]
+
+
+def _ao_records(sysp, occ, orbitals):
+    out = []
+    for k in range(len(occ)):
+        rec = []
+        for oname, level in orbitals:
+            sel = sysp.sps[:, 0] == level
+            rec.append({"name": oname, "N": float(occ[k][sel & (sysp.sps[:, 6] == 1)].sum()),
+                        "Z": float(occ[k][sel & (sysp.sps[:, 6] == -1)].sum())})
+        out.append(rec)
+    return out
+
+
+def _orbitals(xml):
+    import xml.etree.ElementTree as ET
+    return [(o.get("name"), int(o.get("index")) - 1) for o in ET.parse(xml).getroot().find("valencespace")]
+
+
+def _check_ao(name, recs):
+    ref = _ao_reference(name)
+    assert len(recs) == len(ref)
+    for mine, theirs in zip(recs, ref):
+        assert [r["name"] for r in mine] == [a["name"] for a in theirs]
+        for r, a in zip(mine, theirs):
+            assert _close(r["N"], float(a["N"])) and _close(r["Z"], float(a["Z"])), (name, r, a)
+
+
+@pytest.mark.parametrize("name", ["sd22m0s1", "sd13m0s1", "sd22m2s1"])
+def test_oracle_occupations_match_reference(tmp_path, name):
+    """XSHLAO: the oracle's occupation numbers of the reference's vectors
+    against the <occupation> nodes the reference XSHLAO wrote."""
+    s = _systems(str(tmp_path))[name]
+    occ = TR.occupations(s["z"], np.array([x["vec"] for x in s["states"]]), len(s["sys"].sps))
+    _check_ao(name, _ao_records(s["sys"], occ, _orbitals(s["xml"])))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["sd22m0s1", "sd13m0s1"])
+def test_gpu_occupations_and_xshlao(gpu_available, tmp_path, name):
+    import subprocess
+    import cosmo_gb300 as cg
+    s = _systems(str(tmp_path))[name]
+    b = cg.ManyBodyStates(cg.Problem(s["xml"]))
+    vecs = np.array([x["vec"] for x in s["states"]])
+    occ = cg.occupations(b, vecs)
+    assert np.abs(occ - TR.occupations(s["z"], vecs, len(s["sys"].sps))).max() <= 1e-12
+    # the tool and its command line on the XML with the reference's <state> nodes
+    txt = open(s["xml"]).read().replace("</system>", "".join(manifest()[CASE][name]["states"]) + "</system>", 1)
+    open(s["xml"], "w").write(txt)
+    s["ee"].tofile(os.path.join(str(tmp_path), name + ".EE"))
+    out = os.path.join(str(tmp_path), "ao.xml")
+    cg.xshlao(s["xml"], out)
+    states = re.findall(r"<state [^>]*>.*?</state>", open(out).read(), re.S)
+    recs = [[{k: (float(v) if k in ("N", "Z") else v) for k, v in _attrs(o).items()}
+             for o in re.findall(r"<occupation [^>]*/>", st)] for st in states]
+    _check_ao(name, recs)
+    exe = os.path.join(os.path.dirname(cg.__file__), "bin", "cg_xshlao")
+    r = subprocess.run([exe, s["xml"], "-o", os.path.join(str(tmp_path), "ao2.xml")], cwd=str(tmp_path),
+                       capture_output=True, text=True, stdin=subprocess.DEVNULL)
+    assert r.returncode == 0, r.stderr
+    assert open(os.path.join(str(tmp_path), "ao2.xml")).read() == open(out).read()
