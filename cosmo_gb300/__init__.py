@@ -144,6 +144,7 @@ _SIGS = {
     "cg_dense_eigensolve": (C.c_int32, [_P, _P, _P]),
     "cg_occupations": (C.c_int32, [_P, _P, C.c_int32, _P]),
     "cg_xshlao": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p]),
+    "cg_xlevels": (C.c_int32, [C.POINTER(C.c_char_p), C.c_int32, C.c_char_p]),
     "cg_transition_terms": (C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, _P, _P, _P,
                                         C.c_int32, C.POINTER(C.c_int32)]),
     "cg_onebody_amplitudes": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, _P, _P, C.c_int32, _P]),
@@ -332,6 +333,13 @@ def xshlao(xml: str, out: str | None = None, system: str | None = None) -> None:
     as <occupation> nodes, into `out` (the input XML when None)."""
     enc = lambda x: x.encode() if x is not None else None  # noqa: E731
     _check(lib().cg_xshlao(enc(xml), enc(system), enc(out)))
+
+
+def xlevels(files, out: str | None = None) -> None:
+    """The Xlevels tool: the levels of the <state>s of the XML files organized
+    together and listed on stdout (host only)."""
+    arr = (C.c_char_p * len(files))(*[f.encode() for f in files])
+    _check(lib().cg_xlevels(arr, len(files), out.encode() if out else None))
 
 
 def jj_spin(x: float, two_m: int) -> int:

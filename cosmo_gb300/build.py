@@ -84,7 +84,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
 
 CLI_DIR = os.path.join(PKG, "cli")
 BIN_DIR = os.path.join(PKG, "bin")
-CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb", "cg_xshlao"]
+CLIS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb", "cg_xshlao", "cg_xlevels"]
 
 
 def build_cli() -> list[str]:

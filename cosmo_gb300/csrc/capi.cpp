@@ -898,6 +898,21 @@ cg_status cg_xshlao(const char* xml_path, const char* system_name, const char* o
   });
 }
 
+cg_status cg_xlevels(const char* const* files, int32_t nfiles, const char* out_xml) {
+  return guard([&] {
+    if (nfiles < 0) throw cg::Error(CG_ERR_ARG, "negative file count");
+    if (nfiles) CG_NOT_NULL(files);
+    std::vector<std::string> f;
+    for (int32_t i = 0; i < nfiles; ++i) {
+      CG_NOT_NULL(files[i]);
+      f.emplace_back(files[i]);
+    }
+    const std::string out = cg::xlevels(f, out_xml ? out_xml : "");
+    std::fwrite(out.data(), 1, out.size(), stdout);
+    std::fflush(stdout);
+  });
+}
+
 cg_status cg_dense_eigensolve(const cg_hamiltonian* h, double* eig, double* vecs) {
   return guard([&] {
     CG_NOT_NULL(h);

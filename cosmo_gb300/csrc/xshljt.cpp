@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <map>
 #include <sstream>
 
 #include "device.h"
@@ -108,6 +109,60 @@ std::string attrs_text(const Attrs& a) {
   std::string t;
   for (auto& kv : a) t += " " + kv.first + "=\"" + kv.second + "\"";
   return t;
+}
+
+// The <state> children of a system body (attributes, wavefunctions and the
+// other children as written), removed from the body.
+std::vector<StateNode> take_states(std::string& body) {
+  std::vector<StateNode> states;
+  std::string kept;
+  size_t q = 0;
+  while (true) {
+    size_t st = find_tag(body, "state", q, body.size());
+    if (st == std::string::npos) {
+      kept += body.substr(q);
+      break;
+    }
+    size_t ls = st;
+    while (ls > q && (body[ls - 1] == ' ' || body[ls - 1] == '\t')) --ls;
+    if (ls > q && body[ls - 1] == '\n') --ls;
+    kept += body.substr(q, ls - q);
+    const size_t e = tag_end(body, st);
+    StateNode sn;
+    sn.attrs = parse_attrs(body, st + 1, e);
+    size_t next = e + 1;
+    if (body[e - 1] != '/') {
+      size_t close = body.find("</state>", e);
+      if (close == std::string::npos) throw Error(CG_ERR_PARSE, "xml: </state> missing");
+      size_t w = e + 1;
+      while (true) {
+        const size_t c0 = body.find('<', w);
+        if (c0 == std::string::npos || c0 >= close) break;
+        const size_t ce = tag_end(body, c0);
+        size_t n0 = c0 + 1;
+        while (n0 < ce && !is_space(body[n0]) && body[n0] != '/' && body[n0] != '>') ++n0;
+        const std::string name = body.substr(c0 + 1, n0 - c0 - 1);
+        size_t end = ce + 1;  // past the child element
+        if (body[ce - 1] != '/' && name[0] != '!' && name[0] != '?') {
+          const size_t cl = body.find("</" + name + ">", ce);
+          if (cl == std::string::npos || cl > close) throw Error(CG_ERR_PARSE, "xml: </" + name + "> missing");
+          end = cl + name.size() + 3;
+        }
+        if (name == "wavefunction") {
+          sn.wfs.push_back(parse_attrs(body, c0 + 1, ce));
+          sn.kids.emplace_back();
+        } else {
+          sn.kids.push_back(body.substr(c0, end - c0));
+        }
+        w = end;
+      }
+      next = close + 8;
+    }
+    states.push_back(std::move(sn));
+    q = next;
+  }
+  body = kept;
+  return states;
 }
 
 }  // namespace
@@ -215,6 +270,98 @@ std::string xml_append_attrs(const std::string& text, const std::string& tag, in
   return text.substr(0, e) + add + text.substr(e);
 }
 
+std::string xlevels(const std::vector<std::string>& files, const std::string& out_xml) {
+  // every state of every <nucleus> (else <system>) element of the files that
+  // holds states (Xlevels includes each such space)
+  std::vector<StateNode> all;
+  for (const std::string& f : files) {
+    std::ifstream in(f, std::ios::binary);
+    if (!in) throw Error(CG_ERR_IO, "cannot open " + f);
+    std::stringstream ss;
+    ss << in.rdbuf();
+    const std::string text = ss.str();
+    std::string tag = find_tag(text, "nucleus", 0, text.size()) != std::string::npos ? "nucleus" : "system";
+    size_t p = 0;
+    while ((p = find_tag(text, tag, p, text.size())) != std::string::npos) {
+      const size_t e = tag_end(text, p);
+      if (text[e - 1] == '/') { p = e; continue; }
+      const size_t close = text.find("</" + tag + ">", e);
+      if (close == std::string::npos) throw Error(CG_ERR_PARSE, "xml: </" + tag + "> missing in " + f);
+      std::string body = text.substr(e + 1, close - e - 1);
+      std::vector<StateNode> st = take_states(body);
+      for (auto& x : st) all.push_back(std::move(x));
+      p = close;
+    }
+  }
+  // OrganizeStates (include/xsm/xState.cxx:197-247): energy order, names
+  // J P (k) per (J, P), Ex from the lowest
+  std::vector<std::pair<double, size_t>> order;
+  for (size_t i = 0; i < all.size(); ++i) {
+    const std::string* E = get(all[i].attrs, "E");
+    order.emplace_back(E ? std::atof(E->c_str()) : 0.0, i);
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [](const std::pair<double, size_t>& a, const std::pair<double, size_t>& b) { return a < b; });
+  std::map<std::pair<std::string, std::string>, int> count;
+  std::string listing, xml;
+  std::vector<double> diff;
+  for (auto& o : order) {
+    StateNode& sn = all[o.second];
+    const std::string* J = get(sn.attrs, "J");
+    const std::string* P = get(sn.attrs, "P");
+    std::string j = J ? *J : "??", pp = P ? *P : "?";
+    const int k = ++count[{j, pp}];
+    update(sn.attrs, "name", j + pp.substr(0, 1) + "(" + std::to_string(k) + ")");
+    const double ex = o.first - order.front().first;
+    update(sn.attrs, "Ex", num_str(ex));
+    // ListStates (xmlshell/Xlevels.cpp:22-58): name T=.. Ex E [experimental Ex]
+    const std::string* T = get(sn.attrs, "T");
+    listing += *get(sn.attrs, "name") + " T=" + (T ? *T : std::string("???")) + " " + *get(sn.attrs, "Ex") + " " +
+               num_str(o.first);
+    bool data = false;
+    for (const std::string& kid : sn.kids) {
+      if (kid.compare(0, 5, "<data") || (kid.size() > 5 && !is_space(kid[5]) && kid[5] != '>' && kid[5] != '/'))
+        continue;
+      const Attrs da = parse_attrs(kid, 1, tag_end(kid, 0));
+      if (const std::string* dx = get(da, "Ex")) {
+        const double exd = std::atof(dx->c_str());
+        listing += " " + num_str(exd);
+        diff.push_back(std::atof(get(sn.attrs, "Ex")->c_str()) - exd);
+        data = true;
+      }
+      break;
+    }
+    (void)data;
+    listing += "\n";
+    xml += "\n\t\t<state" + attrs_text(sn.attrs);
+    if (sn.kids.empty()) {
+      xml += "/>";
+    } else {
+      xml += ">";
+      size_t wi = 0;
+      for (const std::string& kid : sn.kids)
+        xml += "\n\t\t\t" + (kid.empty() ? "<wavefunction" + attrs_text(sn.wfs[wi++]) + "/>" : kid);
+      xml += "\n\t\t</state>";
+    }
+  }
+  if (!diff.empty()) {
+    double mean = 0.0, sig = 0.0;
+    for (double d : diff) {
+      mean += d;
+      sig += d * d;
+    }
+    mean /= double(diff.size());
+    listing += "Experimental data comparison\nMean (average shift) " + num_str(mean) + "\nRMS " +
+               num_str(std::sqrt(sig / double(diff.size()) - mean * mean)) + "\n";
+  }
+  if (!out_xml.empty()) {
+    std::ofstream of(out_xml, std::ios::binary);
+    if (!of) throw Error(CG_ERR_IO, "cannot write " + out_xml);
+    of << "<?xml version=\"1.0\"?>\n<cosmo>\n\t<nucleus>" << xml << "\n\t</nucleus>\n</cosmo>\n";
+  }
+  return listing;
+}
+
 std::string xml_add_states(const std::string& text, const std::string& system_name,
                            const std::vector<NewState>& add) {
   // the system element
@@ -255,56 +402,7 @@ std::string xml_add_states(const std::string& text, const std::string& system_na
     tail = text.substr(after);
   }
   // existing states, removed from the body
-  std::vector<StateNode> states;
-  {
-    std::string kept;
-    size_t q = 0;
-    while (true) {
-      size_t st = find_tag(body, "state", q, body.size());
-      if (st == std::string::npos) {
-        kept += body.substr(q);
-        break;
-      }
-      size_t ls = st;
-      while (ls > q && (body[ls - 1] == ' ' || body[ls - 1] == '\t')) --ls;
-      if (ls > q && body[ls - 1] == '\n') --ls;
-      kept += body.substr(q, ls - q);
-      const size_t e = tag_end(body, st);
-      StateNode sn;
-      sn.attrs = parse_attrs(body, st + 1, e);
-      size_t next = e + 1;
-      if (body[e - 1] != '/') {
-        size_t close = body.find("</state>", e);
-        if (close == std::string::npos) throw Error(CG_ERR_PARSE, "xml: </state> missing");
-        size_t w = e + 1;
-        while (true) {
-          const size_t c0 = body.find('<', w);
-          if (c0 == std::string::npos || c0 >= close) break;
-          const size_t ce = tag_end(body, c0);
-          size_t n0 = c0 + 1;
-          while (n0 < ce && !is_space(body[n0]) && body[n0] != '/' && body[n0] != '>') ++n0;
-          const std::string name = body.substr(c0 + 1, n0 - c0 - 1);
-          size_t end = ce + 1;  // past the child element
-          if (body[ce - 1] != '/' && name[0] != '!' && name[0] != '?') {
-            const size_t cl = body.find("</" + name + ">", ce);
-            if (cl == std::string::npos || cl > close) throw Error(CG_ERR_PARSE, "xml: </" + name + "> missing");
-            end = cl + name.size() + 3;
-          }
-          if (name == "wavefunction") {
-            sn.wfs.push_back(parse_attrs(body, c0 + 1, ce));
-            sn.kids.emplace_back();
-          } else {
-            sn.kids.push_back(body.substr(c0, end - c0));
-          }
-          w = end;
-        }
-        next = close + 8;
-      }
-      states.push_back(std::move(sn));
-      q = next;
-    }
-    body = kept;
-  }
+  std::vector<StateNode> states = take_states(body);
   // AddState: merge into a state with the same J, T and |dE| <= 0.001, else a new node
   for (const NewState& ns : add) {
     StateNode* hit = nullptr;

@@ -90,6 +90,12 @@ struct XshlembOptions {
 // *added: the M-operator attributes that were absent and took their defaults.
 TransitionOp read_transition_operator(const XmlNode& root, const std::string& op_name, bool phase_infinity, int* index,
                                       std::vector<std::pair<std::string, std::string>>* added);
+// Xlevels (xmlshell/Xlevels.cpp:60-134): the <state>s of every space of the
+// files that holds some, organized together (energy order, names J P (k),
+// Ex from the lowest) and listed one per line as "name T=T Ex E [Ex(data)]",
+// with the mean shift and RMS against <data Ex> children when there are any;
+// the organized states written to out_xml when not empty.  Returns the listing.
+std::string xlevels(const std::vector<std::string>& files, const std::string& out_xml);
 // XSHLAO (xmlshell/XSHLAO.cpp:22-101): orbital occupation numbers of the
 // system's <state>s as <occupation name N Z/> children, into out_xml (the
 // input when empty).

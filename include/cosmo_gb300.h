@@ -447,6 +447,14 @@ cg_status cg_occupations(const cg_basis* b, const double* vecs, int32_t nst, dou
  * input file); a report on stdout. */
 cg_status cg_xshlao(const char* xml_path, const char* system_name, const char* out_xml);
 
+/* The Xlevels tool (xmlshell/Xlevels.cpp:60-134): the <state> nodes of every
+ * space (<nucleus>, else <system>) of nfiles XML files organized together
+ * (energy order, names J P (k), Ex from the lowest) and listed on stdout one
+ * per line, "name T=T Ex E" plus the experimental Ex of a <data> child and
+ * the mean shift and RMS; the organized states written to out_xml when not
+ * NULL.  Host only. */
+cg_status cg_xlevels(const char* const* files, int32_t nfiles, const char* out_xml);
+
 /* Exact diagonalization of a small stored matrix: every eigenpair of the
  * full symmetric matrix in FP64, ascending (eig: n values; vecs: n vectors of
  * n, state k at vecs + k*n, or NULL).  The path the reference's DXHV takes

@@ -319,6 +319,20 @@ def em_case(work: str, manifest: dict) -> None:
             subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLAO"), xmls[name], "-o", xout], cwd=work,
                            stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
         entry["xshlao"][name] = re.findall(r"<state [^>]*>.*?</state>", open(xout).read(), re.S)
+    # level listing (Xlevels) of two systems' states, one state with an
+    # experimental <data Ex> child
+    lv = []
+    for k, name in enumerate(("sd22m0s1", "sd22m2s1")):
+        txt = open(xmls[name]).read()
+        if k == 0:
+            st = re.findall(r"<state [^>]*>.*?</state>", txt, re.S)[1]
+            txt = txt.replace(st, st.replace("</state>", '<data Ex="1.5"/>\n</state>'), 1)
+        path = os.path.join(work, f"lv_{name}.xml")
+        open(path, "w").write(txt)
+        lv.append(path)
+    r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "Xlevels")] + lv, cwd=work, stdin=subprocess.DEVNULL,
+                       capture_output=True, text=True, check=True)
+    entry["xlevels"] = {"data_state": 1, "data_ex": "1.5", "lines": r.stdout.splitlines()}
     manifest["em_sd22"] = entry
     np.savez_compressed(os.path.join(HERE, "em_sd22.npz"), **arrays)
     print("em", {r: sum(s.count("<transition") for s in v["states"]) for r, v in entry["runs"].items()})

@@ -14,7 +14,7 @@ import cosmo_gb300 as cg
 from conftest import ROOT, golden, manifest, synthetic_xml
 
 BIN = os.path.join(ROOT, "cosmo_gb300", "bin")
-TOOLS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb", "cg_xshlao"]
+TOOLS = ["cg_dexhvjt", "cg_xsysmbs", "cg_xhhjj", "cg_davidson_vfile", "cg_xshljt", "cg_xshlsf", "cg_xshlemb", "cg_xshlao", "cg_xlevels"]
 
 
 def _run(args, cwd):

@@ -289,3 +289,35 @@ def test_gpu_occupations_and_xshlao(gpu_available, tmp_path, name):
                        capture_output=True, text=True, stdin=subprocess.DEVNULL)
     assert r.returncode == 0, r.stderr
     assert open(os.path.join(str(tmp_path), "ao2.xml")).read() == open(out).read()
+
+
+def test_xlevels_matches_reference(tmp_path, capfd):
+    """Xlevels (host only): the listing of two systems' states, one with an
+    experimental <data Ex>, line for line the reference tool's stdout; the
+    command line and the C ABI give the same; the organized XML holds every
+    state with its new name and Ex."""
+    import subprocess
+    import cosmo_gb300 as cg
+    s = _systems(str(tmp_path))
+    lv = manifest()[CASE]["xlevels"]
+    files = []
+    for k, name in enumerate(("sd22m0s1", "sd22m2s1")):
+        nodes = list(manifest()[CASE][name]["states"])
+        if k == 0:
+            i = lv["data_state"]
+            nodes[i] = nodes[i].replace("</state>", '<data Ex="%s"/>\n</state>' % lv["data_ex"])
+        txt = open(s[name]["xml"]).read().replace("</system>", "".join(nodes) + "</system>", 1)
+        path = os.path.join(str(tmp_path), "lv_" + name + ".xml")
+        open(path, "w").write(txt)
+        files.append(path)
+    exe = os.path.join(os.path.dirname(cg.__file__), "bin", "cg_xlevels")
+    out = os.path.join(str(tmp_path), "levels.xml")
+    r = subprocess.run([exe] + files + ["-o", out], capture_output=True, text=True, stdin=subprocess.DEVNULL)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines() == lv["lines"]
+    cg.xlevels(files)
+    assert capfd.readouterr().out.splitlines() == lv["lines"]
+    organized = re.findall(r"<state [^>]*>", open(out).read())
+    assert len(organized) == sum(len(manifest()[CASE][n]["states"]) for n in ("sd22m0s1", "sd22m2s1"))
+    names = [_attrs(x)["name"] for x in organized]
+    assert names == [ln.split()[0] for ln in lv["lines"][:len(names)]]
