@@ -44,10 +44,10 @@ WORKLOAD = dict(workload="fp-shell 4p+4n M=0, lowest 10 eigenpairs, |dE|<=1e-4 M
                 space="fp", protons=4, neutrons=4, twoM=0, dimension=1963461, lam=0.5, seed=7,
                 l2="inputs larger than L2 (stored H ~15 GB, vectors ~300 MB)")
 # Davidson settings of the mixed solve (block vectors per SpMM, basis limit)
-MIXED = dict(block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5, refine_lim=32, refine_keep=16)
+MIXED = dict(block=8, lim=96, keep=32, algorithm=1, precond=1, switch_resid=3e-5, refine_lim=32, refine_keep=16)
 # the same solver in FP64 (FP64 products, vectors and projections): the
 # precision-only baseline, run to the same tolerance
-FP64_SAME = dict(block=8, lim=64, keep=32, algorithm=1, precond=1)
+FP64_SAME = dict(block=8, lim=96, keep=32, algorithm=1, precond=1)
 # Iterations the reference algorithm (block 10, limit 30) runs on this problem:
 # its 400-iteration cap (max(40 * nstates, 200)), which it reaches without
 # converging all 10 pairs to 1e-5 (measured with the same algorithm in FP64 on

@@ -76,7 +76,7 @@ int main(int argc, char** argv) {
   } else {
     prm.tol_resid = a.getd("--tol", 1e-5);
     prm.block = nst < 8 ? nst : 8;
-    prm.lim = 64;
+    prm.lim = 96;
     prm.keep = 32;
   }
   std::vector<double> init;

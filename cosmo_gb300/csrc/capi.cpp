@@ -793,7 +793,7 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     if (nume < 1 || nume > 16) throw cg::Error(CG_ERR_ARG, "nstates must be in 1..16");
     if (uint64_t(nume) > h->h.n) throw cg::Error(CG_ERR_ARG, "nstates exceeds the dimension");
     if (prm->block < 1 || prm->block > nume) throw cg::Error(CG_ERR_ARG, "block must be in 1..nstates");
-    if (prm->lim <= nume || prm->lim > 64) throw cg::Error(CG_ERR_ARG, "lim must be in nstates+1..64");
+    if (prm->lim <= nume || prm->lim > 128) throw cg::Error(CG_ERR_ARG, "lim must be in nstates+1..128");
     if (n_init < 0 || (n_init > 0 && !init)) throw cg::Error(CG_ERR_ARG, "bad initial vectors");
     // a restart forms the kept Ritz vectors in place, at most 32 columns a pass
     if (prm->keep < 0 || prm->keep > 32) throw cg::Error(CG_ERR_ARG, "keep must be in 0..32");
@@ -839,8 +839,8 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
       cg::DavConfig c2 = c;
       c2.spmm_prec = CG_PREC_REFINE;
       if (prm->refine_lim > 0) {
-        if (prm->refine_lim <= nume || prm->refine_lim > 64)
-          throw cg::Error(CG_ERR_ARG, "refine_lim must be in nstates+1..64");
+        if (prm->refine_lim <= nume || prm->refine_lim > 128)
+          throw cg::Error(CG_ERR_ARG, "refine_lim must be in nstates+1..128");
         c2.lim = prm->refine_lim;
       }
       if (prm->refine_keep > 0) c2.keep = prm->refine_keep;

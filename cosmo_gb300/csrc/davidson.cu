@@ -35,7 +35,8 @@ namespace cg {
 namespace {
 
 constexpr int kTile = 32;   // rows per tile
-constexpr int kMaxK = 64;   // basis columns per tall-skinny call
+constexpr int kMaxK = 64;   // basis columns per tall-skinny kernel call
+constexpr int kMaxLim = 128;  // basis limit (calls over more than kMaxK columns are split or use the 128-row forms)
 constexpr int kMaxJ = 32;   // right-hand columns per call
 constexpr int kMaxC = 16;   // residual candidates per call
 constexpr int kThreads = 256;
@@ -279,15 +280,15 @@ __global__ void __launch_bounds__(256) k_xty_df(uint64_t n, const double* __rest
 
 // R = AB s_c - lam_c B s_c of the FP64 engine in double-float, one thread per
 // row; s and lam as FP32 pairs in shared memory; R and the norms in FP64.
-template <int CMAX>
+template <int CMAX, int KM>
 __global__ void __launch_bounds__(256) k_resid_df(uint64_t n, const double* __restrict__ B,
                                                   const double* __restrict__ AB, int ld, int K,
                                                   const double* __restrict__ Sc, const double* __restrict__ lam, int C,
                                                   double* __restrict__ R, int ldr, double* __restrict__ part) {
-  __shared__ float sh_[64 * CMAX], sl_[64 * CMAX];
+  __shared__ float sh_[KM * CMAX], sl_[KM * CMAX];
   __shared__ double ls[CMAX];
   __shared__ double red[8][CMAX];
-  for (int i = threadIdx.x; i < 64 * CMAX; i += blockDim.x) {
+  for (int i = threadIdx.x; i < KM * CMAX; i += blockDim.x) {
     const int k = i / CMAX, c = i % CMAX;
     df_split((k < K && c < C) ? Sc[k * C + c] : 0.0, sh_[i], sl_[i]);
   }
@@ -339,12 +340,12 @@ __global__ void __launch_bounds__(256) k_resid_df(uint64_t n, const double* __re
 // Y = beta Y + alpha X G of the FP64 engine in double-float: one thread per
 // row, alpha G as FP32 pairs in shared memory, outputs combined in FP64.  A row
 // is read completely before it is written (X and Y may alias).
-template <int JMAX>
+template <int JMAX, int KM>
 __global__ void __launch_bounds__(256) k_gemm_df(uint64_t n, const double* X, int ldx, int xo, int K,
                                                  const double* __restrict__ G, double* Y, int ldy, int yo, int J,
                                                  double alpha, double beta) {
-  __shared__ float gh[64 * JMAX], gl[64 * JMAX];
-  for (int i = threadIdx.x; i < 64 * JMAX; i += blockDim.x) {
+  __shared__ float gh[KM * JMAX], gl[KM * JMAX];
+  for (int i = threadIdx.x; i < KM * JMAX; i += blockDim.x) {
     const int k = i / JMAX, j = i % JMAX;
     df_split((k < K && j < J) ? alpha * G[k * J + j] : 0.0, gh[i], gl[i]);
   }
@@ -465,15 +466,15 @@ __device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
 // row read 8 values (32 bytes) at a time when aligned, s in shared memory, R
 // rows written 8 columns at a time; per-CTA partial |R[:, c]|^2 (FP32 over a
 // thread's rows, FP64 across threads, fixed order).
-template <class T, int CMAX>
+template <class T, int CMAX, int KM>
 __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict__ B, const T* __restrict__ AB,
                                                  int ld, int K, const double* __restrict__ Sc,
                                                  const double* __restrict__ lam, int C, T* __restrict__ R, int ldr,
                                                  double* __restrict__ part, bool vec, bool vec_r) {
-  __shared__ __align__(16) T ss[64 * CMAX];
+  __shared__ __align__(16) T ss[KM * CMAX];
   __shared__ T ls[CMAX];
   __shared__ double red[8][CMAX];
-  for (int i = threadIdx.x; i < 64 * CMAX; i += blockDim.x) {
+  for (int i = threadIdx.x; i < KM * CMAX; i += blockDim.x) {
     const int k = i / CMAX, c = i % CMAX;
     ss[i] = (k < K && c < C) ? T(Sc[k * C + c]) : T(0);
   }
@@ -551,12 +552,12 @@ __global__ void __launch_bounds__(256) k_resid_v(uint64_t n, const T* __restrict
 // outputs of the row in registers, G (alpha folded in) in shared memory read
 // as broadcast; FP32 X rows read 8 values (32 bytes) at a time when aligned.  A row is
 // read completely before it is written, so X and Y may alias.
-template <class T, int JMAX>
+template <class T, int JMAX, int KM>
 __global__ void __launch_bounds__(256) k_gemm_r(uint64_t n, const T* X, int ldx, int xo, int K,
                                                 const double* __restrict__ G, T* Y, int ldy, int yo, int J,
                                                 double alpha, double beta, bool vec_x, bool vec_y) {
-  __shared__ __align__(16) T gs[64 * JMAX];
-  for (int i = threadIdx.x; i < 64 * JMAX; i += blockDim.x) {
+  __shared__ __align__(16) T gs[KM * JMAX];
+  for (int i = threadIdx.x; i < KM * JMAX; i += blockDim.x) {
     const int k = i / JMAX, j = i % JMAX;
     gs[i] = (k < K && j < J) ? T(alpha * G[k * J + j]) : T(0);
   }
@@ -875,7 +876,7 @@ struct Engine {
   // host wall time per phase (verbose >= 2 prints them)
   double t_eig = 0, t_resid = 0, t_ortho = 0, t_collapse = 0, t_abs = 0;
   int pip_calls_ = 0, pip_fallbacks_ = 0;
-  int gemm_occ_[4] = {0, 0, 0, 0};  // resident CTAs per SM of k_gemm_r<T, 4|8|16|32>
+  int gemm_occ_[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident CTAs per SM of k_gemm_r<T, 4|8|16|32, 64|kMaxLim>
   static double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
   }
@@ -894,7 +895,7 @@ struct Engine {
     mblock = c.block;
     int align = sizeof(T) == 4 ? 4 : 2;
     L = (lim + align - 1) / align * align;
-    if (lim > kMaxK) throw Error(CG_ERR_ARG, "lim above 64 is not supported");
+    if (lim > kMaxLim) throw Error(CG_ERR_ARG, "lim above 128 is not supported");
     if (mblock > kMaxC || nume > kMaxC) throw Error(CG_ERR_ARG, "block and nstates must be <= 16");
     int nsm = 0;
     CG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h.device));
@@ -916,11 +917,11 @@ struct Engine {
     xwarps_ = (xwarps_ + 7) / 8 * 8;
     part.alloc(std::max<size_t>(std::max<size_t>(size_t(nparts) * kMaxK * kMaxJ, size_t(nsm * 8) * kMaxC),
                                 size_t(xwarps_) * 64 * 16));
-    small.alloc(kMaxK * kMaxK);
-    small2.alloc(kMaxK * kMaxK);
-    dlam.alloc(kMaxK);
-    dsel.alloc(kMaxK);
-    drows.alloc(kMaxK);
+    small.alloc(kMaxLim * kMaxLim);
+    small2.alloc(kMaxLim * kMaxLim);
+    dlam.alloc(kMaxLim);
+    dsel.alloc(kMaxLim);
+    drows.alloc(kMaxLim);
     CG_CUDA(cudaMemsetAsync(B.p, 0, B.bytes(), s));
     CG_CUDA(cudaMemsetAsync(AB.p, 0, AB.bytes(), s));
     CG_CUDA(cudaEventCreate(&ev0));
@@ -935,10 +936,22 @@ struct Engine {
     cudaEventDestroy(ev1);
   }
 
-  // G (K x J, row-major, host) = X[:, xo:xo+K]^T Y[:, yo:yo+J]
+  // G (K x J, row-major, host) = X[:, xo:xo+K]^T Y[:, yo:yo+J]; more than
+  // kMaxK columns of X go through the kernels kMaxK at a time (rows of G)
   void xty(const T* X, int xo, int K, const T* Y, int yo, int J, std::vector<double>& G) {
+    if (K > kMaxK && J > 0) {
+      if (K > kMaxLim) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
+      G.assign(size_t(K) * J, 0.0);
+      std::vector<double> Gc;
+      for (int k0 = 0; k0 < K; k0 += kMaxK) {
+        const int kc = std::min(kMaxK, K - k0);
+        xty(X, xo + k0, kc, Y, yo, J, Gc);
+        std::copy(Gc.begin(), Gc.end(), G.begin() + size_t(k0) * J);
+      }
+      return;
+    }
     if (K == 0 || J == 0) { G.assign(size_t(K) * J, 0.0); return; }
-    if (J > 16 || K > 64) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
+    if (J > 16 || K > kMaxK) throw Error(CG_ERR_INTERNAL, "xty shape out of range");
     const unsigned blocks = unsigned(xwarps_ / 8);
     // the refinement phase of the mixed solve multiplies in double-float; the
     // plain FP64 solve (and any product of fewer than 3 columns) stays FP64
@@ -963,9 +976,10 @@ struct Engine {
   }
   // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
-    // every kernel below holds G (K x J) in shared memory sized kMaxK x kMaxJ
-    // and gives a row at most 32 lanes
-    if (K < 0 || K > kMaxK || J < 0 || J > kMaxJ) throw Error(CG_ERR_INTERNAL, "gemm shape out of range");
+    // every kernel below holds G (K x J) in shared memory sized 64 (or, for
+    // K > 64, kMaxLim) x kMaxJ and gives a row at most 32 lanes
+    if (K < 0 || K > kMaxLim || J < 0 || J > kMaxJ) throw Error(CG_ERR_INTERNAL, "gemm shape out of range");
+    const bool wide = K > kMaxK;
     if (K == 0 || J == 0) return;
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
@@ -975,9 +989,11 @@ struct Engine {
       if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
         const double* Xd = reinterpret_cast<const double*>(Xp);
         double* Yd = reinterpret_cast<double*>(Yp);
-        if (J <= 8) k_gemm_df<8><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
-        else if (J <= 16) k_gemm_df<16><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
-        else k_gemm_df<32><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta);
+#define CG_GEMM_DF(JM, KM) k_gemm_df<JM, KM><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta)
+        if (J <= 8) { if (wide) CG_GEMM_DF(8, kMaxLim); else CG_GEMM_DF(8, kMaxK); }
+        else if (J <= 16) { if (wide) CG_GEMM_DF(16, kMaxLim); else CG_GEMM_DF(16, kMaxK); }
+        else { if (wide) CG_GEMM_DF(32, kMaxLim); else CG_GEMM_DF(32, kMaxK); }
+#undef CG_GEMM_DF
         CG_CUDA(cudaGetLastError());
         count_launch();
         CG_CUDA(cudaStreamSynchronize(s));
@@ -986,20 +1002,28 @@ struct Engine {
     }
     // one wave of resident CTAs (the grid-stride loop gives each thread whole
     // rows, so the grid changes no result)
-    const int jc = J <= 4 ? 0 : J <= 8 ? 1 : J <= 16 ? 2 : 3;
+    const int jc = (J <= 4 ? 0 : J <= 8 ? 1 : J <= 16 ? 2 : 3) + (wide ? 4 : 0);
     if (!gemm_occ_[jc]) {
       int per_sm = 0;
-      if (jc == 0) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 4>, 256, 0));
-      if (jc == 1) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 8>, 256, 0));
-      if (jc == 2) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 16>, 256, 0));
-      if (jc == 3) CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 32>, 256, 0));
+      switch (jc) {
+        case 0: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 4, kMaxK>, 256, 0)); break;
+        case 1: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 8, kMaxK>, 256, 0)); break;
+        case 2: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 16, kMaxK>, 256, 0)); break;
+        case 3: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 32, kMaxK>, 256, 0)); break;
+        case 4: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 4, kMaxLim>, 256, 0)); break;
+        case 5: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 8, kMaxLim>, 256, 0)); break;
+        case 6: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 16, kMaxLim>, 256, 0)); break;
+        default: CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_r<T, 32, kMaxLim>, 256, 0)); break;
+      }
       gemm_occ_[jc] = std::max(per_sm, 1);
     }
     grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * gemm_occ_[jc])));
-    if (J <= 4) k_gemm_r<T, 4><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
-    else if (J <= 8) k_gemm_r<T, 8><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
-    else if (J <= 16) k_gemm_r<T, 16><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
-    else k_gemm_r<T, 32><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy);
+#define CG_GEMM_R(JM, KM) k_gemm_r<T, JM, KM><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy)
+    if (J <= 4) { if (wide) CG_GEMM_R(4, kMaxLim); else CG_GEMM_R(4, kMaxK); }
+    else if (J <= 8) { if (wide) CG_GEMM_R(8, kMaxLim); else CG_GEMM_R(8, kMaxK); }
+    else if (J <= 16) { if (wide) CG_GEMM_R(16, kMaxLim); else CG_GEMM_R(16, kMaxK); }
+    else { if (wide) CG_GEMM_R(32, kMaxLim); else CG_GEMM_R(32, kMaxK); }
+#undef CG_GEMM_R
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));  // G's staging buffer is reused by the next call
@@ -1147,18 +1171,18 @@ struct Engine {
     bool done = false;
     if constexpr (sizeof(T) == 8) {
       if (cfg.spmm_prec == CG_PREC_REFINE) {
-        if (C <= 8)
-          k_resid_df<8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
-        else
-          k_resid_df<16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p);
+#define CG_RESID_DF(CM, KM) k_resid_df<CM, KM><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p)
+        if (C <= 8) { if (kpass > kMaxK) CG_RESID_DF(8, kMaxLim); else CG_RESID_DF(8, kMaxK); }
+        else { if (kpass > kMaxK) CG_RESID_DF(16, kMaxLim); else CG_RESID_DF(16, kMaxK); }
+#undef CG_RESID_DF
         done = true;
       }
     }
     if (!done) {
-      if (C <= 8)
-        k_resid_v<T, 8><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec, vec_r);
-      else
-        k_resid_v<T, 16><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec, vec_r);
+#define CG_RESID_V(CM, KM) k_resid_v<T, CM, KM><<<rgrid, 256, 0, s>>>(n, B.p, AB.p, L, kpass, small2.p, dlam.p, C, R.p, ldr, part.p, vec, vec_r)
+      if (C <= 8) { if (kpass > kMaxK) CG_RESID_V(8, kMaxLim); else CG_RESID_V(8, kMaxK); }
+      else { if (kpass > kMaxK) CG_RESID_V(16, kMaxLim); else CG_RESID_V(16, kMaxK); }
+#undef CG_RESID_V
     }
     CG_CUDA(cudaGetLastError());
     count_launch();
@@ -1262,7 +1286,7 @@ struct Engine {
   // factorisation fails: the classical form then takes over.
   bool orthogonalize_pip(int basis_dim, int m) {
     const int K = basis_dim + m;
-    if (K > 64 || m > 16) return false;
+    if (K > kMaxLim || m > 16) return false;
     const double min_ratio = sizeof(T) == 4 ? 1e-3 : 1e-8;  // |Y_perp|^2 / |Y|^2 below: cancellation
     for (int pass = 0; pass < 2; ++pass) {
       std::vector<double> W;

@@ -91,7 +91,7 @@ def test_fp44_mixed_solve_true_residuals(gpu_available, tmp_path):
     p, b = _system(tmp_path, "fp", 4, 4, 7)
     h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
     r = cg.davidson_diagonalization(h, 10, want_vectors=True, precision=cg.CG_PREC_FP32, tol_resid=1e-5,
-                                    block=8, lim=64, keep=32, algorithm=1, precond=1, switch_resid=3e-5,
+                                    block=8, lim=96, keep=32, algorithm=1, precond=1, switch_resid=3e-5,
                                     refine_lim=32, refine_keep=16)
     assert r.stats.converged == 10, (r.resid, r.stats.ierr)
     del h
@@ -102,9 +102,9 @@ def test_fp44_mixed_solve_true_residuals(gpu_available, tmp_path):
     np.testing.assert_allclose(res, r.resid, rtol=1e-3, atol=1e-8)
 
 
-MIXED = dict(precision=cg.CG_PREC_FP32, tol_resid=1e-5, block=8, lim=64, keep=32, algorithm=1, precond=1,
+MIXED = dict(precision=cg.CG_PREC_FP32, tol_resid=1e-5, block=8, lim=96, keep=32, algorithm=1, precond=1,
              switch_resid=3e-5, refine_lim=32, refine_keep=16)
-FP64_SAME = dict(precision=cg.CG_PREC_FP64, tol_resid=1e-5, block=8, lim=64, keep=32, algorithm=1, precond=1)
+FP64_SAME = dict(precision=cg.CG_PREC_FP64, tol_resid=1e-5, block=8, lim=96, keep=32, algorithm=1, precond=1)
 
 
 def _compare_states(b, rm, r64):
