@@ -796,8 +796,8 @@ cg_status cg_davidson(const cg_hamiltonian* h, const cg_davidson_params* prm, co
     if (prm->lim <= nume || prm->lim > 128) throw cg::Error(CG_ERR_ARG, "lim must be in nstates+1..128");
     if (n_init < 0 || (n_init > 0 && !init)) throw cg::Error(CG_ERR_ARG, "bad initial vectors");
     // a restart forms the kept Ritz vectors in place, at most 32 columns a pass
-    if (prm->keep < 0 || prm->keep > 32) throw cg::Error(CG_ERR_ARG, "keep must be in 0..32");
-    if (prm->refine_keep < 0 || prm->refine_keep > 32) throw cg::Error(CG_ERR_ARG, "refine_keep must be in 0..32");
+    if (prm->keep < 0 || prm->keep > 64) throw cg::Error(CG_ERR_ARG, "keep must be in 0..64");
+    if (prm->refine_keep < 0 || prm->refine_keep > 64) throw cg::Error(CG_ERR_ARG, "refine_keep must be in 0..64");
     if (prm->precision != CG_PREC_FP64 && prm->precision != CG_PREC_FP32)
       throw cg::Error(CG_ERR_ARG, "precision must be CG_PREC_FP64 or CG_PREC_FP32");
     if (prm->precision != h->h.precision && !h->h.virt)

@@ -37,6 +37,7 @@ namespace {
 constexpr int kTile = 32;   // rows per tile
 constexpr int kMaxK = 64;   // basis columns per tall-skinny kernel call
 constexpr int kMaxLim = 128;  // basis limit (calls over more than kMaxK columns are split or use the 128-row forms)
+constexpr int kMaxKeep = 64;  // Ritz vectors kept at a thick restart
 constexpr int kMaxJ = 32;   // right-hand columns per call
 constexpr int kMaxC = 16;   // residual candidates per call
 constexpr int kThreads = 256;
@@ -974,8 +975,33 @@ struct Engine {
     CG_CUDA(cudaMemcpyAsync(G.data(), small.p, sizeof(double) * K * J, cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
   }
-  // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J)
+  // Y[:, yo:yo+J] = beta Y + alpha X[:, xo:xo+K] G (G host K x J).  More
+  // than kMaxJ outputs (beta 0 only: the thick restart keeping more than 32
+  // Ritz vectors, X and Y the same block) go kMaxJ columns at a time into a
+  // scratch block, then into Y, so no output overwrites an input still read.
+  DBuf<T> wide_;
   void gemm(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int yo, int J, double alpha, double beta) {
+    if (J > kMaxJ) {
+      if (beta != 0.0 || J > kMaxKeep) throw Error(CG_ERR_INTERNAL, "gemm shape out of range");
+      if (wide_.n < n * uint64_t(J)) wide_.alloc(n * uint64_t(J));
+      std::vector<double> Gc;
+      for (int j0 = 0; j0 < J; j0 += kMaxJ) {
+        const int jc = std::min(kMaxJ, J - j0);
+        Gc.assign(size_t(K) * jc, 0.0);
+        for (int k = 0; k < K; ++k)
+          for (int j = 0; j < jc; ++j) Gc[size_t(k) * jc + j] = G[size_t(k) * J + j0 + j];
+        gemm_ld(Xp, xo, K, Gc, wide_.p, J, j0, jc, alpha, 0.0);
+      }
+      k_copy_cols<T><<<blocks_for(n * uint64_t(J)), 256, 0, s>>>(n, wide_.p, J, 0, Yp, L, yo, J);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+      CG_CUDA(cudaStreamSynchronize(s));
+      return;
+    }
+    gemm_ld(Xp, xo, K, G, Yp, L, yo, J, alpha, beta);
+  }
+  void gemm_ld(T* Xp, int xo, int K, const std::vector<double>& G, T* Yp, int ldy, int yo, int J, double alpha,
+               double beta) {
     // every kernel below holds G (K x J) in shared memory sized 64 (or, for
     // K > 64, kMaxLim) x kMaxJ and gives a row at most 32 lanes
     if (K < 0 || K > kMaxLim || J < 0 || J > kMaxJ) throw Error(CG_ERR_INTERNAL, "gemm shape out of range");
@@ -983,13 +1009,13 @@ struct Engine {
     if (K == 0 || J == 0) return;
     CG_CUDA(cudaMemcpyAsync(small2.p, G.data(), sizeof(double) * K * J, cudaMemcpyHostToDevice, s));
     const bool vx = reinterpret_cast<uintptr_t>(Xp + xo) % 32 == 0 && L % 8 == 0;
-    const bool vy = reinterpret_cast<uintptr_t>(Yp + yo) % 32 == 0 && L % 8 == 0 && J % 8 == 0;
+    const bool vy = reinterpret_cast<uintptr_t>(Yp + yo) % 32 == 0 && ldy % 8 == 0 && J % 8 == 0;
     unsigned grid = unsigned(std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * 8));
     if constexpr (sizeof(T) == 8) {
       if (J <= 32 && J >= 3 && cfg.spmm_prec == CG_PREC_REFINE) {
         const double* Xd = reinterpret_cast<const double*>(Xp);
         double* Yd = reinterpret_cast<double*>(Yp);
-#define CG_GEMM_DF(JM, KM) k_gemm_df<JM, KM><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, L, yo, J, alpha, beta)
+#define CG_GEMM_DF(JM, KM) k_gemm_df<JM, KM><<<grid, 256, 0, s>>>(n, Xd, L, xo, K, small2.p, Yd, ldy, yo, J, alpha, beta)
         if (J <= 8) { if (wide) CG_GEMM_DF(8, kMaxLim); else CG_GEMM_DF(8, kMaxK); }
         else if (J <= 16) { if (wide) CG_GEMM_DF(16, kMaxLim); else CG_GEMM_DF(16, kMaxK); }
         else { if (wide) CG_GEMM_DF(32, kMaxLim); else CG_GEMM_DF(32, kMaxK); }
@@ -1018,7 +1044,7 @@ struct Engine {
       gemm_occ_[jc] = std::max(per_sm, 1);
     }
     grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, uint64_t(nsm_) * gemm_occ_[jc])));
-#define CG_GEMM_R(JM, KM) k_gemm_r<T, JM, KM><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, L, yo, J, alpha, beta, vx, vy)
+#define CG_GEMM_R(JM, KM) k_gemm_r<T, JM, KM><<<grid, 256, 0, s>>>(n, Xp, L, xo, K, small2.p, Yp, ldy, yo, J, alpha, beta, vx, vy)
     if (J <= 4) { if (wide) CG_GEMM_R(4, kMaxLim); else CG_GEMM_R(4, kMaxK); }
     else if (J <= 8) { if (wide) CG_GEMM_R(8, kMaxLim); else CG_GEMM_R(8, kMaxK); }
     else if (J <= 16) { if (wide) CG_GEMM_R(16, kMaxLim); else CG_GEMM_R(16, kMaxK); }

@@ -266,7 +266,7 @@ cg_status cg_spmm_set_tiled_shape(cg_hamiltonian* h, int32_t slices_per_warp, in
 typedef struct {
   int32_t nstates;   /* eigenpairs wanted (nume)                          */
   int32_t block;     /* vectors added per iteration (mblock)              */
-  int32_t lim;       /* maximum basis size before collapse (limmax)       */
+  int32_t lim;       /* maximum basis size before collapse (limmax; <= 128) */
   int32_t maxiter;   /* iteration cap (0: max(40*nstates, 200) as the reference) */
   double crite;      /* eigenvalue-change threshold (reference 1e-15)     */
   double critc;      /* Ritz-coefficient threshold (reference 1e-12)      */
@@ -283,10 +283,10 @@ typedef struct {
                         Test_Convergence, collapse to nstates vectors);
                         1: residual-driven block Davidson: every wanted residual is
                         re-checked each iteration, restarts keep `keep` Ritz vectors */
-  int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates; at most 32) */
+  int32_t keep;      /* algorithm 1: Ritz vectors kept at a restart (0: 2 * nstates; at most 64) */
   int32_t precond;   /* algorithm 1: 1 = diagonal preconditioner (lambda - H_ii), 0 = none */
   int32_t refine_lim;   /* mixed solve: basis limit of the FP64 refinement phase (0: lim) */
-  int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep; at most 32) */
+  int32_t refine_keep;  /* mixed solve: Ritz vectors kept at its restarts (0: keep; at most 64) */
   int32_t ortho_pip;    /* algorithm 1 (default 1): orthogonalise each new block by two
                            passes of block Gram-Schmidt with Pythagorean inner products,
                            the Cholesky-QR of the block folded into the same update

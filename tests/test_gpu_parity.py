@@ -230,12 +230,19 @@ def test_davidson_fp32_corrections_check_fails_over(gpu_available, tmp_path, cap
 
 
 def test_davidson_keep_bound(gpu_available, tmp_path):
-    """A restart forms the kept Ritz vectors in place, at most 32 columns: keep
-    and refine_keep above 32 are refused on the host before any work."""
+    """A restart keeps at most 64 Ritz vectors (more than 32 are formed 32
+    columns at a time in a scratch block): keep and refine_keep above 64 are
+    refused on the host before any work, and a solve keeping 40 (more than
+    one kernel's 32 outputs) matches the one keeping 16."""
     _, _, h = _gpu("sd22m0s1", str(tmp_path), cg.CG_PREC_FP32)
-    for kw in (dict(keep=40), dict(refine_keep=40)):
-        with pytest.raises(cg.CosmoError, match="keep must be in 0..32"):
-            cg.davidson_diagonalization(h, 4, precision=cg.CG_PREC_FP32, lim=64, block=4, **kw)
+    for kw in (dict(keep=72), dict(refine_keep=72)):
+        with pytest.raises(cg.CosmoError, match="keep must be in 0..64"):
+            cg.davidson_diagonalization(h, 4, precision=cg.CG_PREC_FP32, lim=96, block=4, **kw)
+    kw = dict(precision=cg.CG_PREC_FP32, tol_resid=1e-6, block=4, lim=56, algorithm=1, switch_resid=3e-5)
+    a = cg.davidson_diagonalization(h, 4, keep=40, refine_keep=40, **kw)
+    b = cg.davidson_diagonalization(h, 4, keep=16, **kw)
+    assert int(a.stats.converged) == 4 and int(b.stats.converged) == 4
+    np.testing.assert_allclose(a.eig, b.eig, rtol=0, atol=1e-8)
 
 
 def test_ee_roundtrip(gpu_available, tmp_path):
