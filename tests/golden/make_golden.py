@@ -250,7 +250,11 @@ def sf_case(work: str, manifest: dict) -> None:
 # .mbs from the reference's XsysmbsOMP
 EM_SYSTEMS = (("sd22m0s1", SyntheticSystem("sd", 2, 2, 0, "+", 0.5, 1)),
               ("sd13m0s1", SyntheticSystem("sd", 1, 3, 0, "+", 0.5, 1)),
-              ("sd22m2s1", SyntheticSystem("sd", 2, 2, 2, "+", 0.5, 1)))
+              ("sd22m2s1", SyntheticSystem("sd", 2, 2, 2, "+", 0.5, 1)),
+              # fp: oscillator radial integrals of 0f and 1p orbits
+              ("fp11m0s9", SyntheticSystem("fp", 1, 1, 0, "+", 0.5, 9)),
+              ("fp20m0s9", SyntheticSystem("fp", 2, 0, 0, "+", 0.5, 9)))
+EM_CORE = {"sd": 16, "fp": 40}  # mass number of the core (Weisskopf and standard units)
 EM_STATES = 5
 # run name: (operator node, daughter system or None for the parent itself, flags[, parent system])
 EM_RUNS = {
@@ -264,6 +268,11 @@ EM_RUNS = {
     "E2k": ('<operator name="E2" J="2" en="0.6" ep="1.4"/>', "sd22m2s1", ["-w"]),
     # beta plus from the sd 1n+3p states to the sd 2n+2p ones
     "GT+": ('<operator name="GT+" J="1"/>', "sd22m0s1", ["-ft"], "sd13m0s1"),
+    # fp shell: E2, M1, E4 (r^4 radial integrals) within fp 1n+1p, GT- from fp 2n+0p
+    "E2fp": ('<operator name="E2" J="2" en="0.5" ep="1.5"/>', None, ["-w", "-u"], "fp11m0s9"),
+    "M1fp": ('<operator name="M1" J="1"/>', None, ["-w"], "fp11m0s9"),
+    "E4fp": ('<operator name="E4" J="4" en="0.5" ep="1.5"/>', None, ["-u"], "fp11m0s9"),
+    "GT-fp": ('<operator name="GT-" J="1"/>', "fp11m0s9", ["-ft"], "fp20m0s9"),
 }
 
 
@@ -271,7 +280,7 @@ def em_xml(work: str, name: str, sysd) -> str:
     """A system with its reference basis (.mbs, XsysmbsOMP), eigenvectors
     (.EE, ref_dump) and <state> nodes (XSHLJT); returns the XML path."""
     xml = sf_xml(work, name, sysd)
-    txt = open(xml).read().replace("<system ", f'<system A="{16 + sysd.nv + sysd.zv}" ', 1)
+    txt = open(xml).read().replace("<system ", f'<system A="{EM_CORE[sysd.space] + sysd.nv + sysd.zv}" ', 1)
     open(xml, "w").write(txt)
     run_ref("ref_dump", xml, name, work, EM_STATES, 0)
     txt = open(xml).read()

@@ -59,12 +59,13 @@ def _systems(tmp):
     g = np.load(os.path.join(GOLDEN, CASE + ".npz"))
     out = {}
     for name, sysd in MG.EM_SYSTEMS:
+        A = MG.EM_CORE[sysd.space] + sysd.nv + sysd.zv
         xml = MG.sf_xml(tmp, name, sysd)
-        txt = open(xml).read().replace("<system ", f'<system A="{16 + sysd.nv + sysd.zv}" ', 1)
+        txt = open(xml).read().replace("<system ", f'<system A="{A}" ', 1)
         open(xml, "w").write(txt)
         sp = OI.System(xml)
         z = O.basis(sp.sps, sp.nv + sp.zv, sp.twom, sp.nv - sp.zv, sp.parity)
-        out[name] = dict(xml=xml, sys=sp, z=z, states=_states(name, g[name + "_EE"]), ee=g[name + "_EE"])
+        out[name] = dict(xml=xml, sys=sp, z=z, states=_states(name, g[name + "_EE"]), ee=g[name + "_EE"], A=A)
     return out
 
 
@@ -112,7 +113,7 @@ def _flags(run):
     return tuple(manifest()[CASE]["runs"][run]["flags"])
 
 
-RUNS = ("E2", "E2p", "M1", "GT-", "F", "M1k", "E2k", "GT+")
+RUNS = ("E2", "E2p", "M1", "GT-", "F", "M1k", "E2k", "GT+", "E2fp", "M1fp", "E4fp", "GT-fp")
 
 
 def _parent(s, run):
@@ -131,8 +132,8 @@ def test_oracle_transitions_match_reference(tmp_path, run):
     P, D = parent["states"], daughter["states"]
     amp = TR.onebody_amplitudes(parent["z"], np.array([p["vec"] for p in P]), daughter["z"],
                                 np.array([q["vec"] for q in D]), terms)
-    trans, moms = TR.transitions(op, P, D, amp, A=parent["sys"].A + 16, flags=_flags(run))
-    _check_records(run, trans, moms, parent["sys"].A + 16)
+    trans, moms = TR.transitions(op, P, D, amp, A=parent["A"], flags=_flags(run))
+    _check_records(run, trans, moms, parent["A"])
 
 
 @pytest.mark.parametrize("run", RUNS)
@@ -213,7 +214,7 @@ def test_gpu_transition_amplitudes_and_tool(gpu_available, tmp_path, run):
                     for k, v in _attrs(t).items()}) for t in re.findall(r"<transition [^>]*/>", st)]
              for st in states]
     moms = [[{"m": float(_attrs(m)["m"])} for m in re.findall(r"<moment [^>]*/>", st)] for st in states]
-    _check_records(run, trans, moms, parent["sys"].A + 16)
+    _check_records(run, trans, moms, parent["A"])
     if run == "E2":
         # XSHLJT run again on the result keeps the states' other children
         ntr = txt.count("<transition"), txt.count("<moment")
