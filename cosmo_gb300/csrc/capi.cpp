@@ -301,7 +301,6 @@ cg_status cg_hamiltonian_build_virtual(const cg_problem* p, const cg_basis* b, i
     CG_NOT_NULL(b);
     CG_NOT_NULL(out);
     *out = nullptr;
-    cg::refuse_truncated(b->sys, "the on-the-fly product");
     same_device(b->b.device);
     if (p->sys.sps.size() != b->sys.sps.size() || p->sys.nv != b->sys.nv || p->sys.zv != b->sys.zv)
       throw cg::Error(CG_ERR_ARG, "basis was built for another problem");

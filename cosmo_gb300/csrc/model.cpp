@@ -350,12 +350,6 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   return sys;
 }
 
-void refuse_truncated(const System& sys, const char* route) {
-  if (sys.trunc.active())
-    throw Error(CG_ERR_UNSUPPORTED, std::string(route) + " does not take truncated bases (" + sys.truncation +
-                                        "on the system)");
-}
-
 // ----------------------------------------------------- Oxbash reader
 namespace {
 std::string resolve_int(const System& sys, const std::string& name) {

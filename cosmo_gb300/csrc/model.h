@@ -98,10 +98,6 @@ struct System {
 
 System load_system(const std::string& xml_path, const std::string& system_name);
 
-// Throws CG_ERR_UNSUPPORTED for a system with a basis truncation, on routes
-// that do not take truncated bases (the on-the-fly product), before any
-// device work.
-void refuse_truncated(const System& sys, const char* route);
 // Oscillator quanta 2n + l of s.p. state i.
 inline int sp_quanta(const SPState& s) { return 2 * s.n + s.l; }
 

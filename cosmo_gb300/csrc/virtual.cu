@@ -103,6 +103,12 @@ struct VArgs {
   const uint32_t* pp_off;  // per slice: first PP2 entry (32 lanes x count)
   const uint32_t* pp_rank;
   const double* diag;
+  // truncated basis: class rank of each list member, and per list a map
+  // class rank -> list rank (0xffff: outside the basis), rmax entries at most
+  const uint32_t* gcr;
+  const uint16_t* lmap;
+  const uint32_t *lmap_off, *lmap_len;
+  int rmax;
 };
 
 template <class T>
@@ -208,7 +214,13 @@ __device__ __forceinline__ void vmac(T (&acc)[VB], DF2 v, const T (&x)[VB]) {
 // rows, table values as (hi, lo) pairs (tl holds the low parts), products and
 // sums in double-float, Y written as FP64: the refinement product on the FP32
 // pipe instead of the FP64 one.
-template <class T, int VB, int RPT, bool DF>
+// TR = true: a truncated basis, whose block rows are a list (the allowed
+// proton configurations of the block's class).  The proton-transition tables
+// then hold class ranks of the target configuration; the class-to-list map
+// of every staged block comes into shared memory with its x rows, and a
+// target outside the basis is skipped.  NN2 reads the target's map from global
+// memory.
+template <class T, int VB, int RPT, bool DF, bool TR>
 __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab<T> tb, VTab<T> tl,
                                                                    const T* __restrict__ x, void* __restrict__ yv,
                                                                    int ldy, int m, int* __restrict__ err) {
@@ -226,6 +238,11 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   V* un0 = wsl1 + nw;
   V* un1 = un0 + 32;
   V* Pp = un1 + 32;
+  // TR: class-to-list maps of the own block and the two staged blocks, from the
+  // first 16-byte boundary after Pp
+  uint16_t* rown = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(Pp + npp + 1) + 15) & ~uintptr_t(15));
+  uint16_t* rbuf0 = rown + a.rmax;
+  uint16_t* rbuf1 = rbuf0 + a.rmax;
 
   // half-swapped row reads (Row) for up to 2 rows per thread: fp 4+4 (2 rows)
   // 4.46 -> 4.04 ms; with 4 rows per thread (fp 5+5) they measured slower
@@ -257,12 +274,28 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
     wsl1[npp] = vfrom<V>(0.0);
   }
   __syncthreads();
-  if (tid == 0) {
-    bulk_load(own, x + start * VB, uint32_t(L) * uint32_t(VB * sizeof(T)), &mbar[2]);
-    if (t0 < t1) {
-      const uint32_t tg = a.nt[t0].target;
-      bulk_load(buf0, x + a.bstart[tg] * VB, a.blen[tg] * uint32_t(VB * sizeof(T)), &mbar[0]);
+  // one elected thread: the x rows of block blk (and, TR, its class-to-list map) onto one barrier
+  auto stage = [&](T* dst, uint16_t* rdst, uint32_t blk, uint64_t* bar) {
+    const uint32_t xb = a.blen[blk] * uint32_t(VB * sizeof(T));
+    if constexpr (TR) {
+      const uint32_t lc = a.bclass[blk], rb = a.lmap_len[lc] * 2u;
+      bulk::expect_tx(bar, xb + rb);
+      bulk::copy(dst, x + a.bstart[blk] * VB, xb, bar);
+      bulk::copy(rdst, a.lmap + a.lmap_off[lc], rb, bar);
+    } else {
+      bulk_load(dst, x + a.bstart[blk] * VB, xb, bar);
     }
+  };
+  if (tid == 0) {
+    stage(own, rown, beta, &mbar[2]);
+    if (t0 < t1) stage(buf0, rbuf0, a.nt[t0].target, &mbar[0]);
+  }
+  // TR: class rank of each own row's proton configuration
+  uint32_t gr[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int r = tid + k * NT;
+    gr[k] = (TR && r < L) ? a.gcr[cs + r] : 0u;
   }
 
   T acc[RPT][VB];
@@ -281,8 +314,16 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       const int r = tid + k * NT;
       if (r < L) {
         Row<T, VB> xr;
-        xr.load_g(x + (ts + r) * VB, sw);
-        vmac(acc[k], h, xr.v);
+        if constexpr (TR) {  // the same proton configuration in the target's list (q.pad: its map)
+          const uint32_t rr = __ldg(a.lmap + q.pad + gr[k]);
+          if (rr != 0xffffu) {
+            xr.load_g(x + (ts + rr) * VB, sw);
+            vmac(acc[k], h, xr.v);
+          }
+        } else {
+          xr.load_g(x + (ts + r) * VB, sw);
+          vmac(acc[k], h, xr.v);
+        }
       }
     }
   }
@@ -321,8 +362,16 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
         const uint32_t q = a.sl_e[e];
         V v = Pp[(q >> 16) & 0x7ff];
         v = vadd(vtab<V>(tb.sl_c, tl.sl_c, e), ((q >> 27) & 1) ? vneg(v) : v);
-        xr.load_s(own + size_t(q & 0xffff) * VB, sw);
-        vmac(acc[k], v, xr.v);
+        if constexpr (TR) {
+          const uint32_t rr = rown[q & 0xffff];
+          if (rr != 0xffffu) {
+            xr.load_s(own + size_t(rr) * VB, sw);
+            vmac(acc[k], v, xr.v);
+          }
+        } else {
+          xr.load_s(own + size_t(q & 0xffff) * VB, sw);
+          vmac(acc[k], v, xr.v);
+        }
       }
     }
   }
@@ -344,10 +393,7 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       un[tid] = tr.sign ? vneg(w) : w;
     }
     __syncthreads();
-    if (tid == 0 && t + 1 < t1) {
-      const uint32_t tg = a.nt[t + 1].target;
-      bulk_load(jb ? buf0 : buf1, x + a.bstart[tg] * VB, a.blen[tg] * uint32_t(VB * sizeof(T)), &mbar[jb ^ 1]);
-    }
+    if (tid == 0 && t + 1 < t1) stage(jb ? buf0 : buf1, jb ? rbuf0 : rbuf1, a.nt[t + 1].target, &mbar[jb ^ 1]);
     const bool ok = mbar_wait(&mbar[jb], (u >> 1) & 1);
     if (__syncthreads_or(!ok)) {
       // give the copies in flight a second bounded wait, report, leave
@@ -360,6 +406,7 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       return;
     }
     const T* bf = jb ? buf1 : buf0;
+    const uint16_t* rbf = jb ? rbuf1 : rbuf0;
     const int dmp = a.ndm - 2 - (tr.dmi & ~1) + (tr.dmi & 1);  // opposite 2m change, same parity change
     const V cn = vfrom<V>(tr.cn);
 #pragma unroll
@@ -374,15 +421,27 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
           V w = wsl[(q >> 16) & 0x7ff];
           w = ((q >> 27) & 1) ? vneg(w) : w;
           Row<T, VB> xr;
-          xr.load_s(bf + size_t(q & 0xffff) * VB, sw);
-          vmac(acc[k], w, xr.v);
+          if constexpr (TR) {
+            const uint32_t rr = rbf[q & 0xffff];
+            if (rr != 0xffffu) {
+              xr.load_s(bf + size_t(rr) * VB, sw);
+              vmac(acc[k], w, xr.v);
+            }
+          } else {
+            xr.load_s(bf + size_t(q & 0xffff) * VB, sw);
+            vmac(acc[k], w, xr.v);
+          }
         }
+        // N1: the same proton configuration in the target block (TR: its rank in the target's list)
         if (same_m && r < L) {
-          V v = cn;
-          for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v = vadd(v, un[__ffs(w) - 1]);
-          Row<T, VB> xr;
-          xr.load_s(bf + size_t(r) * VB, sw);
-          vmac(acc[k], v, xr.v);
+          const uint32_t rn = TR ? uint32_t(rbf[gr[k]]) : uint32_t(r);
+          if (rn != 0xffffu) {
+            V v = cn;
+            for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v = vadd(v, un[__ffs(w) - 1]);
+            Row<T, VB> xr;
+            xr.load_s(bf + size_t(rn) * VB, sw);
+            vmac(acc[k], v, xr.v);
+          }
         }
       }
     }
@@ -434,10 +493,10 @@ __global__ void k_virtual_diag(uint64_t n, int nblocks, const uint64_t* __restri
   diag[i] = d;
 }
 
-template <class T, int VB, int RPT, bool DF>
+template <class T, int VB, int RPT, bool DF, bool TR>
 void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const VTab<T>& tl, const T* x, void* y,
                 int ldy, int m, int threads, size_t smem, int* err, cudaStream_t s) {
-  auto kern = k_virtual<T, VB, RPT, DF>;
+  auto kern = k_virtual<T, VB, RPT, DF, TR>;
   CG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   kern<<<unsigned(a.lmax ? h.virt->nblocks : 0), threads, smem, s>>>(a, tb, tl, x, y, ldy, m, err);
   CG_CUDA(cudaGetLastError());
@@ -452,6 +511,11 @@ VArgs make_args(const VirtualOp& v, const Hamiltonian& h) {
   a.nt_off = v.nt_off.p; a.nt = v.nt.p; a.nn_off = v.nn_off.p; a.nn2 = v.nn2.p;
   a.cslice = v.cslice.p; a.sl_off = v.sl_off.p; a.sl_e = v.sl_e.p; a.pp_off = v.pp_off.p; a.pp_rank = v.pp_rank.p;
   a.diag = h.diag.p;
+  a.gcr = v.gcr.p;
+  a.lmap = v.lmap.p;
+  a.lmap_off = v.lmap_off.p;
+  a.lmap_len = v.lmap_len.p;
+  a.rmax = v.rmax;
   return a;
 }
 
@@ -468,7 +532,8 @@ void virtual_product(const Hamiltonian& h, const T* x, void* y, int ldy, int m, 
   VArgs a = make_args(v, h);
   const int npp = v.np * v.np;
   const size_t vsz = DF ? 2 * sizeof(float) : sizeof(T);  // bytes of one element value
-  const size_t smem = kVirtualSmemHead + size_t(3) * v.lmax * VB * sizeof(T) + (3 * size_t(npp + 4) + 64) * vsz;
+  const size_t smem = kVirtualSmemHead + size_t(3) * v.lmax * VB * sizeof(T) + (3 * size_t(npp + 4) + 64) * vsz +
+                      (v.truncated ? 16 + size_t(3) * v.rmax * sizeof(uint16_t) : 0);
   if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "neutron block too long for the shared-memory staging");
   // rows per thread: threads <= 512, or <= 1024 when the staging buffers
   // leave room for one CTA per SM only (long blocks, e.g. fp 5+5): there two
@@ -482,11 +547,20 @@ void virtual_product(const Hamiltonian& h, const T* x, void* y, int ldy, int m, 
   if (rpt > 8) throw Error(CG_ERR_UNSUPPORTED, "neutron block longer than 4096 rows");
   DBuf<int>& err = v.err;
   CG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-  switch (rpt) {
-    case 1: launch_rpt<T, VB, 1, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-    case 2: launch_rpt<T, VB, 2, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-    case 4: launch_rpt<T, VB, 4, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-    default: launch_rpt<T, VB, 8, DF>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+  if (v.truncated) {
+    switch (rpt) {
+      case 1: launch_rpt<T, VB, 1, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      case 2: launch_rpt<T, VB, 2, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      case 4: launch_rpt<T, VB, 4, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      default: launch_rpt<T, VB, 8, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+    }
+  } else {
+    switch (rpt) {
+      case 1: launch_rpt<T, VB, 1, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      case 2: launch_rpt<T, VB, 2, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      case 4: launch_rpt<T, VB, 4, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+      default: launch_rpt<T, VB, 8, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
+    }
   }
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -638,9 +712,48 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   }
   std::vector<int32_t> block_of(std::max<uint64_t>(b.neut.nconf, 1), -1);
   for (int i = 0; i < nblocks; ++i) block_of[colex_host(b.h_bmask[i], b.h_binom)] = i;
-  std::vector<int32_t> pclass(std::max<uint64_t>(b.prot.nconf, 1), -1);
-  for (int c = 0; c < nclasses; ++c)
-    for (uint32_t g = b.h_cstart[c]; g < b.h_cstart[c + 1]; ++g) pclass[colex_host(b.h_cmasks[g], b.h_binom)] = c;
+  // truncated basis: the "classes" of the basis are its lists.  Each list
+  // member keeps its rank in the untruncated class (b.h_pcrank), and each list
+  // a map class rank -> list rank (0xffff: not in the list), padded to 8
+  // entries so that every map is a 16-byte bulk copy
+  const bool trunc = b.truncated;
+  std::vector<uint32_t> gcr, lmap_off, lmap_len, g_list;
+  std::vector<uint16_t> lmap;
+  if (trunc) {
+    std::map<std::pair<int, int>, uint32_t> csize;  // untruncated class sizes by (2m, parity)
+    std::vector<uint32_t> key_of(std::max<uint64_t>(b.prot.nconf, 1), 0);
+    std::vector<std::pair<int, int>> keys;
+    for (uint64_t i = 0; i < b.prot.nconf; ++i) {
+      const std::pair<int, int> k{b.prot.lex_m2[i], b.prot.lex_par[i]};
+      if (csize[k]++ == 0) keys.push_back(k);
+    }
+    std::map<std::pair<int, int>, uint32_t> key_id;
+    for (size_t i = 0; i < keys.size(); ++i) key_id[keys[i]] = uint32_t(i);
+    for (uint64_t i = 0; i < b.prot.nconf; ++i)
+      key_of[colex_host(b.prot.lex_mask[i], b.h_binom)] = key_id[{b.prot.lex_m2[i], b.prot.lex_par[i]}];
+    gcr.assign(std::max<size_t>(b.h_cmasks.size(), 1), 0);
+    g_list.assign(std::max<size_t>(b.h_cmasks.size(), 1), 0);
+    for (int L = 0; L < nclasses; ++L) {
+      const uint32_t g0 = b.h_cstart[L], g1 = b.h_cstart[L + 1];
+      uint32_t cs = 0;
+      if (g1 > g0) cs = csize[keys[key_of[colex_host(b.h_cmasks[g0], b.h_binom)]]];
+      if (cs > 0xffff) throw Error(CG_ERR_UNSUPPORTED, "proton class longer than 65535 configurations");
+      const uint32_t len = std::max<uint32_t>(8, (cs + 7) / 8 * 8);
+      lmap_off.push_back(uint32_t(lmap.size()));
+      lmap_len.push_back(len);
+      v.rmax = std::max<int>(v.rmax, int(len));
+      lmap.resize(lmap.size() + len, 0xffff);
+      for (uint32_t g = g0; g < g1; ++g) {
+        const uint32_t r = b.h_pcrank[colex_host(b.h_cmasks[g], b.h_binom)];
+        if (r >= cs) throw Error(CG_ERR_INTERNAL, "list member outside its class");
+        gcr[g] = r;
+        g_list[g] = uint32_t(L);
+        lmap[lmap_off[L] + r] = uint16_t(g - g0);
+      }
+    }
+    if (lmap.size() >= (1ull << 32)) throw Error(CG_ERR_UNSUPPORTED, "class-to-list maps beyond 2^32 entries");
+  }
+  v.truncated = trunc;
   const uint64_t nall = nn == 64 ? ~0ull : ((1ull << nn) - 1);
   const uint64_t pall_local = np == 64 ? ~0ull : ((1ull << np) - 1);
   const auto& m2 = b.sp_m2;
@@ -705,10 +818,15 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
             if (m2[a] + m2[bb] != m2[c] + m2[d] || (par[a] ^ par[bb] ^ par[c] ^ par[d])) continue;
             const uint64_t K = nu ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
             const int tb = block_of[colex_host(K, b.h_binom)];
-            if (tb < 0) throw Error(CG_ERR_INTERNAL, "two-neutron move leaves the basis");
+            if (tb < 0) {
+              if (trunc) continue;  // the target block is outside the truncated basis
+              throw Error(CG_ERR_INTERNAL, "two-neutron move leaves the basis");
+            }
             const bool fwd = (a < c) || (a == c && bb < d);
             const double val = fwd ? H.term2(nu, a, bb, c, d) : H.term2(K, c, d, a, bb);
-            if (std::fabs(val) >= kDropV) nn2.push_back(VPair{uint32_t(tb), 0u, val});
+            // truncated basis: pad = the target list's class-to-list map
+            if (std::fabs(val) >= kDropV)
+              nn2.push_back(VPair{uint32_t(tb), trunc ? lmap_off[b.h_bclass[tb]] : 0u, val});
           }
         }
       }
@@ -784,7 +902,12 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
             const uint64_t K = P ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
             const bool fwd = (a < c) || (a == c && bb < d);
             const double val = fwd ? H.term2(P, a, bb, c, d) : H.term2(K, c, d, a, bb);
-            const uint32_t rank = b.h_pcrank[colex_host(K >> nn, b.h_binom)];
+            // rank in the own block's list (the class; truncated: skip targets outside the list)
+            uint32_t rank = b.h_pcrank[colex_host(K >> nn, b.h_binom)];
+            if (trunc) {
+              rank = lmap[lmap_off[g_list[g]] + rank];
+              if (rank == 0xffff) continue;
+            }
             if (std::fabs(val) >= kDropV) pp2.push_back(VPair{rank, 0u, val});
           }
         }
@@ -927,6 +1050,12 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   v.pp_off.upload(pps_off, s);
   v.pp_rank.upload(pp_rank, s);
   v.pp_h.upload(pp_h, s);
+  if (trunc) {
+    v.gcr.upload(gcr, s);
+    v.lmap.upload(lmap, s);
+    v.lmap_off.upload(lmap_off, s);
+    v.lmap_len.upload(lmap_len, s);
+  }
   std::vector<float> sl_cf(sl_c.begin(), sl_c.end()), pp_hf(pp_h.begin(), pp_h.end());
   v.sl_cf.upload(sl_cf, s);
   v.pp_hf.upload(pp_hf, s);

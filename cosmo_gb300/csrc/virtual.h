@@ -72,6 +72,13 @@ struct VirtualOp {
   DBuf<double> W, Un, Up;                           // nn*nn*np*np, nn*nn*np, np*np*nn
   DBuf<float> Wf, Unf, Upf;
   DBuf<float> Wl, Unl, Upl, sl_cl, pp_hl;            // low parts (value - float(value)), double-float product
+  // truncated basis: rows of a block are a list (allowed proton configurations of its class);
+  // proton-transition tables hold class ranks, mapped to list ranks by lmap (0xffff: outside)
+  bool truncated = false;
+  int rmax = 0;                                     // longest map (entries, a multiple of 8)
+  DBuf<uint32_t> gcr;                               // nconf_p: class rank of each list member
+  DBuf<uint16_t> lmap;                              // per list: class rank -> list rank
+  DBuf<uint32_t> lmap_off, lmap_len;                // lists: first entry, entries (16-byte multiples)
   mutable DBuf<int> err;                            // staged-copy timeout flag
   uint64_t bytes() const {
     return bstart.bytes() + blen.bytes() + bclass.bytes() + bmask.bytes() + order.bytes() + cstart.bytes() +
@@ -79,7 +86,7 @@ struct VirtualOp {
            sl_off.bytes() + sl_e.bytes() + sl_c.bytes() + sl_cf.bytes() + pp_off.bytes() + pp_rank.bytes() +
            pp_h.bytes() + pp_hf.bytes() + W.bytes() + Un.bytes() + Up.bytes() +
            Wf.bytes() + Unf.bytes() + Upf.bytes() + Wl.bytes() + Unl.bytes() + Upl.bytes() + sl_cl.bytes() +
-           pp_hl.bytes();
+           pp_hl.bytes() + gcr.bytes() + lmap.bytes() + lmap_off.bytes() + lmap_len.bytes();
   }
 };
 

@@ -102,8 +102,9 @@ cg_status cg_problem_two_body(const cg_problem* p, int32_t* keys, double* vals);
  * s.p. tuples.  Replaces SM::MakeMBS2 (include/sm/MakeMBS.cxx:186) and the
  * Xsysmbs/XsysmbsOMP tools (xmlshell/xmbs/XsysmbsOMP.cpp:323).  A system with
  * a basis truncation (hwmax attribute, <hwrejection> or <rejection> children,
- * XsysmbsOMP.cpp:214-300) is refused with CG_ERR_UNSUPPORTED before any
- * device work: the full basis built here would not be the reference's. */
+ * XsysmbsOMP.cpp:214-300) gets the truncated basis in the same order as the
+ * reference's: neutron configurations in lexicographic order, each followed
+ * by the proton configurations the truncation allows with it. */
 typedef struct cg_basis cg_basis;
 
 cg_status cg_basis_build(const cg_problem* p, cg_basis** out);
@@ -148,7 +149,9 @@ cg_status cg_hamiltonian_build(const cg_problem* p, const cg_basis* b, int32_t p
  * (include/sm/PPMatrix.cxx:42-152) as used by DEXHVJT (davidson/DEXHVJT.cpp:36-78):
  * the product regenerates every element per call from the basis bitstrings and
  * the interaction, through per-species transition tables (neutron blocks x
- * proton classes of the M-scheme basis).  The handle works with every product
+ * proton classes of the M-scheme basis; in a truncated basis the allowed proton
+ * configurations of each neutron block, targets outside the basis dropped as
+ * the reference's locate drops them).  The handle works with every product
  * and Davidson call: CG_PREC_FP32 products compute in FP32, CG_PREC_FP64 and
  * CG_PREC_REFINE products in FP64; precision only sets the default of
  * cg_spmm calls.  info.nnz_full = elements generated per product and vector,

@@ -48,9 +48,20 @@ def truncation(name: str) -> tuple[tuple[int, int] | None, list[tuple[int, int, 
     return hw, rej
 
 
+# larger cases for the on-the-fly product (no fixtures: checked against the
+# stored matrix, which the cases above pin to the reference): lists of up to
+# 260 rows over several 32-row slices, and lists far shorter than their class
+LARGE = {
+    "psd44m0_hw4": dict(orbits=PSD_ORBITS, nv=4, zv=4, twom=0, parity="+", hwmax=4),
+    "psd44m0_hw4_rej": dict(orbits=PSD_ORBITS, nv=4, zv=4, twom=0, parity="+", hwmax=4,
+                            rej=[(0, 2, [5])]),
+    "psd66m0_hw2": dict(orbits=PSD_ORBITS, nv=6, zv=6, twom=0, parity="+", hwmax=2),
+}
+
+
 def write_case(workdir: str, name: str) -> str:
     """Write <name>.int and <name>.xml into workdir; returns the XML path."""
-    c = CASES[name]
+    c = CASES[name] if name in CASES else LARGE[name]
     os.makedirs(workdir, exist_ok=True)
     sysd = SyntheticSystem("psd", c["nv"], c["zv"], c["twom"], c["parity"], 0.0, 1, name=name)
     ip = os.path.join(workdir, name + ".int")
