@@ -110,6 +110,8 @@ _SIGS = {
     "cg_problem_one_body": (C.c_int32, [_P, _P, _P]),
     "cg_problem_two_body": (C.c_int32, [_P, _P, _P]),
     "cg_basis_build": (C.c_int32, [_P, C.POINTER(_P)]),
+    "cg_basis_build_wide": (C.c_int32, [_P, C.POINTER(_P)]),
+    "cg_basis_is_wide": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "cg_basis_destroy": (None, [_P]),
     "cg_basis_dims": (C.c_int32, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]),
     "cg_basis_states": (C.c_int32, [_P, C.c_uint64, C.c_uint64, _P]),
@@ -422,12 +424,17 @@ class Problem:
 
 
 class ManyBodyStates:
-    """GPU-resident M-scheme basis in the reference's lexicographic order."""
+    """GPU-resident M-scheme basis in the reference's lexicographic order.
+    wide=True builds the wide representation (64-bit species masks, binary
+    search locate) even where the bitstring one applies."""
 
-    def __init__(self, problem: Problem):
+    def __init__(self, problem: Problem, wide: bool = False):
         h = _P()
-        _check(lib().cg_basis_build(problem._h, C.byref(h)))
+        _check((lib().cg_basis_build_wide if wide else lib().cg_basis_build)(problem._h, C.byref(h)))
         self._h = h
+        w = C.c_int32()
+        _check(lib().cg_basis_is_wide(h, C.byref(w)))
+        self.wide = bool(w.value)
         n = C.c_uint64()
         N = C.c_int32()
         _check(lib().cg_basis_dims(h, C.byref(n), C.byref(N)))

@@ -22,7 +22,7 @@ SRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libcosmo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu", "sf.cu", "xshlsf.cpp", "em.cpp", "xshlemb.cpp"]
+SOURCES = ["model.cpp", "dense.cpp", "capi.cpp", "basis.cu", "hbuild.cu", "spmm.cu", "davidson.cu", "virtual.cu", "jt.cu", "xshljt.cpp", "batched.cu", "hhread.cpp", "tiled.cu", "sf.cu", "xshlsf.cpp", "em.cpp", "xshlemb.cpp", "wide.cu"]
 
 
 def nvcc() -> str:

@@ -133,6 +133,10 @@ void enumerate_species(SpeciesTables& sp, int norb, int k, const int* m2, const 
 }  // namespace
 
 void basis_build(const System& sys, Basis& b) {
+  if (sys.n_neutron_states > 32 || int(sys.sps.size()) - sys.n_neutron_states > 32) {
+    basis_build_wide(sys, b);
+    return;
+  }
   CG_CUDA(cudaGetDevice(&b.device));
   if (!b.stream) CG_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
   cudaStream_t s = b.stream;
@@ -305,6 +309,10 @@ void basis_build(const System& sys, Basis& b) {
 
 void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out) {
   if (first + count > b.n) throw Error(CG_ERR_ARG, "state range outside the basis");
+  if (b.wide) {
+    basis_tuples_wide(b, first, count, out);
+    return;
+  }
   int N = b.kn + b.kp;
   const uint64_t chunk = 1ull << 24;
   DBuf<uint16_t> d(std::min(count, chunk) * std::max(N, 1));
@@ -320,6 +328,7 @@ void basis_tuples(const Basis& b, uint64_t first, uint64_t count, uint16_t* out)
 }
 
 uint64_t basis_locate_host(const Basis& b, const uint16_t* t) {
+  if (b.wide) return basis_locate_wide_host(b, t);
   const uint64_t miss = b.n + 1;
   int N = b.kn + b.kp;
   uint64_t nmask = 0, pmask = 0;
@@ -340,6 +349,11 @@ uint64_t basis_locate_host(const Basis& b, const uint16_t* t) {
     return r == ~0u ? miss : no + r;
   }
   return no + b.h_pcrank[colex_host(pmask, b.h_binom)];
+}
+
+void refuse_wide(const Basis& b, const char* route) {
+  if (b.wide)
+    throw Error(CG_ERR_UNSUPPORTED, std::string(route) + " takes valence spaces of at most 32 m-states per species");
 }
 
 }  // namespace cg

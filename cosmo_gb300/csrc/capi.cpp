@@ -227,6 +227,25 @@ cg_status cg_basis_build(const cg_problem* p, cg_basis** out) {
     *out = b.release();
   });
 }
+cg_status cg_basis_build_wide(const cg_problem* p, cg_basis** out) {
+  return guard([&] {
+    CG_NOT_NULL(p);
+    CG_NOT_NULL(out);
+    *out = nullptr;
+    require_device();
+    auto b = std::make_unique<cg_basis>();
+    b->sys = p->sys;
+    cg::basis_build_wide(p->sys, b->b);
+    *out = b.release();
+  });
+}
+cg_status cg_basis_is_wide(const cg_basis* b, int32_t* wide) {
+  return guard([&] {
+    CG_NOT_NULL(b);
+    CG_NOT_NULL(wide);
+    *wide = b->b.wide ? 1 : 0;
+  });
+}
 void cg_basis_destroy(cg_basis* b) { delete b; }
 
 cg_status cg_basis_dims(const cg_basis* b, uint64_t* n, int32_t* np) {

@@ -105,6 +105,16 @@ struct Basis {
   DBuf<uint32_t> nlist;            // by neutron colex rank: list of its block, ~0u if none
   DBuf<uint32_t> lrank;            // lists x npc
   std::vector<uint32_t> h_nlist, h_lrank;
+  // valence spaces with a species of more than 32 m-states (wide.cu): a
+  // determinant is a pair of 64-bit species masks; blocks and lists as above
+  // (h_bstart, h_bclass, h_cstart) with 64-bit masks, located by binary search
+  bool wide = false;
+  DBuf<uint64_t> wstate;                     // 2 per basis state: neutron mask, proton mask
+  std::vector<uint64_t> h_wbmask, h_wcmask;  // block neutron masks; list members in h_cstart order
+  std::vector<uint64_t> h_wnkey, h_wpkey;    // block neutron masks sorted; list members sorted per list
+  std::vector<uint32_t> h_wnblk, h_wprank;   // block of each sorted neutron mask; rank of each sorted member
+  DBuf<uint64_t> wbstart, wnkey, wpkey;
+  DBuf<uint32_t> wbclass, wcstart, wnblk, wprank;
   // host copies used for locate and .mbs output
   std::vector<uint64_t> h_noff;
   std::vector<uint32_t> h_pcrank;
@@ -113,7 +123,15 @@ struct Basis {
   ~Basis();
 };
 
+// the bitstring basis, or the wide one (wide.cu) when a species has more than 32 m-states
 void basis_build(const System& sys, Basis& b);
+// the wide representation for any system (up to 64 m-states per species)
+void basis_build_wide(const System& sys, Basis& b);
+void basis_tuples_wide(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);
+uint64_t basis_locate_wide_host(const Basis& b, const uint16_t* tuple);
+void jt_expectations_wide(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt);
+// refuses a wide basis on a route that only takes bitstring bases
+void refuse_wide(const Basis& b, const char* route);
 uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom);
 
 // <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nst host vectors (state k at vecs + k*n).
@@ -178,6 +196,16 @@ struct Hamiltonian {
   ~Hamiltonian();
   uint64_t device_bytes() const;  // HBM held by the matrix (or the on-the-fly tables)
 };
+
+// Rows of H on a wide basis (wide.cu): per-row element counts, then the
+// elements (unsorted columns) and the diagonal, as the bitstring builder's
+// count and fill passes.
+struct WideRows {
+  virtual ~WideRows() = default;
+  virtual void count(uint32_t* counts, int* err) = 0;
+  virtual void fill(const uint64_t* rowptr, uint32_t* col, double* val, double* diag) = 0;
+};
+std::unique_ptr<WideRows> wide_rows(const System& sys, const Operator& op, const Basis& b, cudaStream_t s);
 
 // tiled_copy: also build the block-tiled copy of an FP32 matrix (tiled.h)
 void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h,

@@ -473,13 +473,18 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   CG_CUDA(cudaEventRecord(e0, s));
 
   DevOperator dop;
-  upload_operator(sys, op, dop, s);
+  std::unique_ptr<WideRows> wide;
   std::vector<int8_t> m2(b.ns);
   for (int i = 0; i < b.ns; ++i) m2[i] = int8_t(b.sp_m2[i]);
   DBuf<int8_t> dm2;
   dm2.upload(m2, s);
-
-  Ctx c;
+  Ctx c{};
+  if (b.wide) {
+    wide = wide_rows(sys, op, b, s);
+  } else {
+    upload_operator(sys, op, dop, s);
+  }
+  if (!b.wide) {
   c.ns = b.ns;
   c.nn = b.nn;
   c.npairs = dop.npairs;
@@ -496,6 +501,7 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   c.v2 = dop.v2.p;
   c.mmask = dop.mmask.p;
   c.m2 = dm2.p;
+  }
 
   const uint64_t n = b.n;
   DBuf<uint32_t> counts(std::max<uint64_t>(n, 1));
@@ -504,9 +510,13 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   if (grid == 0) grid = 1;
   DBuf<int> derr(1);
   CG_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), s));
-  k_count<<<grid, T, 0, s>>>(c, b.binom.p, counts.p, derr.p);
-  CG_CUDA(cudaGetLastError());
+  if (wide) {
+    wide->count(counts.p, derr.p);
+  } else {
+    k_count<<<grid, T, 0, s>>>(c, b.binom.p, counts.p, derr.p);
+    CG_CUDA(cudaGetLastError());
     count_launch();
+  }
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
 
@@ -544,7 +554,9 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   h.col.alloc(std::max<uint64_t>(h.nnz, 1));
   DBuf<double> tmpval(std::max<uint64_t>(h.nnz, 1));
   h.diag.alloc(std::max<uint64_t>(n, 1));
-  if (n) {
+  if (n && wide) {
+    wide->fill(h.rowptr.p, h.col.p, tmpval.p, h.diag.p);
+  } else if (n) {
     k_fill<<<grid, T, 0, s>>>(c, b.binom.p, h.rowptr.p, h.col.p, tmpval.p, h.diag.p);
     CG_CUDA(cudaGetLastError());
     count_launch();

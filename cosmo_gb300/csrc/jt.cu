@@ -162,6 +162,10 @@ void raise_norms(const Basis& src, const Basis& tb, const std::vector<int8_t>& p
 
 void jt_expectations(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt) {
   if (nst < 1 || nst > kMaxStates) throw Error(CG_ERR_ARG, "1..16 states per call");
+  if (b.wide) {
+    jt_expectations_wide(sys, b, vecs, nst, jj, tt);
+    return;
+  }
   cudaStream_t s = b.stream;
   const uint64_t n = b.n;
   const int ns = b.ns, nn = b.nn;

@@ -241,7 +241,9 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
   sys.sps = neutrons;
   sys.sps.insert(sys.sps.end(), protons.begin(), protons.end());
   sys.n_neutron_states = int(neutrons.size());
-  if (sys.sps.size() > 64) throw Error(CG_ERR_UNSUPPORTED, "more than 64 m-scheme s.p. states");
+  // up to 64 m-states per species (masks of one 64-bit word per species)
+  if (sys.n_neutron_states > 64 || int(sys.sps.size()) - sys.n_neutron_states > 64)
+    throw Error(CG_ERR_UNSUPPORTED, "more than 64 m-scheme s.p. states per species");
 
   // system node
   const XmlNode* sn = nullptr;
@@ -311,8 +313,11 @@ System load_system(const std::string& xml_path, const std::string& system_name) 
       const std::string type = ob->attr("type") ? *ob->attr("type") : std::string("n");
       for (size_t i = 0; i < sys.sps.size(); ++i) {
         const bool neut = sys.sps[i].tz2 > 0;
-        if (sys.sps[i].level == level && ((neut && (type == "pn" || type == "n")) || (!neut && (type == "pn" || type == "p"))))
-          rej.mask |= 1ull << i;
+        if (sys.sps[i].level == level && ((neut && (type == "pn" || type == "n")) || (!neut && (type == "pn" || type == "p")))) {
+          if (i < 64) rej.mask |= 1ull << i;
+          if (int(i) < sys.n_neutron_states) rej.nmask |= 1ull << i;
+          else rej.pmask |= 1ull << (i - sys.n_neutron_states);
+        }
       }
     }
     sys.trunc.rejections.push_back(rej);
@@ -690,6 +695,27 @@ void j_minus_j_plus(const std::map<Key2, double>& jo, std::map<Key2, double>& js
   }
 }
 }  // namespace
+
+std::map<Key2, double> j_plus_terms(const std::vector<SPState>& sps) { return j_plus(sps); }
+
+std::map<Key2, double> t_plus_terms(const System& sys) {
+  std::map<Key2, double> to;
+  const int nn = sys.n_neutron_states, ns = int(sys.sps.size());
+  for (int y = 0; y < nn; ++y)
+    for (int x = nn; x < ns; ++x) {
+      const SPState &X = sys.sps[x], &Y = sys.sps[y];
+      if (X.level == Y.level && X.m2 == Y.m2 && X.n == Y.n && X.l == Y.l && X.j2 == Y.j2 && X.parity == Y.parity &&
+          X.t2 == Y.t2 && X.tz2 + 2 == Y.tz2)
+        to[{x, y}] = std::sqrt(double(X.t2 - X.tz2) * double(X.t2 + X.tz2 + 2)) / 2.0;
+    }
+  return to;
+}
+
+Operator square_operator(const std::map<Key2, double>& raise) {
+  Operator op;
+  j_minus_j_plus(raise, op.one, op.two);
+  return op;
+}
 
 // xReadSPInt, Oxbash branch + JJ branch (include/xsm/xReadSPInt.cxx:58-73,
 // 273-287): ESP from the s.p. energies (MakeESPO, include/sm/MakeSPO.cxx:195),

@@ -67,7 +67,8 @@ struct Truncation {
   int hwmin = 0, hwmax = 0;
   struct Rejection {
     int nmin = 0, nmax = 0;
-    uint64_t mask = 0;  // flagged s.p. states (global index, neutrons first)
+    uint64_t mask = 0;          // flagged s.p. states (global index, neutrons first; spaces of <= 64 states)
+    uint64_t nmask = 0, pmask = 0;  // the same per species (species-local bits)
   };
   std::vector<Rejection> rejections;
   bool active() const { return hw || !rejections.empty(); }
@@ -121,6 +122,17 @@ struct SphericalInt {
 
 SphericalInt read_oxbash(const System& sys);
 Operator build_operator(const System& sys);
+
+// One-body raising operators keyed (annihilated, created): J+ (SPJPlus, same
+// orbit and species, m -> m + 1, sqrt((j - m)(j + m + 1))) and T+ (SPTPlus,
+// proton -> neutron in the same orbit and m, value 1), include/sm/
+// spherical2sp.cxx:629-700; and the Hermitian square O+ O of such an operator
+// as forward-ordered one- and two-body terms (SPSqrM + StripHermitianOperator,
+// include/sm/cioperators.cxx:200-287): <psi| O+ O |psi> = ||O psi||^2, which
+// gives <J-J+> and <T-T+> in the basis of psi itself.
+std::map<Key2, double> j_plus_terms(const std::vector<SPState>& sps);
+std::map<Key2, double> t_plus_terms(const System& sys);
+Operator square_operator(const std::map<Key2, double>& raise);
 
 // Clebsch-Gordan coefficient <j1 m1 j2 m2 | j3 m3>, all arguments doubled.
 double clebsch_gordan(int j1, int m1, int j2, int m2, int j3, int m3);

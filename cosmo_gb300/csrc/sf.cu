@@ -202,6 +202,23 @@ __global__ void k_occupations(uint64_t n, const uint64_t* __restrict__ state, co
   for (int i = threadIdx.x; i < ns; i += blockDim.x) part[size_t(blockIdx.x) * 64 + i] = occ[i];
 }
 
+// The same on a wide basis: determinants as (neutron, proton) 64-bit masks,
+// proton s.p. state j at index nn + j, CTA rows of 128 s.p. states.
+__global__ void k_occupations_wide(uint64_t n, const uint64_t* __restrict__ wstate, const double* __restrict__ psi,
+                                   int ns, int nn, double* __restrict__ part) {
+  __shared__ double occ[128];
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) occ[i] = 0.0;
+  __syncthreads();
+  for (uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; row < n;
+       row += uint64_t(gridDim.x) * blockDim.x) {
+    const double p = psi[row] * psi[row];
+    for (uint64_t D = wstate[2 * row]; D; D &= D - 1) atomicAdd(&occ[__ffsll((long long)D) - 1], p);
+    for (uint64_t D = wstate[2 * row + 1]; D; D &= D - 1) atomicAdd(&occ[nn + __ffsll((long long)D) - 1], p);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) part[size_t(blockIdx.x) * 128 + i] = occ[i];
+}
+
 }  // namespace
 
 void occupations(const Basis& b, const double* v, int nst, double* occ) {
@@ -210,23 +227,27 @@ void occupations(const Basis& b, const double* v, int nst, double* occ) {
   if (b.n == 0 || nst < 1) return;
   cudaStream_t st = b.stream;
   const unsigned gx = unsigned(std::min<uint64_t>((b.n + 255) / 256, 152ull * 4));
-  DBuf<double> psi(b.n), part(size_t(gx) * 64);
+  const int stride = b.wide ? 128 : 64;
+  DBuf<double> psi(b.n), part(size_t(gx) * stride);
   std::vector<double> h(part.n);
   for (int k = 0; k < nst; ++k) {
     psi.upload(v + uint64_t(k) * b.n, b.n, st);
-    k_occupations<<<gx, 256, 0, st>>>(b.n, b.state.p, psi.p, ns, part.p);
+    if (b.wide) k_occupations_wide<<<gx, 256, 0, st>>>(b.n, b.wstate.p, psi.p, ns, b.nn, part.p);
+    else k_occupations<<<gx, 256, 0, st>>>(b.n, b.state.p, psi.p, ns, part.p);
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
     for (unsigned g = 0; g < gx; ++g)
-      for (int s = 0; s < ns; ++s) occ[size_t(k) * ns + s] += h[size_t(g) * 64 + s];
+      for (int s = 0; s < ns; ++s) occ[size_t(k) * ns + s] += h[size_t(g) * stride + s];
   }
 }
 
 void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                         const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp) {
   if (np < 1 || nd < 1 || nd > kMaxDaughter) throw Error(CG_ERR_ARG, "1..16 daughter states, at least one parent state");
+  refuse_wide(parent, "the transition amplitudes");
+  refuse_wide(daughter, "the transition amplitudes");
   if (parent.ns != daughter.ns || parent.nn != daughter.nn)
     throw Error(CG_ERR_ARG, "parent and daughter bases have different valence spaces");
   if (parent.kn + parent.kp != daughter.kn + daughter.kp)
@@ -304,6 +325,8 @@ void onebody_amplitudes(const System& psys, const Basis& parent, const double* v
 void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                    const double* vd, int nd, double* amp) {
   if (np < 1 || nd < 1 || nd > kMaxDaughter) throw Error(CG_ERR_ARG, "1..16 daughter states, at least one parent state");
+  refuse_wide(parent, "the spectroscopic amplitudes");
+  refuse_wide(daughter, "the spectroscopic amplitudes");
   if (parent.ns != daughter.ns || parent.nn != daughter.nn)
     throw Error(CG_ERR_ARG, "parent and daughter bases have different valence spaces");
   const int ns = parent.ns;

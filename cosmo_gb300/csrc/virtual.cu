@@ -673,6 +673,7 @@ uint64_t Hamiltonian::device_bytes() const {
 void virtual_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h) {
   if (precision != CG_PREC_FP64 && precision != CG_PREC_FP32)
     throw Error(CG_ERR_ARG, "Hamiltonian precision must be CG_PREC_FP64 or CG_PREC_FP32");
+  refuse_wide(b, "the on-the-fly product");
   auto t_begin = std::chrono::steady_clock::now();
   CG_CUDA(cudaGetDevice(&h.device));
   if (h.device != b.device) throw Error(CG_ERR_ARG, "basis lives on another device");

@@ -108,6 +108,19 @@ cg_status cg_problem_two_body(const cg_problem* p, int32_t* keys, double* vals);
 typedef struct cg_basis cg_basis;
 
 cg_status cg_basis_build(const cg_problem* p, cg_basis** out);
+/* A valence space with more than 32 m-states in a species (up to 64 per
+ * species, e.g. the spsdpf space: 40) gets the wide representation: species
+ * configurations enumerated on the host in the reference's order, pruned by
+ * the truncation's oscillator quanta (an untruncated species of more than
+ * 2^26 configurations is refused), determinants as pairs of 64-bit species
+ * masks located by binary search (SM::locate, include/sm/ManyBodyStates.cxx:
+ * 92-130).  Same order, .mbs bytes, stored Hamiltonian, Davidson, <J-J+> /
+ * <T-T+> and occupations as the bitstring basis; the on-the-fly product, the
+ * batched solver and the XSHLSF / XSHLEMB amplitudes refuse it
+ * (CG_ERR_UNSUPPORTED).  cg_basis_build_wide builds that representation for
+ * any system (the two agree on every system both take). */
+cg_status cg_basis_build_wide(const cg_problem* p, cg_basis** out);
+cg_status cg_basis_is_wide(const cg_basis* b, int32_t* wide);
 void cg_basis_destroy(cg_basis* b);
 /* dimension n and particle number N */
 cg_status cg_basis_dims(const cg_basis* b, uint64_t* n, int32_t* nparticles);

@@ -95,6 +95,99 @@ def basis(sps: np.ndarray, N: int, twom: int, tz2: int, parity: int, cap: int | 
     return z
 
 
+def basis_pruned(sps: np.ndarray, nv: int, zv: int, twom: int, parity: int,
+                 hw: tuple[int, int] | None = None, rejections=()) -> np.ndarray:
+    """The same truncated basis as basis_truncated, built without the
+    untruncated one, so that it reaches spaces whose untruncated basis is out
+    of reach (the spsdpf space: 20 neutrons in 40 m-states).
+
+    XsysmbsOMP forms the occupation partitions of each species with quanta in
+    [core, core + hwmax] before combining them (Partition::MakeQ,
+    xmlshell/xmbs/PartitionClass.cxx:151-190); here each species' configurations
+    are enumerated in lexicographic order by a depth-first search that leaves a
+    branch once its quanta plus the least quanta the remaining particles can
+    add exceed core + hwmax.  Neutron configurations in that order, each
+    followed by the proton configurations that pass the determinant filters of
+    basis_truncated (M, parity, hw window, rejections), is the order of the
+    reference's sorted map (XsysmbsOMP.cpp:405-428)."""
+    import sys as _sys
+    sps = np.asarray(sps)
+    neut = sps[:, 6] > 0
+    q = (2 * sps[:, 1] + sps[:, 2]).astype(np.int64)
+    m2 = sps[:, 4].astype(np.int64)
+    par = sps[:, 7].astype(np.int64)
+    nidx = np.where(neut)[0]
+    pidx = np.where(~neut)[0]
+    ncore = int(q[nidx][:nv].sum())
+    pcore = int(q[pidx][:zv].sum())
+    hwmin, hwmax = hw if hw is not None else (0, 0)
+
+    def species(idx: np.ndarray, k: int, qlim: int | None) -> list[tuple[int, ...]]:
+        qs = [int(x) for x in q[idx]]
+        norb = len(qs)
+        big = 1 << 40
+        minsum = [[big] * (k + 1) for _ in range(norb + 1)]
+        for i in range(norb + 1):
+            rest = sorted(qs[i:])
+            acc = 0
+            minsum[i][0] = 0
+            for r in range(1, min(k, len(rest)) + 1):
+                acc += rest[r - 1]
+                minsum[i][r] = acc
+        out: list[tuple[int, ...]] = []
+        cur: list[int] = []
+        lim = big if qlim is None else qlim
+
+        def go(start: int, left: int, Q: int) -> None:
+            if left == 0:
+                out.append(tuple(cur))
+                return
+            for c in range(start, norb - left + 1):
+                Q2 = Q + qs[c]
+                if Q2 + minsum[c + 1][left - 1] > lim:
+                    continue
+                cur.append(c)
+                go(c + 1, left - 1, Q2)
+                cur.pop()
+        old = _sys.getrecursionlimit()
+        _sys.setrecursionlimit(max(old, 4 * (k + 16)))
+        try:
+            if k <= norb:
+                go(0, k, 0)
+        finally:
+            _sys.setrecursionlimit(old)
+        return out
+
+    nconf = species(nidx, nv, ncore + hwmax if hw is not None else None)
+    pconf = species(pidx, zv, pcore + hwmax if hw is not None else None)
+    P = np.array([[int(pidx[c]) for c in t] for t in pconf], dtype=np.int64).reshape(len(pconf), zv)
+    pm = m2[P].sum(1) if zv else np.zeros(len(pconf), np.int64)
+    pp = (par[P].sum(1) & 1) if zv else np.zeros(len(pconf), np.int64)
+    pq = q[P].sum(1) - pcore if zv else np.zeros(len(pconf), np.int64)
+    flags = [np.isin(sps[:, 0], levels) for _, _, levels in rejections]
+    pc = [f[P].sum(1) if zv else np.zeros(len(pconf), np.int64) for f in flags]
+    rows = []
+    for t in nconf:
+        Nn = np.array([int(nidx[c]) for c in t], dtype=np.int64)
+        mn = int(m2[Nn].sum()) if nv else 0
+        pn = int(par[Nn].sum() & 1) if nv else 0
+        qn = int(q[Nn].sum()) - ncore if nv else -ncore
+        keep = (pm == twom - mn) & (pp == (parity ^ pn))
+        if hw is not None:
+            if qn < 0 or qn > hwmax:
+                continue
+            keep &= (pq >= 0) & (pq <= hwmax) & (qn + pq >= hwmin) & (qn + pq <= hwmax)
+        for (nmin, nmax, _), f, c in zip(rejections, flags, pc):
+            cnt = int(f[Nn].sum()) + c
+            keep &= (cnt >= nmin) & (cnt <= nmax)
+        sel = P[keep]
+        if len(sel):
+            rows.append(np.hstack([np.broadcast_to(Nn, (len(sel), nv)), sel]))
+    if not rows:
+        return np.zeros((0, nv + zv), dtype=np.uint16)
+    return np.vstack(rows).astype(np.uint16)
+
+
 def basis_truncated(sps: np.ndarray, nv: int, zv: int, twom: int, parity: int,
                     hw: tuple[int, int] | None = None, rejections=()) -> np.ndarray:
     """The reference's truncated bases as a filter of the untruncated one.

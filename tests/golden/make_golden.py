@@ -43,6 +43,7 @@ from cosmo_gb300.synthetic import SD_ORBITS, SyntheticSystem, make_system, write
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 import truncated as TRUNC  # noqa: E402
+import wide as WIDE  # noqa: E402
 
 # name: (system, full dumps, Davidson nstates, Davidson iterations)
 CASES = {
@@ -423,6 +424,20 @@ def main() -> None:
             np.savez_compressed(os.path.join(HERE, name + ".npz"),
                                 mbs=np.frombuffer(raw[12:], np.uint16).reshape(n, N))
             print(name, manifest[name])
+        # wide valence space (spsdpf, 40 m-states per species): the reference's
+        # basis (XsysmbsOMP), its rows and Davidson on that basis (ref_dump reads
+        # the .mbs), and <J-J+>, <T-T+> of its vectors
+        for name, c in WIDE.CASES.items():
+            if skip(name):
+                continue
+            xml = WIDE.write_case(work, name)
+            run_ref("XsysmbsOMP", xml, name + ".x", work, 0, 0)
+            dump_case(name, work, xml, c["full"], c["nstates"], 0, manifest)
+            manifest[name]["truncation"] = dict(hw=list(c["hw"]), rejections=[])
+            manifest[name]["system"] = dict(space="spsdpf", nv=c["nv"], zv=c["zv"], twom=c["twom"],
+                                            parity=c["parity"], jj=0.0, seed=WIDE.SEED)
+            if c["full"]:
+                jt_case(name, work, xml, c["nstates"], manifest, keep_vecs=True)
         if not skip("mg24usdb"):
             sysd = SyntheticSystem("sd", 4, 4, 0, "+", 0.0, 0, name="mg24usdb")
             xml = os.path.join(work, "mg24usdb.xml")

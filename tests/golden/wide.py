@@ -1,0 +1,40 @@
+"""Wide valence-space cases: the spsdpf space of the reference's 33Al example
+(0s, 0p, 1s0d, 1p0f in the order of the reference's interactions/int.xml:
+40 m-states per species), 20 neutrons and 13 protons with 2Jz = 1, the 0 hw
+positive-parity window (119 states) and the 1 hw negative-parity one (23,842
+states) of the example.  A seeded synthetic interaction stands in for fsu (the
+bases are the example's, the spectra are not).  Shared by the fixture script
+(make_golden.py, which runs the reference's XsysmbsOMP and ref_dump on these
+XML files) and the tests (which rebuild the same XML)."""
+from __future__ import annotations
+
+import os
+
+from cosmo_gb300.synthetic import SyntheticSystem, write_int, write_xml
+
+SPSDPF_ORBITS = [("0s1", 0, 0, 1), ("0p3", 0, 1, 3), ("0p1", 0, 1, 1), ("0d5", 0, 2, 5), ("0d3", 0, 2, 3),
+                 ("1s1", 1, 0, 1), ("0f7", 0, 3, 7), ("0f5", 0, 3, 5), ("1p3", 1, 1, 3), ("1p1", 1, 1, 1)]
+SEED = 33
+
+# name: system, the <hwrejection> window, reference Davidson states, full dumps
+CASES = {
+    "spsdpf_0hw": dict(nv=20, zv=13, twom=1, parity="+", hw=(0, 0), nstates=10, full=True),
+    "spsdpf_1hw": dict(nv=20, zv=13, twom=1, parity="-", hw=(1, 1), nstates=5, full=False),
+}
+
+
+def write_case(workdir: str, name: str) -> str:
+    """Write the interaction and <name>.xml into workdir; returns the XML path."""
+    c = CASES[name]
+    os.makedirs(workdir, exist_ok=True)
+    sysd = SyntheticSystem("spsdpf", c["nv"], c["zv"], c["twom"], c["parity"], 0.0, SEED, name=name)
+    ip = os.path.join(workdir, f"spsdpf_s{SEED}.int")
+    xp = os.path.join(workdir, name + ".xml")
+    write_int(ip, SPSDPF_ORBITS, -8.0, SEED)
+    write_xml(xp, sysd, os.path.abspath(ip), SPSDPF_ORBITS)
+    txt = open(xp).read()
+    lo, hi = c["hw"]
+    txt = txt.replace("<matrix JJ", f'<hwrejection HWMIN="{lo}" HWMAX="{hi}"/><matrix JJ', 1)
+    with open(xp, "w") as f:
+        f.write(txt)
+    return xp

@@ -1,0 +1,203 @@
+"""Wide valence spaces (a species with more than 32 m-states): the spsdpf
+space of the reference's 33Al example, 20 neutrons and 13 protons in 40
+m-states each, in its 0 hw (119 states) and 1 hw (23,842 states) windows,
+pinned to the reference run on the same XML (tests/golden/wide.py,
+make_golden.py): the oracle's pruned enumeration and the GPU basis equal the
+reference's .mbs byte for byte; the operator terms equal the reference's dump;
+the Hamiltonian rows equal the reference's PPMatrix2CSBBlk rows (bit-exact
+connectivity, values within 1e-12); eigenvalues within 1e-6 MeV of the
+reference's Davidson (and of the dense spectrum of its rows); <J-J+> and
+<T-T+> of the reference's vectors within 1e-9.  The wide representation
+forced on bitstring-sized systems gives the same basis, rows, <J-J+>, <T-T+>
+and occupations as the bitstring path."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import conn_hash, golden, manifest, mbs_sha, problem_for
+from oracle import oracle as O
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import truncated as T  # noqa: E402
+import wide as W  # noqa: E402
+
+CASES = sorted(W.CASES)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_pruned_basis_matches_reference(name, tmp_path):
+    import cosmo_gb300 as cg
+    p = cg.Problem(W.write_case(str(tmp_path), name))
+    inf = p.info
+    assert inf.n_sps == 80
+    z = O.basis_pruned(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw=W.CASES[name]["hw"])
+    m = manifest()[name]
+    assert z.shape == (m["n"], m["N"])
+    assert mbs_sha(z) == m["mbs_sha256"]
+
+
+@pytest.mark.parametrize("name", sorted(T.CASES))
+def test_oracle_pruned_equals_filtered(name, tmp_path):
+    """The pruned enumeration against the filter of the untruncated basis."""
+    import cosmo_gb300 as cg
+    p = cg.Problem(T.write_case(str(tmp_path), name))
+    inf = p.info
+    hw, rej = T.truncation(name)
+    a = O.basis_truncated(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw=hw, rejections=rej)
+    b = O.basis_pruned(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw=hw, rejections=rej)
+    assert np.array_equal(a, b)
+
+
+def test_wide_operator_terms_match_reference(tmp_path):
+    import cosmo_gb300 as cg
+    g = golden("spsdpf_0hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    assert np.array_equal(p.sps(), g["sps"])
+    k1, v1 = p.one_body()
+    k2, v2 = p.two_body()
+    assert np.array_equal(k1, g["esp_keys"]) and np.array_equal(v1, g["esp_vals"])
+    assert np.array_equal(k2, g["vspx_keys"])
+    np.testing.assert_allclose(v2, g["vspx_vals"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_wide_basis_matches_reference(gpu_available, name, tmp_path):
+    import cosmo_gb300 as cg
+    m = manifest()[name]
+    b = cg.ManyBodyStates(cg.Problem(W.write_case(str(tmp_path), name)))
+    assert b.wide and (b.n, b.N) == (m["n"], m["N"])
+    z = b.states()
+    assert mbs_sha(z) == m["mbs_sha256"]
+    assert np.array_equal(b.locate(z), np.arange(b.n))
+    # misses: a determinant two oscillator quanta up (two sd protons moved into
+    # the fp shell, M and parity kept) and a wrongly ordered tuple
+    sps = cg.Problem(W.write_case(str(tmp_path), name)).sps()
+    q = 2 * sps[:, 1] + sps[:, 2]
+    d = [int(x) for x in z[0]]
+    occ = set(d)
+    sd = [i for i in d if i >= 40 and q[i] == 2]
+    fp = [i for i in range(40, 80) if q[i] == 3 and i not in occ]
+    up = next(sorted(set(d) - {a, b2} | {c, e}) for a in sd for b2 in sd if a < b2 for c in fp for e in fp
+              if c < e and sps[a, 4] + sps[b2, 4] == sps[c, 4] + sps[e, 4])
+    swapped = list(d)
+    swapped[0], swapped[1] = swapped[1], swapped[0]
+    out = b.locate(np.array([up, swapped], dtype=np.uint16))
+    assert list(out) == [b.n + 1, b.n + 1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_wide_hamiltonian_rows_match_reference(gpu_available, name, tmp_path):
+    import cosmo_gb300 as cg
+    m, g = manifest()[name], golden(name)
+    p = cg.Problem(W.write_case(str(tmp_path), name))
+    b = cg.ManyBodyStates(p)
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
+    rp, c, v = h.upper_rows()
+    assert int(rp[-1]) == m["nnz_upper"]
+    assert conn_hash(rp, c) == m["conn_sha256"]
+    if "vals" in g:
+        np.testing.assert_allclose(v, g["vals"], rtol=0, atol=1e-12)
+    else:
+        for k, r in enumerate(g["sample_rows"]):
+            a, e = int(g["sample_rowptr"][k]), int(g["sample_rowptr"][k + 1])
+            np.testing.assert_allclose(v[int(rp[r]):int(rp[r + 1])], g["sample_vals"][a:e], rtol=0, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_wide_spectrum_0hw(gpu_available, tmp_path):
+    """All 119 states: the exact path against the dense spectrum of the
+    reference's rows, both Davidson engines against the reference's."""
+    import cosmo_gb300 as cg
+    g = golden("spsdpf_0hw")
+    H = O.full_from_upper(g["rowptr"], g["cols"], g["vals"]).toarray()
+    exact = np.linalg.eigvalsh(H)
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    b = cg.ManyBodyStates(p)
+    for prec in (cg.CG_PREC_FP64, cg.CG_PREC_FP32):
+        h = cg.Hamiltonian(p, b, prec)
+        eig, _ = h.dense_eigensolve()
+        np.testing.assert_allclose(eig, exact, rtol=0, atol=1e-9)
+        r = cg.davidson_diagonalization(h, 10, precision=prec, tol_resid=1e-6, block=10, lim=40, algorithm=1)
+        assert r.stats.converged == 10
+        np.testing.assert_allclose(r.eig, g["ref_eig"][:10], rtol=0, atol=1e-6)
+
+
+@pytest.mark.gpu
+def test_wide_davidson_1hw(gpu_available, tmp_path):
+    import cosmo_gb300 as cg
+    g = golden("spsdpf_1hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_1hw"))
+    b = cg.ManyBodyStates(p)
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP32)
+    r = cg.davidson_diagonalization(h, 5, want_vectors=True, precision=cg.CG_PREC_FP32, tol_resid=1e-6, block=5,
+                                    lim=48)
+    assert r.stats.converged == 5
+    np.testing.assert_allclose(r.eig, g["ref_eig"][:5], rtol=0, atol=1e-6)
+    jj, tt = cg.jt_expectations(b, r.vecs)
+    for q in jj:  # 2J of the M = 1/2 states: odd integers
+        x = np.sqrt(4 * q + 1 * 3 + 1) - 1
+        assert abs(x - round(x)) < 1e-5 and round(x) % 2 == 1, jj
+
+
+@pytest.mark.gpu
+def test_wide_jt_of_reference_vectors(gpu_available, tmp_path):
+    import cosmo_gb300 as cg
+    m, g = manifest()["spsdpf_0hw"], golden("spsdpf_0hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    b = cg.ManyBodyStates(p)
+    vecs = g["ref_vecs"]
+    jj, tt = cg.jt_expectations(b, vecs)
+    np.testing.assert_allclose(jj, m["ref_jj"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(tt, m["ref_tt"], rtol=0, atol=1e-9)
+    occ = cg.occupations(b, vecs)
+    assert occ.shape == (len(vecs), 80)
+    np.testing.assert_allclose(occ.sum(1), 33.0, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(occ[:, :40].sum(1), 20.0, rtol=0, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_wide_refused_routes(gpu_available, tmp_path):
+    import cosmo_gb300 as cg
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    b = cg.ManyBodyStates(p)
+    with pytest.raises(cg.CosmoError) as e:
+        cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
+    assert e.value.status == -6  # CG_ERR_UNSUPPORTED
+
+
+def _narrow_cases(tmp):
+    out = [(n, problem_for(n, tmp)) for n in ("sd22m0s1", "fp21m3s6", "sd32m1s2")]
+    import cosmo_gb300 as cg
+    out += [(n, cg.Problem(T.write_case(tmp, n))) for n in ("psd22m0_hw2_rej", "psd32m1_hwr13")]
+    return out
+
+
+@pytest.mark.gpu
+def test_wide_forced_equals_bitstring(gpu_available, tmp_path):
+    import cosmo_gb300 as cg
+    for name, p in _narrow_cases(str(tmp_path)):
+        bn = cg.ManyBodyStates(p)
+        bw = cg.ManyBodyStates(p, wide=True)
+        assert bw.wide and not bn.wide and bw.n == bn.n, name
+        z = bn.states()
+        assert np.array_equal(bw.states(), z), name
+        assert np.array_equal(bw.locate(z), np.arange(bn.n)), name
+        hn = cg.Hamiltonian(p, bn, cg.CG_PREC_FP64)
+        hw = cg.Hamiltonian(p, bw, cg.CG_PREC_FP64)
+        rn, cn, vn = hn.upper_rows()
+        rw, cw, vw = hw.upper_rows()
+        assert np.array_equal(rn, rw) and np.array_equal(cn, cw), name
+        np.testing.assert_allclose(vw, vn, rtol=0, atol=1e-13)
+        np.testing.assert_allclose(hw.diagonal(), hn.diagonal(), rtol=0, atol=1e-13)
+        k = min(4, bn.n)
+        r = cg.davidson_diagonalization(hn, k, want_vectors=True, precision=cg.CG_PREC_FP64, tol_resid=1e-8,
+                                        block=k, lim=min(bn.n, 4 * k), algorithm=1)
+        jn, tn = cg.jt_expectations(bn, r.vecs)
+        jw, tw = cg.jt_expectations(bw, r.vecs)
+        np.testing.assert_allclose(jw, jn, rtol=0, atol=1e-9)
+        np.testing.assert_allclose(tw, tn, rtol=0, atol=1e-9)
+        np.testing.assert_allclose(cg.occupations(bw, r.vecs), cg.occupations(bn, r.vecs), rtol=0, atol=1e-12)
