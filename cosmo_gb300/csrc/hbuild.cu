@@ -480,27 +480,25 @@ void hamiltonian_build(const System& sys, const Operator& op, const Basis& b, in
   dm2.upload(m2, s);
   Ctx c{};
   if (b.wide) {
-    wide = wide_rows(sys, op, b, s);
+    wide = wide_rows(sys, op, b, s);  // valence spaces of more than 32 m-states per species (wide.cu)
   } else {
     upload_operator(sys, op, dop, s);
-  }
-  if (!b.wide) {
-  c.ns = b.ns;
-  c.nn = b.nn;
-  c.npairs = dop.npairs;
-  c.nall = b.nn ? ((b.nn == 64) ? ~0ull : ((1ull << b.nn) - 1)) : 0;
-  c.pall = (b.ns == 64 ? ~0ull : ((1ull << b.ns) - 1)) & ~c.nall;
-  c.n = b.n;
-  c.state = b.state.p;
-  c.noff = b.noff.p;
-  c.pcrank = b.pcrank.p;
-  c.nlist = b.truncated ? b.nlist.p : nullptr;
-  c.lrank = b.truncated ? b.lrank.p : nullptr;
-  c.npc = b.npc;
-  c.e1 = dop.e1.p;
-  c.v2 = dop.v2.p;
-  c.mmask = dop.mmask.p;
-  c.m2 = dm2.p;
+    c.ns = b.ns;
+    c.nn = b.nn;
+    c.npairs = dop.npairs;
+    c.nall = b.nn ? ((b.nn == 64) ? ~0ull : ((1ull << b.nn) - 1)) : 0;
+    c.pall = (b.ns == 64 ? ~0ull : ((1ull << b.ns) - 1)) & ~c.nall;
+    c.n = b.n;
+    c.state = b.state.p;
+    c.noff = b.noff.p;
+    c.pcrank = b.pcrank.p;
+    c.nlist = b.truncated ? b.nlist.p : nullptr;
+    c.lrank = b.truncated ? b.lrank.p : nullptr;
+    c.npc = b.npc;
+    c.e1 = dop.e1.p;
+    c.v2 = dop.v2.p;
+    c.mmask = dop.mmask.p;
+    c.m2 = dm2.p;
   }
 
   const uint64_t n = b.n;
