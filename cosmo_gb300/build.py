@@ -33,8 +33,11 @@ def nvcc() -> str:
 
 
 def _flags(src: str) -> list[str]:
+    # -ffp-contract=off: host arithmetic without fused multiply-adds, so that
+    # the host results (dense eigensolves, XML numbers, level listings) are
+    # the same on x86-64 and aarch64 hosts
     common = ["-std=c++17", "-O3", "-I", os.path.join(ROOT, "include"), "-I", SRC,
-              "-Xcompiler", "-fPIC,-Wall,-Wno-unused-function"]
+              "-Xcompiler", "-fPIC,-Wall,-Wno-unused-function,-ffp-contract=off"]
     if src.endswith(".cu"):
         return common + ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
     return common
@@ -94,7 +97,7 @@ def build_cli() -> list[str]:
 
     def one(name: str) -> str:
         out = os.path.join(BIN_DIR, name)
-        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
                os.path.join(CLI_DIR, name + ".cpp"), "-o", out, "-L", PKG, "-lcosmo_gb300",
                "-Wl,-rpath,$ORIGIN/.."]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -130,6 +130,14 @@ void basis_build_wide(const System& sys, Basis& b);
 void basis_tuples_wide(const Basis& b, uint64_t first, uint64_t count, uint16_t* out);
 uint64_t basis_locate_wide_host(const Basis& b, const uint16_t* tuple);
 void jt_expectations_wide(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt);
+// per-CTA partial sums of the pull-form overlaps (sf.cu) on wide bases: the
+// one-body transition amplitudes (part[cta * 16 + q]) and the removal
+// amplitudes (part[(s * grid + cta) * 16 + q]), 256 threads per CTA
+void wide_onebody_partials(const Basis& parent, const Basis& daughter, const double* psid, int nq,
+                           const double* psip, const int2* tif, const double* tv, int nt, double* part,
+                           unsigned grid, int* err, cudaStream_t s);
+void wide_sf_partials(const Basis& parent, const Basis& daughter, const double* psid, int nq, const double* psip,
+                      const int* sidx, int nsidx, double* part, unsigned grid, int* err, cudaStream_t s);
 // refuses a wide basis on a route that only takes bitstring bases
 void refuse_wide(const Basis& b, const char* route);
 uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom);

@@ -246,8 +246,7 @@ void occupations(const Basis& b, const double* v, int nst, double* occ) {
 void onebody_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                         const double* vd, int nd, const std::vector<OneBodyTerm>& terms, double* amp) {
   if (np < 1 || nd < 1 || nd > kMaxDaughter) throw Error(CG_ERR_ARG, "1..16 daughter states, at least one parent state");
-  refuse_wide(parent, "the transition amplitudes");
-  refuse_wide(daughter, "the transition amplitudes");
+  if (parent.wide != daughter.wide) throw Error(CG_ERR_ARG, "parent and daughter bases of different representations");
   if (parent.ns != daughter.ns || parent.nn != daughter.nn)
     throw Error(CG_ERR_ARG, "parent and daughter bases have different valence spaces");
   if (parent.kn + parent.kp != daughter.kn + daughter.kp)
@@ -308,9 +307,13 @@ void onebody_amplitudes(const System& psys, const Basis& parent, const double* v
   for (int p = 0; p < np; ++p) {
     pv.upload(vp + uint64_t(p) * parent.n, parent.n, st);
     a.psip = pv.p;
-    k_onebody_amplitudes<<<gx, T, 0, st>>>(a, part.p, err.p);
-    CG_CUDA(cudaGetLastError());
-    count_launch();
+    if (parent.wide) {
+      wide_onebody_partials(parent, daughter, psid.p, nd, pv.p, dtif.p, dtv.p, a.nt, part.p, gx, err.p, st);
+    } else {
+      k_onebody_amplitudes<<<gx, T, 0, st>>>(a, part.p, err.p);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+    }
     CG_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
     for (unsigned g = 0; g < gx; ++g)
@@ -325,8 +328,7 @@ void onebody_amplitudes(const System& psys, const Basis& parent, const double* v
 void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, int np, const Basis& daughter,
                    const double* vd, int nd, double* amp) {
   if (np < 1 || nd < 1 || nd > kMaxDaughter) throw Error(CG_ERR_ARG, "1..16 daughter states, at least one parent state");
-  refuse_wide(parent, "the spectroscopic amplitudes");
-  refuse_wide(daughter, "the spectroscopic amplitudes");
+  if (parent.wide != daughter.wide) throw Error(CG_ERR_ARG, "parent and daughter bases of different representations");
   if (parent.ns != daughter.ns || parent.nn != daughter.nn)
     throw Error(CG_ERR_ARG, "parent and daughter bases have different valence spaces");
   const int ns = parent.ns;
@@ -372,9 +374,13 @@ void sf_amplitudes(const System& psys, const Basis& parent, const double* vp, in
   for (int p = 0; p < np; ++p) {
     pv.upload(vp + uint64_t(p) * parent.n, parent.n, st);
     a.psip = pv.p;
-    k_sf_amplitudes<<<grid, T, 0, st>>>(a, part.p, err.p);
-    CG_CUDA(cudaGetLastError());
-    count_launch();
+    if (parent.wide) {
+      wide_sf_partials(parent, daughter, psid.p, nd, pv.p, dsidx.p, int(sidx.size()), part.p, gx, err.p, st);
+    } else {
+      k_sf_amplitudes<<<grid, T, 0, st>>>(a, part.p, err.p);
+      CG_CUDA(cudaGetLastError());
+      count_launch();
+    }
     CG_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
     for (size_t y = 0; y < sidx.size(); ++y)

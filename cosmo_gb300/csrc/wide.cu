@@ -344,6 +344,104 @@ __global__ void k_wide_fill(WCtx c, const uint64_t* __restrict__ rowptr, uint32_
   }
 }
 
+// ------------------------------------------------ overlaps between two bases
+// The pull forms of sf.cu on wide bases: one thread per daughter determinant,
+// the parent determinant located by wide_index on the parent's tables.
+constexpr int kMaxDaughterW = 16;
+
+WCtx locate_ctx(const Basis& b) {
+  WCtx c{};
+  c.ns = b.ns;
+  c.nn = b.nn;
+  c.nblocks = int(b.h_bstart.size());
+  c.truncated = b.truncated;
+  c.n = b.n;
+  c.wstate = b.wstate.p;
+  c.bstart = b.wbstart.p;
+  c.nkey = b.wnkey.p;
+  c.pkey = b.wpkey.p;
+  c.bclass = b.wbclass.p;
+  c.cstart = b.wcstart.p;
+  c.nblk = b.wnblk.p;
+  c.prank = b.wprank.p;
+  return c;
+}
+
+__device__ __forceinline__ void reduce_daughter(const double (&acc)[kMaxDaughterW], double* __restrict__ part,
+                                                size_t slot) {
+  __shared__ double red[kMaxDaughterW][256 / 32];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kMaxDaughterW; ++q) {
+    double v = acc[q];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+    if (lane == 0) red[q][wi] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kMaxDaughterW) {
+    double v = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) v += red[threadIdx.x][i];
+    part[slot * kMaxDaughterW + threadIdx.x] = v;
+  }
+}
+
+// <D_q| sum_t v_t a+_f a_i |P>: P = D - f + i, phase of a+_f a_i on P
+__global__ void __launch_bounds__(256) k_wide_onebody(WCtx par, const uint64_t* __restrict__ dstate, uint64_t nd,
+                                                      const double* __restrict__ psid, int nq,
+                                                      const double* __restrict__ psip, const int2* __restrict__ tif,
+                                                      const double* __restrict__ tv, int nt,
+                                                      double* __restrict__ part, int* __restrict__ err) {
+  double acc[kMaxDaughterW];
+#pragma unroll
+  for (int q = 0; q < kMaxDaughterW; ++q) acc[q] = 0.0;
+  for (uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; row < nd;
+       row += uint64_t(gridDim.x) * blockDim.x) {
+    const Occ D = occ_join(dstate[2 * row], dstate[2 * row + 1], par.nn);
+    double w = 0.0;
+    for (int t = 0; t < nt; ++t) {
+      const int2 e = tif[t];
+      if (!occ_any(D & occ_bit(e.y))) continue;
+      const Occ Df = D & ~occ_bit(e.y);
+      if (e.x != e.y && occ_any(Df & occ_bit(e.x))) continue;
+      const Occ P = e.x == e.y ? D : (Df ^ occ_bit(e.x));
+      const uint64_t idx = wide_index(par, P);
+      if (idx == kOutsideW) continue;
+      if (idx >= par.n) { atomicOr(err, 1); continue; }
+      const int ph = occ_popc_below(P, e.x) + occ_popc_below(Df, e.y);
+      const double v = tv[t] * psip[idx];
+      w += (ph & 1) ? -v : v;
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxDaughterW; ++q)
+      if (q < nq) acc[q] += w * psid[row * nq + q];
+  }
+  reduce_daughter(acc, part, blockIdx.x);
+}
+
+// <D_q| a_s |P>: P = D + s, phase of the states of D below s
+__global__ void __launch_bounds__(256) k_wide_sf(WCtx par, const uint64_t* __restrict__ dstate, uint64_t nd,
+                                                 const double* __restrict__ psid, int nq,
+                                                 const double* __restrict__ psip, const int* __restrict__ sidx,
+                                                 double* __restrict__ part, int* __restrict__ err) {
+  const int s = sidx[blockIdx.y];
+  double acc[kMaxDaughterW];
+#pragma unroll
+  for (int q = 0; q < kMaxDaughterW; ++q) acc[q] = 0.0;
+  for (uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; row < nd;
+       row += uint64_t(gridDim.x) * blockDim.x) {
+    const Occ D = occ_join(dstate[2 * row], dstate[2 * row + 1], par.nn);
+    if (occ_any(D & occ_bit(s))) continue;
+    const uint64_t idx = wide_index(par, D ^ occ_bit(s));
+    if (idx == kOutsideW) continue;
+    if (idx >= par.n) { atomicOr(err, 1); continue; }
+    const double c = ((occ_popc_below(D, s) & 1) ? -1.0 : 1.0) * psip[idx];
+#pragma unroll
+    for (int q = 0; q < kMaxDaughterW; ++q)
+      if (q < nq) acc[q] += c * psid[row * nq + q];
+  }
+  reduce_daughter(acc, part, size_t(blockIdx.y) * gridDim.x + blockIdx.x);
+}
+
 class WideRowsImpl : public WideRows {
  public:
   WideRowsImpl(const System& sys, const Operator& op, const Basis& b, cudaStream_t s) : s_(s) {
@@ -617,6 +715,25 @@ uint64_t basis_locate_wide_host(const Basis& b, const uint16_t* t) {
   auto jt = std::lower_bound(a, e, pmask);
   if (jt == e || *jt != pmask) return miss;
   return b.h_bstart[blk] + b.h_wprank[size_t(jt - b.h_wpkey.begin())];
+}
+
+void wide_onebody_partials(const Basis& parent, const Basis& daughter, const double* psid, int nq,
+                           const double* psip, const int2* tif, const double* tv, int nt, double* part,
+                           unsigned grid, int* err, cudaStream_t s) {
+  if (!parent.wide || !daughter.wide) throw Error(CG_ERR_ARG, "both bases must use the wide representation");
+  k_wide_onebody<<<grid, 256, 0, s>>>(locate_ctx(parent), daughter.wstate.p, daughter.n, psid, nq, psip, tif, tv, nt,
+                                      part, err);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
+}
+
+void wide_sf_partials(const Basis& parent, const Basis& daughter, const double* psid, int nq, const double* psip,
+                      const int* sidx, int nsidx, double* part, unsigned grid, int* err, cudaStream_t s) {
+  if (!parent.wide || !daughter.wide) throw Error(CG_ERR_ARG, "both bases must use the wide representation");
+  k_wide_sf<<<dim3(grid, unsigned(nsidx)), 256, 0, s>>>(locate_ctx(parent), daughter.wstate.p, daughter.n, psid, nq,
+                                                        psip, sidx, part, err);
+  CG_CUDA(cudaGetLastError());
+  count_launch();
 }
 
 void jt_expectations_wide(const System& sys, const Basis& b, const double* vecs, int nst, double* jj, double* tt) {

@@ -201,3 +201,105 @@ def test_wide_forced_equals_bitstring(gpu_available, tmp_path):
         np.testing.assert_allclose(jw, jn, rtol=0, atol=1e-9)
         np.testing.assert_allclose(tw, tn, rtol=0, atol=1e-9)
         np.testing.assert_allclose(cg.occupations(bw, r.vecs), cg.occupations(bn, r.vecs), rtol=0, atol=1e-12)
+
+
+def _random_terms(sps, rng, same_species=True):
+    """Random one-body terms (i, f, v) that keep species, m and parity."""
+    ns = len(sps)
+    nn = int((sps[:, 6] > 0).sum())
+    out = []
+    for i in range(ns):
+        for f in range(ns):
+            if (i < nn) != (f < nn) or sps[i, 4] != sps[f, 4] or sps[i, 7] != sps[f, 7]:
+                continue
+            out.append((i, f, float(rng.standard_normal())))
+    return out
+
+
+@pytest.mark.gpu
+def test_wide_forced_amplitudes_equal_bitstring(gpu_available, tmp_path):
+    """Transition (XSHLEMB) and removal (XSHLSF) amplitudes on wide bases equal
+    the bitstring kernels' on the same systems and vectors."""
+    import cosmo_gb300 as cg
+    from cosmo_gb300.synthetic import SyntheticSystem, make_system
+    rng = np.random.default_rng(5)
+    pp = problem_for("sd22m0s1", str(tmp_path))
+    pd = cg.Problem(make_system(str(tmp_path), SyntheticSystem("sd", 2, 1, 1, "+", 0.5, 1, name="sd21m1s1"))[1])
+    bpn, bpw = cg.ManyBodyStates(pp), cg.ManyBodyStates(pp, wide=True)
+    bdn, bdw = cg.ManyBodyStates(pd), cg.ManyBodyStates(pd, wide=True)
+    vp = rng.standard_normal((3, bpn.n))
+    vd = rng.standard_normal((4, bdn.n))
+    np.testing.assert_allclose(cg.sf_amplitudes(bpw, vp, bdw, vd), cg.sf_amplitudes(bpn, vp, bdn, vd),
+                               rtol=0, atol=1e-12)
+    terms = _random_terms(pp.sps(), rng)
+    vq = rng.standard_normal((5, bpn.n))
+    np.testing.assert_allclose(cg.onebody_amplitudes(bpw, vp, bpw, vq, terms),
+                               cg.onebody_amplitudes(bpn, vp, bpn, vq, terms), rtol=0, atol=1e-12)
+    with pytest.raises(cg.CosmoError):
+        cg.onebody_amplitudes(bpw, vp, bpn, vq, terms)
+
+
+@pytest.mark.gpu
+def test_wide_onebody_amplitudes_spsdpf(gpu_available, tmp_path):
+    """Transition amplitudes between the reference's 0 hw spsdpf vectors on
+    the GPU against the oracle's pull over the reference's .mbs tuples."""
+    import cosmo_gb300 as cg
+    from oracle import transitions as TR
+    g = golden("spsdpf_0hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    b = cg.ManyBodyStates(p)
+    vecs = g["ref_vecs"]
+    terms = _random_terms(p.sps(), np.random.default_rng(7))
+    amp = cg.onebody_amplitudes(b, vecs, b, vecs[:8], terms)
+    ref = TR.onebody_amplitudes(g["mbs"], vecs, g["mbs"], vecs[:8], terms)
+    np.testing.assert_allclose(amp, ref, rtol=0, atol=1e-11 * max(1.0, np.abs(ref).max()))
+
+
+@pytest.mark.gpu
+def test_wide_cli_example_flow(gpu_available, tmp_path):
+    """The command-line flow of the reference's 33Al example (basis tool,
+    DEXHVJTcsb, Xlevels, XSHLAO) on the two spsdpf windows: cg_xsysmbs writes
+    the reference's .mbs; cg_dexhvjt diagonalizes the 119-state window exactly
+    (every state in the .EE, the <state> records of the reference's XSHLJT)
+    and the 23,842-state one by Davidson; cg_xlevels lists both systems'
+    states; cg_xshlao writes occupations."""
+    import hashlib
+    import re
+    import subprocess
+    import cosmo_gb300 as cg
+    bindir = os.path.join(os.path.dirname(cg.__file__), "bin")
+    work = str(tmp_path)
+
+    def run(*args):
+        r = subprocess.run([os.path.join(bindir, args[0])] + list(args[1:]), cwd=work, capture_output=True,
+                           text=True, stdin=subprocess.DEVNULL)
+        assert r.returncode == 0, r.stderr
+        return r
+    m0, m1 = manifest()["spsdpf_0hw"], manifest()["spsdpf_1hw"]
+    xml0 = W.write_case(work, "spsdpf_0hw")
+    xml1 = W.write_case(work, "spsdpf_1hw")
+    for xml, m, tag in ((xml0, m0, "a"), (xml1, m1, "b")):
+        run("cg_xsysmbs", xml, "-o", tag + ".mbs")
+        assert hashlib.sha256(open(os.path.join(work, tag + ".mbs"), "rb").read()).hexdigest() == m["mbs_sha256"]
+    r = run("cg_dexhvjt", xml0, "-n", "10", "-o", "out0.xml")
+    assert "exact diagonalization" in r.stderr
+    E, D, R, V = cg.read_ee(os.path.join(work, "spsdpf_0hw.HH.EE"))
+    g = golden("spsdpf_0hw")
+    exact = np.linalg.eigvalsh(O.full_from_upper(g["rowptr"], g["cols"], g["vals"]).toarray())
+    assert len(E) == 119
+    np.testing.assert_allclose(E, exact, rtol=0, atol=1e-9)
+    txt = open(os.path.join(work, "out0.xml")).read()
+    states = [dict(re.findall(r'(\w+)="([^"]*)"', x)) for x in re.findall(r"<state ([^>]*)>", txt)]
+    ref_states = m0["ref_xshljt_states"]
+    assert [s["J"] for s in states] == [s["J"] for s in ref_states]
+    assert [s["name"] for s in states] == [s["name"] for s in ref_states]
+    for a, b in zip(states, ref_states):
+        assert abs(float(a["E"]) - float(b["E"])) < 2e-4
+    run("cg_dexhvjt", xml1, "-n", "5", "-o", "out1.xml")
+    E1, _, R1, _ = cg.read_ee(os.path.join(work, "spsdpf_1hw.HH.EE"))
+    assert np.all(R1 <= 1e-5)
+    np.testing.assert_allclose(E1, m1["ref_eig"][:5], rtol=0, atol=1e-4)
+    lv = run("cg_xlevels", "out0.xml", "out1.xml", "-o", "levels.xml")
+    assert len(lv.stdout.splitlines()) >= len(states) + 1
+    run("cg_xshlao", "out0.xml", "-o", "ao.xml")
+    assert len(re.findall(r"<occupation ", open(os.path.join(work, "ao.xml")).read())) > 0
