@@ -348,6 +348,39 @@ def em_case(work: str, manifest: dict) -> None:
     print("em", {r: sum(s.count("<transition") for s in v["states"]) for r, v in entry["runs"].items()})
 
 
+def wide_em_case(work: str, manifest: dict) -> None:
+    """E2 transitions among the lowest states of the spsdpf 0 hw window, as
+    step 5 of the reference's 33Al example (XSHLEMB -w -u, en 0.5, ep 1.5):
+    the reference's basis, Davidson vectors (.EE), XSHLJT <state> nodes and
+    XSHLEMB output."""
+    name = "spsdpf_0hw"
+    xml = WIDE.write_case(work, name)
+    txt = open(xml).read().replace("<system ", '<system A="33" ', 1)
+    open(xml, "w").write(txt)
+    run_ref("XsysmbsOMP", xml, name + ".x", work, 0, 0)
+    run_ref("ref_dump", xml, name, work, EM_STATES, 0)
+    txt = open(xml).read()
+    jj = re.search(r'<matrix JJ="([^"]*)"/>', txt)
+    open(xml, "w").write(txt.replace(jj.group(0), f'<matrix name="{name}" format="pp" JJ="{jj.group(1)}"/>'))
+    with open(os.path.join(work, name + ".jt.log"), "w") as log:
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLJT"), xml, "-n", str(EM_STATES)], cwd=work,
+                       stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+    op, flags = '<operator name="E2" J="2" en="0.5" ep="1.5"/>', ["-w", "-u"]
+    xin = os.path.join(work, "em_wide.xml")
+    open(xin, "w").write(open(xml).read().replace("</cosmo>", op + "\n</cosmo>", 1))
+    xout = os.path.join(work, "em_wide.out.xml")
+    with open(os.path.join(work, "em_wide.log"), "w") as log:
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "XSHLEMB"), xin, "-o", xout] + flags, cwd=work,
+                       stdin=subprocess.DEVNULL, stdout=log, stderr=subprocess.STDOUT, check=True)
+    out = open(xout).read()
+    manifest["em_wide"] = {
+        "states": re.findall(r"<state [^>]*>\s*<wavefunction[^>]*/>\s*</state>", open(xml).read()),
+        "operator": op, "flags": flags, "operator_out": re.search(r"<operator [^>]*/>", out).group(0),
+        "out_states": re.findall(r"<state [^>]*>.*?</state>", out, re.S)}
+    np.savez_compressed(os.path.join(HERE, "em_wide.npz"), EE=np.fromfile(os.path.join(work, name + ".EE"), np.uint8))
+    print("em_wide", sum(st.count("<transition") for st in manifest["em_wide"]["out_states"]), "transitions")
+
+
 def hh_case(name: str, work: str, xml: str, manifest: dict, keep_bytes: bool) -> None:
     """The reference's .HH file (XHH+JJ, PPMatrix::Write): sha256, and the bytes
     for one small case so the .HH reader can be pinned on a GPU."""
@@ -438,6 +471,8 @@ def main() -> None:
                                             parity=c["parity"], jj=0.0, seed=WIDE.SEED)
             if c["full"]:
                 jt_case(name, work, xml, c["nstates"], manifest, keep_vecs=True)
+        if not skip("em_wide"):
+            wide_em_case(work, manifest)
         if not skip("mg24usdb"):
             sysd = SyntheticSystem("sd", 4, 4, 0, "+", 0.0, 0, name="mg24usdb")
             xml = os.path.join(work, "mg24usdb.xml")

@@ -16,7 +16,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import conn_hash, golden, manifest, mbs_sha, problem_for
+from conftest import GOLDEN, conn_hash, golden, manifest, mbs_sha, problem_for
 from oracle import oracle as O
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
@@ -303,3 +303,38 @@ def test_wide_cli_example_flow(gpu_available, tmp_path):
     assert len(lv.stdout.splitlines()) >= len(states) + 1
     run("cg_xshlao", "out0.xml", "-o", "ao.xml")
     assert len(re.findall(r"<occupation ", open(os.path.join(work, "ao.xml")).read())) > 0
+
+
+@pytest.mark.gpu
+def test_wide_xshlemb_matches_reference(gpu_available, tmp_path):
+    """Step 5 of the 33Al example on the spsdpf 0 hw window: E2 transitions
+    (-w -u, en 0.5, ep 1.5) among the reference's own lowest states (its .EE
+    and XSHLJT <state> nodes); B, Weisskopf and Bu within 1e-6 + 1e-5
+    relative of the 6 digits the reference XSHLEMB writes."""
+    import re
+    import cosmo_gb300 as cg
+    m = manifest()["em_wide"]
+    work = str(tmp_path)
+    xml = W.write_case(work, "spsdpf_0hw")
+    txt = open(xml).read().replace("<system ", '<system A="33" ', 1)
+    jj = re.search(r'<matrix JJ="([^"]*)"/>', txt)
+    txt = txt.replace(jj.group(0), f'<matrix name="spsdpf_0hw" format="pp" JJ="{jj.group(1)}"/>')
+    txt = txt.replace("</system>", "".join(m["states"]) + "</system>", 1)
+    pin = os.path.join(work, "em_wide.xml")
+    open(pin, "w").write(txt.replace("</cosmo>", m["operator"] + "\n</cosmo>", 1))
+    np.load(os.path.join(GOLDEN, "em_wide.npz"))["EE"].tofile(os.path.join(work, "spsdpf_0hw.EE"))
+    out = os.path.join(work, "out.xml")
+    cg.xshlemb(pin, out, weisskopf=True, units=True)
+
+    def attrs(t):
+        return dict(re.findall(r'(\w+)="([^"]*)"', t))
+    mine = re.findall(r"<state [^>]*>.*?</state>", open(out).read(), re.S)
+    ref = m["out_states"]
+    assert len(mine) == len(ref) and sum(x.count("<transition") for x in ref) > 0
+    for a, b in zip(mine, ref):
+        ta = [attrs(t) for t in re.findall(r"<transition [^>]*/>", a)]
+        tb = [attrs(t) for t in re.findall(r"<transition [^>]*/>", b)]
+        assert [t["final"] for t in ta] == [t["final"] for t in tb]
+        for x, y in zip(ta, tb):
+            for key in ("B", "weisskopf", "Bu"):
+                assert abs(float(x[key]) - float(y[key])) <= 1e-6 + 1e-5 * abs(float(y[key])), (key, x, y)
