@@ -466,11 +466,15 @@ def main() -> None:
             xml = WIDE.write_case(work, name)
             run_ref("XsysmbsOMP", xml, name + ".x", work, 0, 0)
             dump_case(name, work, xml, c["full"], c["nstates"], 0, manifest)
-            manifest[name]["truncation"] = dict(hw=list(c["hw"]), rejections=[])
+            manifest[name]["truncation"] = dict(hw=list(c["hw"]) if c["hw"] else None, rejections=[])
             manifest[name]["system"] = dict(space="spsdpf", nv=c["nv"], zv=c["zv"], twom=c["twom"],
                                             parity=c["parity"], jj=0.0, seed=WIDE.SEED)
             if c["full"]:
                 jt_case(name, work, xml, c["nstates"], manifest, keep_vecs=True)
+            if name != "spsdpf_0hw":  # same interaction: its terms are pinned on the 0 hw case
+                path = os.path.join(HERE, name + ".npz")
+                arrays = {k: v for k, v in np.load(path).items() if not k.startswith(("esp_", "vspx_"))}
+                np.savez_compressed(path, **arrays)
         if not skip("em_wide"):
             wide_em_case(work, manifest)
         if not skip("mg24usdb"):

@@ -2,7 +2,7 @@
 (0s, 0p, 1s0d, 1p0f in the order of the reference's interactions/int.xml:
 40 m-states per species), 20 neutrons and 13 protons with 2Jz = 1, the 0 hw
 positive-parity window (119 states) and the 1 hw negative-parity one (23,842
-states) of the example.  A seeded synthetic interaction stands in for fsu (the
+states) of the example, and an untruncated 2 neutrons + 1 proton system.  A seeded synthetic interaction stands in for fsu (the
 bases are the example's, the spectra are not).  Shared by the fixture script
 (make_golden.py, which runs the reference's XsysmbsOMP and ref_dump on these
 XML files) and the tests (which rebuild the same XML)."""
@@ -20,6 +20,8 @@ SEED = 33
 CASES = {
     "spsdpf_0hw": dict(nv=20, zv=13, twom=1, parity="+", hw=(0, 0), nstates=10, full=True),
     "spsdpf_1hw": dict(nv=20, zv=13, twom=1, parity="-", hw=(1, 1), nstates=5, full=False),
+    # untruncated: every configuration of 2 neutrons and 1 proton in the 40 m-states
+    "spsdpf_21": dict(nv=2, zv=1, twom=1, parity="-", hw=None, nstates=5, full=True),
 }
 
 
@@ -33,8 +35,9 @@ def write_case(workdir: str, name: str) -> str:
     write_int(ip, SPSDPF_ORBITS, -8.0, SEED)
     write_xml(xp, sysd, os.path.abspath(ip), SPSDPF_ORBITS)
     txt = open(xp).read()
-    lo, hi = c["hw"]
-    txt = txt.replace("<matrix JJ", f'<hwrejection HWMIN="{lo}" HWMAX="{hi}"/><matrix JJ', 1)
+    if c["hw"] is not None:
+        lo, hi = c["hw"]
+        txt = txt.replace("<matrix JJ", f'<hwrejection HWMIN="{lo}" HWMAX="{hi}"/><matrix JJ', 1)
     with open(xp, "w") as f:
         f.write(txt)
     return xp

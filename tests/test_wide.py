@@ -72,20 +72,23 @@ def test_wide_basis_matches_reference(gpu_available, name, tmp_path):
     z = b.states()
     assert mbs_sha(z) == m["mbs_sha256"]
     assert np.array_equal(b.locate(z), np.arange(b.n))
-    # misses: a determinant two oscillator quanta up (two sd protons moved into
-    # the fp shell, M and parity kept) and a wrongly ordered tuple
-    sps = cg.Problem(W.write_case(str(tmp_path), name)).sps()
-    q = 2 * sps[:, 1] + sps[:, 2]
+    # misses: a wrongly ordered tuple and, in a truncated window, a determinant
+    # two oscillator quanta up (two sd protons moved into the fp shell, M and
+    # parity kept)
     d = [int(x) for x in z[0]]
-    occ = set(d)
-    sd = [i for i in d if i >= 40 and q[i] == 2]
-    fp = [i for i in range(40, 80) if q[i] == 3 and i not in occ]
-    up = next(sorted(set(d) - {a, b2} | {c, e}) for a in sd for b2 in sd if a < b2 for c in fp for e in fp
-              if c < e and sps[a, 4] + sps[b2, 4] == sps[c, 4] + sps[e, 4])
     swapped = list(d)
     swapped[0], swapped[1] = swapped[1], swapped[0]
-    out = b.locate(np.array([up, swapped], dtype=np.uint16))
-    assert list(out) == [b.n + 1, b.n + 1]
+    probes = [swapped]
+    if W.CASES[name]["hw"] is not None:
+        sps = cg.Problem(W.write_case(str(tmp_path), name)).sps()
+        q = 2 * sps[:, 1] + sps[:, 2]
+        occ = set(d)
+        sd = [i for i in d if i >= 40 and q[i] == 2]
+        fp = [i for i in range(40, 80) if q[i] == 3 and i not in occ]
+        probes.append(next(sorted(set(d) - {a, b2} | {c, e}) for a in sd for b2 in sd if a < b2 for c in fp
+                           for e in fp if c < e and sps[a, 4] + sps[b2, 4] == sps[c, 4] + sps[e, 4]))
+    out = b.locate(np.array(probes, dtype=np.uint16))
+    assert list(out) == [b.n + 1] * len(probes)
 
 
 @pytest.mark.gpu
@@ -338,3 +341,25 @@ def test_wide_xshlemb_matches_reference(gpu_available, tmp_path):
         for x, y in zip(ta, tb):
             for key in ("B", "weisskopf", "Bu"):
                 assert abs(float(x[key]) - float(y[key])) <= 1e-6 + 1e-5 * abs(float(y[key])), (key, x, y)
+
+
+@pytest.mark.gpu
+def test_wide_untruncated_spectrum_and_product(gpu_available, tmp_path):
+    """Untruncated wide basis (2 neutrons and 1 proton in the spsdpf space):
+    the stored product against the reference's SpMM output, the 5 lowest
+    states against the reference's Davidson, <J-J+> and <T-T+> of the
+    reference's vectors."""
+    import cosmo_gb300 as cg
+    m, g = manifest()["spsdpf_21"], golden("spsdpf_21")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_21"))
+    b = cg.ManyBodyStates(p)
+    assert b.wide and b.n == m["n"]
+    h = cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
+    y = h.times_matrix(g["spmm_x"].T.copy())
+    np.testing.assert_allclose(y, g["spmm_y"].T, rtol=0, atol=1e-11 * np.abs(g["spmm_y"]).max())
+    r = cg.davidson_diagonalization(h, 5, precision=cg.CG_PREC_FP64, tol_resid=1e-7, block=5, lim=40, algorithm=1)
+    assert r.stats.converged == 5
+    np.testing.assert_allclose(r.eig, g["ref_eig"], rtol=0, atol=1e-6)
+    jj, tt = cg.jt_expectations(b, g["ref_vecs"])
+    np.testing.assert_allclose(jj, m["ref_jj"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(tt, m["ref_tt"], rtol=0, atol=1e-9)
