@@ -932,7 +932,6 @@ void batch_build(const std::vector<const System*>& sys, const std::vector<const 
   for (int p = 0; p < P; ++p) {
     Basis b;
     basis_build(*sys[p], b);
-    refuse_wide(b, "the batched solver");
     bs.dims[p] = b.n;
     if (b.n == 0) continue;
     hs[p] = std::make_unique<Hamiltonian>();

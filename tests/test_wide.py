@@ -363,3 +363,16 @@ def test_wide_untruncated_spectrum_and_product(gpu_available, tmp_path):
     jj, tt = cg.jt_expectations(b, g["ref_vecs"])
     np.testing.assert_allclose(jj, m["ref_jj"], rtol=0, atol=1e-9)
     np.testing.assert_allclose(tt, m["ref_tt"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_wide_batched(gpu_available, tmp_path):
+    """Wide and bitstring systems solved together in lockstep (the batched
+    solver takes the wide bases' rows like any other)."""
+    import cosmo_gb300 as cg
+    probs = [cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw")),
+             cg.Problem(W.write_case(str(tmp_path), "spsdpf_21")), problem_for("sd22m0s1", str(tmp_path))]
+    eig, res, nconv, _ = cg.Batch(probs).solve(3)
+    np.testing.assert_allclose(eig[0], golden("spsdpf_0hw")["ref_eig"][:3], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(eig[1], golden("spsdpf_21")["ref_eig"][:3], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(eig[2], golden("sd22m0s1")["ref_eig"][:3], rtol=0, atol=1e-4)
