@@ -33,11 +33,13 @@ def nvcc() -> str:
 
 
 def _flags(src: str) -> list[str]:
-    # -ffp-contract=off: host arithmetic without fused multiply-adds, so that
-    # the host results (dense eigensolves, XML numbers, level listings) are
-    # the same on x86-64 and aarch64 hosts
-    common = ["-std=c++17", "-O3", "-I", os.path.join(ROOT, "include"), "-I", SRC,
-              "-Xcompiler", "-fPIC,-Wall,-Wno-unused-function,-ffp-contract=off"]
+    host = "-fPIC,-Wall,-Wno-unused-function"
+    if src == "xshljt.cpp":
+        # the level listing's RMS over one experimental level is the difference
+        # of two equal squares: without fused multiply-adds it is 0 on x86-64
+        # and aarch64 hosts alike, as the reference prints it
+        host += ",-ffp-contract=off"
+    common = ["-std=c++17", "-O3", "-I", os.path.join(ROOT, "include"), "-I", SRC, "-Xcompiler", host]
     if src.endswith(".cu"):
         return common + ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
     return common
