@@ -584,6 +584,7 @@ cg_status cg_xshlsf(const char* parent_xml, const char* parent_system, const cha
     const std::string px = parent_xml, dx = daughter_xml ? daughter_xml : parent_xml;
     cg::xshlsf(px, parent_system ? parent_system : "", dx, daughter_system ? daughter_system : "",
                out_path ? out_path : "", full != 0);
+    std::fflush(stdout);  // the tool's listing leaves the library with the call
   });
 }
 
@@ -647,6 +648,7 @@ cg_status cg_xshlemb(const char* parent_xml, const char* parent_system, const ch
     o.op_name = op_name ? op_name : "";
     cg::xshlemb(parent_xml, parent_system ? parent_system : "", daughter_xml ? daughter_xml : "",
                 daughter_system ? daughter_system : "", out_xml ? out_xml : "", o);
+    std::fflush(stdout);  // the tool's listing leaves the library with the call
   });
 }
 
@@ -913,6 +915,7 @@ cg_status cg_xshlao(const char* xml_path, const char* system_name, const char* o
     CG_NOT_NULL(xml_path);
     require_device();
     cg::xshlao(xml_path, system_name ? system_name : "", out_xml ? out_xml : "");
+    std::fflush(stdout);  // the tool's listing leaves the library with the call
   });
 }
 
@@ -925,6 +928,7 @@ cg_status cg_xlevels(const char* const* files, int32_t nfiles, const char* out_x
       CG_NOT_NULL(files[i]);
       f.emplace_back(files[i]);
     }
+    std::fflush(stdout);
     const std::string out = cg::xlevels(f, out_xml ? out_xml : "");
     std::fwrite(out.data(), 1, out.size(), stdout);
     std::fflush(stdout);
