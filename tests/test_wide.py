@@ -50,6 +50,23 @@ def test_oracle_pruned_equals_filtered(name, tmp_path):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["spsdpf_0hw", "spsdpf_21"])
+def test_oracle_rows_wide_match_reference(name, tmp_path):
+    """The oracle's tuple-based row builder (no width limit on the s.p.
+    index) on the pruned basis: the reference's rows, connectivity bit-exact,
+    values within 1e-12."""
+    import cosmo_gb300 as cg
+    m, g = manifest()[name], golden(name)
+    p = cg.Problem(W.write_case(str(tmp_path), name))
+    inf = p.info
+    z = O.basis_pruned(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw=W.CASES[name]["hw"])
+    k1, v1 = p.one_body()
+    k2, v2 = p.two_body()
+    rp, c, v = O.build_upper(inf.n_sps, k1, v1, k2, v2, z)
+    assert conn_hash(rp, c) == m["conn_sha256"]
+    np.testing.assert_allclose(v, g["vals"], rtol=0, atol=1e-12)
+
+
 def test_wide_operator_terms_match_reference(tmp_path):
     import cosmo_gb300 as cg
     g = golden("spsdpf_0hw")
