@@ -41,3 +41,43 @@ def write_case(workdir: str, name: str) -> str:
     with open(xp, "w") as f:
         f.write(txt)
     return xp
+
+
+# The reference's own 33Al example (EXAMPLE-33Al-fsu.md) with its fsu9
+# interaction files, which stay in the reference checkout: the system node
+# the reference's XML creator writes (Av, Nv, Zv, A, Tz, Jz, P and the hw
+# window), the fsu9 file list of the reference's interactions/int.xml (its
+# formulascale element is read by no reference code), and the levels the
+# example prints (Xlevels: name, T, Ex, E).
+FSU9_FILES = [("spsdpfpb.int", ""),
+              ("fsu9/spsdfp-fsu9.int", '<formulascale rank="2">(18/A)^0.3</formulascale>'),
+              ("fsu9/0p1sd.int", ""), ("fsu9/0p3sd.int", ""), ("0s0f1p0.int", ""),
+              ("spsdpfcm.int", '<scale rank="1">10.000000</scale><scale rank="2">10.000000</scale>')]
+EXAMPLE_33AL = {"+": (0, 0, 119), "-": (1, 1, 23842)}
+EXAMPLE_33AL_LEVELS = [("5/2+(1)", -303.079), ("1/2-(1)", -301.132), ("7/2-(1)", -299.928),
+                       ("5/2-(1)", -299.874), ("3/2-(1)", -299.817)]
+
+
+def write_33al(workdir: str, int_dir: str, parity: str) -> str:
+    """The example's system of one parity with the fsu9 files read from
+    int_dir (the reference's interactions/spsdpf); returns the XML path."""
+    hwmin, hwmax, _ = EXAMPLE_33AL[parity]
+    os.makedirs(workdir, exist_ok=True)
+    out = ['<?xml version="1.0"?>', '<cosmo version="4.1">', ' <valencespace name="spsdpf">',
+           '  <core name="0n" N="0" Z="0"/>']
+    for i, (nm, n, l, tj) in enumerate(SPSDPF_ORBITS):
+        j = f"{tj}/2"
+        out.append(f'  <orbital name="{nm}" n="{n}" l="{l}" j="{j}" type="pn" index="{i + 1}"/>')
+    out.append(" </valencespace>")
+    out.append(' <hamiltonian name="fsu9" valencespace="spsdpf">')
+    for f, extra in FSU9_FILES:
+        out.append(f'  <file format="ascii"><name>{os.path.join(int_dir, f)}</name>{extra}</file>')
+    out.append(" </hamiltonian>")
+    name = f"33Al_fsu9_M1T7{parity}"
+    out.append(f' <system Av="33" Nv="20" Zv="13" A="33" Tz="7/2" Jz="1/2" P="{parity}" name="{name}">'
+               f'<hwrejection HWMAX="{hwmax}" HWMIN="{hwmin}"/></system>')
+    out.append("</cosmo>")
+    path = os.path.join(workdir, f"33Al_fsu9{parity}.xml")
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+    return path

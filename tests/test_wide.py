@@ -393,3 +393,27 @@ def test_wide_batched(gpu_available, tmp_path):
     np.testing.assert_allclose(eig[0], golden("spsdpf_0hw")["ref_eig"][:3], rtol=0, atol=1e-4)
     np.testing.assert_allclose(eig[1], golden("spsdpf_21")["ref_eig"][:3], rtol=0, atol=1e-4)
     np.testing.assert_allclose(eig[2], golden("sd22m0s1")["ref_eig"][:3], rtol=0, atol=1e-4)
+
+
+def test_example_33al_known_answers(tmp_path):
+    """The reference's 33Al example with its fsu9 interaction (needs the
+    reference checkout, COSMO_REFERENCE; skipped elsewhere): the basis tool's
+    counts (119 and 23,842, the oracle's pruned enumeration) and the printed
+    ground state 5/2+ at -303.079 MeV from the library's operator terms and
+    the oracle's rows of the 0 hw window."""
+    root = O.reference_root()
+    int_dir = os.path.join(root, "interactions", "spsdpf") if root else ""
+    if not os.path.exists(os.path.join(int_dir, "fsu9", "spsdfp-fsu9.int")):
+        pytest.skip("reference checkout not given (COSMO_REFERENCE)")
+    import cosmo_gb300 as cg
+    for parity, (lo, hi, n) in W.EXAMPLE_33AL.items():
+        p = cg.Problem(W.write_33al(str(tmp_path), int_dir, parity))
+        inf = p.info
+        z = O.basis_pruned(p.sps(), inf.nv, inf.zv, inf.twom, inf.parity, hw=(lo, hi))
+        assert len(z) == n
+        if parity == "+":
+            k1, v1 = p.one_body()
+            k2, v2 = p.two_body()
+            rp, c, v = O.build_upper(inf.n_sps, k1, v1, k2, v2, z)
+            e = np.linalg.eigvalsh(O.full_from_upper(rp, c, v).toarray())
+            assert abs(e[0] - W.EXAMPLE_33AL_LEVELS[0][1]) < 5e-4
