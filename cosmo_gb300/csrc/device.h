@@ -115,6 +115,10 @@ struct Basis {
   std::vector<uint32_t> h_wnblk, h_wprank;   // block of each sorted neutron mask; rank of each sorted member
   DBuf<uint64_t> wbstart, wnkey, wpkey;
   DBuf<uint32_t> wbclass, wcstart, wnblk, wprank;
+  // every enumerated proton configuration (lexicographic) with its rank in, and
+  // the size of, its (2m, parity) class (the on-the-fly product's class ranks)
+  std::vector<uint64_t> h_wpuniv;
+  std::vector<uint32_t> h_wpuniv_rank, h_wpuniv_csize;
   // host copies used for locate and .mbs output
   std::vector<uint64_t> h_noff;
   std::vector<uint32_t> h_pcrank;

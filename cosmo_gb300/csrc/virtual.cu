@@ -19,8 +19,10 @@
 // balancing 2m change, gathering from shared memory.
 #include <algorithm>
 #include <chrono>
+#include <functional>
 #include <map>
 #include <numeric>
+#include <unordered_map>
 
 #include "bulk.h"
 #include "dfloat.h"
@@ -36,6 +38,16 @@ constexpr int kVirtualSmemHead = 128;  // three mbarriers; keeps the staging buf
 
 inline int popc(uint64_t x) { return __builtin_popcountll(x); }
 inline uint64_t below_h(int b) { return b >= 64 ? ~0ull : (1ull << b) - 1ull; }
+// global occupation words (neutron s.p. states from bit 0, protons above) of
+// up to 128 s.p. states, host only
+using G = unsigned __int128;
+inline int popg(G x) { return __builtin_popcountll(uint64_t(x)) + __builtin_popcountll(uint64_t(x >> 64)); }
+inline G below_g(int b) { return b >= 128 ? ~G(0) : ((G(1) << b) - 1); }
+inline G gbit(int b) { return G(1) << b; }
+inline int ctzg(G x) {
+  const uint64_t lo = uint64_t(x);
+  return lo ? __builtin_ctzll(lo) : 64 + __builtin_ctzll(uint64_t(x >> 64));
+}
 
 struct HostOp {
   int ns = 0, np_pairs = 0;
@@ -46,16 +58,16 @@ struct HostOp {
     return v2[size_t(pidx[a * ns + b]) * np_pairs + pidx[c * ns + d]];
   }
   // forward two-body term (b0 < b1 annihilated, b2 < b3 created) on S0
-  double term2(uint64_t S0, int b0, int b1, int b2, int b3) const {
+  double term2(G S0, int b0, int b1, int b2, int b3) const {
     double v = V(b0, b1, b2, b3);
-    int p = popc(S0 & below_h(b0)) + popc(S0 & below_h(b1)) - 1;
-    uint64_t I = S0 & ~((1ull << b0) | (1ull << b1));
-    p += popc(I & below_h(b2)) + popc(I & below_h(b3));
+    int p = popg(S0 & below_g(b0)) + popg(S0 & below_g(b1)) - 1;
+    G I = S0 & ~(gbit(b0) | gbit(b1));
+    p += popg(I & below_g(b2)) + popg(I & below_g(b3));
     return (p & 1) ? -v : v;
   }
-  double term1(uint64_t S0, int x, int y) const {
+  double term1(G S0, int x, int y) const {
     double v = e1[x * ns + y];
-    int p = popc(S0 & below_h(x)) + popc((S0 & ~(1ull << x)) & below_h(y));
+    int p = popg(S0 & below_g(x)) + popg((S0 & ~gbit(x)) & below_g(y));
     return (p & 1) ? -v : v;
   }
 };
@@ -91,8 +103,9 @@ inline int move_sign(uint64_t mask, int from, int to) {
 struct VArgs {
   int nn, np, ndm, dm0, lmax;
   const uint64_t* bstart;
-  const uint32_t *blen, *bclass, *bmask, *order;
-  const uint32_t *cstart, *cmask;
+  const uint32_t *blen, *bclass, *order;
+  const void *bmask, *cmask;  // species masks: uint32_t, or uint64_t for a wide basis
+  const uint32_t* cstart;
   const uint32_t* nt_off;
   const NTrans* nt;
   const uint32_t* nn_off;
@@ -117,6 +130,9 @@ struct VTab {
   const T* sl_c;  // P1 value without neutron spectators, parallel to sl_e
   const T* pp_h;  // PP2 values, parallel to pp_rank
 };
+
+__device__ __forceinline__ int lowbit(uint32_t w) { return __ffs(w) - 1; }
+__device__ __forceinline__ int lowbit(unsigned long long w) { return __ffsll((long long)w) - 1; }
 
 using bulk::bulk_load;
 using bulk::fence_mbar_init;
@@ -219,8 +235,11 @@ __device__ __forceinline__ void vmac(T (&acc)[VB], DF2 v, const T (&x)[VB]) {
 // then hold class ranks of the target configuration; the class-to-list map
 // of every staged block comes into shared memory with its x rows, and a
 // target outside the basis is skipped.  NN2 reads the target's map from global
-// memory.
-template <class T, int VB, int RPT, bool DF, bool TR>
+// memory.  M: the species-mask type (uint64_t for a wide basis, which always
+// takes the TR form).  ST = false (blocks whose staging does not fit in
+// shared memory): the own block, the target blocks and their class-to-list
+// maps are read from global memory (L2) instead of being staged.
+template <class T, int VB, int RPT, bool DF, bool TR, class M, bool ST>
 __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab<T> tb, VTab<T> tl,
                                                                    const T* __restrict__ x, void* __restrict__ yv,
                                                                    int ldy, int m, int* __restrict__ err) {
@@ -230,14 +249,15 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int npp = a.np * a.np, nw = npp + 4;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
+  const size_t stg = ST ? size_t(a.lmax) * VB : 0;
   T* own = reinterpret_cast<T*>(smem_raw + kVirtualSmemHead);
-  T* buf0 = own + size_t(a.lmax) * VB;
-  T* buf1 = buf0 + size_t(a.lmax) * VB;
-  V* wsl0 = reinterpret_cast<V*>(buf1 + size_t(a.lmax) * VB);
+  T* buf0 = own + stg;
+  T* buf1 = buf0 + stg;
+  V* wsl0 = reinterpret_cast<V*>(buf1 + stg);
   V* wsl1 = wsl0 + nw;
   V* un0 = wsl1 + nw;
-  V* un1 = un0 + 32;
-  V* Pp = un1 + 32;
+  V* un1 = un0 + a.np;
+  V* Pp = un1 + a.np;
   // TR: class-to-list maps of the own block and the two staged blocks, from the
   // first 16-byte boundary after Pp
   uint16_t* rown = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(Pp + npp + 1) + 15) & ~uintptr_t(15));
@@ -253,7 +273,8 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   const int L = int(a.blen[beta]);
   const uint32_t cls = a.bclass[beta];
   const uint32_t cs = a.cstart[cls], slice0 = a.cslice[cls];
-  const uint32_t nmask = a.bmask[beta];
+  const M nmask = static_cast<const M*>(a.bmask)[beta];
+  const M* cmask = static_cast<const M*>(a.cmask);
   const uint32_t t0 = a.nt_off[beta], t1 = a.nt_off[beta + 1];
 
   if (tid == 0) {
@@ -266,7 +287,7 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
   for (int i = tid; i <= npp; i += NT) {
     V s = vfrom<V>(0.0);
     if (i < npp)
-      for (uint32_t w = nmask; w; w &= w - 1) s = vadd(s, vtab<V>(tb.Up, tl.Up, size_t(i) * a.nn + (__ffs(w) - 1)));
+      for (M w = nmask; w; w &= w - 1) s = vadd(s, vtab<V>(tb.Up, tl.Up, size_t(i) * a.nn + lowbit(w)));
     Pp[i] = s;
   }
   if (tid == 0) {
@@ -286,10 +307,17 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       bulk_load(dst, x + a.bstart[blk] * VB, xb, bar);
     }
   };
-  if (tid == 0) {
+  if (ST && tid == 0) {
     stage(own, rown, beta, &mbar[2]);
     if (t0 < t1) stage(buf0, rbuf0, a.nt[t0].target, &mbar[0]);
   }
+  // where the own block's rows and map are read from
+  const T* ownx = ST ? own : x + start * VB;
+  auto ldrow = [&](Row<T, VB>& xr, const T* p) {
+    if constexpr (ST) xr.load_s(p, sw);
+    else xr.load_g(p, sw);
+  };
+  const uint16_t* rownp = ST ? rown : (TR ? a.lmap + a.lmap_off[cls] : nullptr);
   // TR: class rank of each own row's proton configuration
   uint32_t gr[RPT];
 #pragma unroll
@@ -327,7 +355,7 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       }
     }
   }
-  {
+  if constexpr (ST) {
     const bool ok = mbar_wait(&mbar[2], 0);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
@@ -349,12 +377,12 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       const uint32_t sl = slice0 + uint32_t(rb >> 5);
       Row<T, VB> xr;
       if (r < L) {
-        xr.load_s(own + size_t(r) * VB, sw);
+        ldrow(xr, ownx + size_t(r) * VB);
         vmac(acc[k], vfrom<V>(a.diag[start + r]), xr.v);
       }
       for (uint32_t e = a.pp_off[sl] + lane, e1 = a.pp_off[sl + 1]; e < e1; e += 32) {
         const V h = vtab<V>(tb.pp_h, tl.pp_h, e);
-        xr.load_s(own + size_t(a.pp_rank[e]) * VB, sw);
+        ldrow(xr, ownx + size_t(a.pp_rank[e]) * VB);
         vmac(acc[k], h, xr.v);
       }
       const size_t o = size_t(sl) * a.ndm + a.dm0;
@@ -363,13 +391,13 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
         V v = Pp[(q >> 16) & 0x7ff];
         v = vadd(vtab<V>(tb.sl_c, tl.sl_c, e), ((q >> 27) & 1) ? vneg(v) : v);
         if constexpr (TR) {
-          const uint32_t rr = rown[q & 0xffff];
+          const uint32_t rr = rownp[q & 0xffff];
           if (rr != 0xffffu) {
-            xr.load_s(own + size_t(rr) * VB, sw);
+            ldrow(xr, ownx + size_t(rr) * VB);
             vmac(acc[k], v, xr.v);
           }
         } else {
-          xr.load_s(own + size_t(q & 0xffff) * VB, sw);
+          ldrow(xr, ownx + size_t(q & 0xffff) * VB);
           vmac(acc[k], v, xr.v);
         }
       }
@@ -393,20 +421,22 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
       un[tid] = tr.sign ? vneg(w) : w;
     }
     __syncthreads();
-    if (tid == 0 && t + 1 < t1) stage(jb ? buf0 : buf1, jb ? rbuf0 : rbuf1, a.nt[t + 1].target, &mbar[jb ^ 1]);
-    const bool ok = mbar_wait(&mbar[jb], (u >> 1) & 1);
-    if (__syncthreads_or(!ok)) {
-      // give the copies in flight a second bounded wait, report, leave
-      if (tid == 0) {
-        atomicOr(err, 1);
-        mbar_wait(&mbar[jb], (u >> 1) & 1);
-        if (t + 1 < t1) mbar_wait(&mbar[jb ^ 1], ((u + 1) >> 1) & 1);
+    if constexpr (ST) {
+      if (tid == 0 && t + 1 < t1) stage(jb ? buf0 : buf1, jb ? rbuf0 : rbuf1, a.nt[t + 1].target, &mbar[jb ^ 1]);
+      const bool ok = mbar_wait(&mbar[jb], (u >> 1) & 1);
+      if (__syncthreads_or(!ok)) {
+        // give the copies in flight a second bounded wait, report, leave
+        if (tid == 0) {
+          atomicOr(err, 1);
+          mbar_wait(&mbar[jb], (u >> 1) & 1);
+          if (t + 1 < t1) mbar_wait(&mbar[jb ^ 1], ((u + 1) >> 1) & 1);
+        }
+        __syncthreads();
+        return;
       }
-      __syncthreads();
-      return;
     }
-    const T* bf = jb ? buf1 : buf0;
-    const uint16_t* rbf = jb ? rbuf1 : rbuf0;
+    const T* bf = ST ? (jb ? buf1 : buf0) : x + a.bstart[tr.target] * VB;
+    const uint16_t* rbf = ST ? (jb ? rbuf1 : rbuf0) : (TR ? a.lmap + a.lmap_off[a.bclass[tr.target]] : nullptr);
     const int dmp = a.ndm - 2 - (tr.dmi & ~1) + (tr.dmi & 1);  // opposite 2m change, same parity change
     const V cn = vfrom<V>(tr.cn);
 #pragma unroll
@@ -424,11 +454,11 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
           if constexpr (TR) {
             const uint32_t rr = rbf[q & 0xffff];
             if (rr != 0xffffu) {
-              xr.load_s(bf + size_t(rr) * VB, sw);
+              ldrow(xr, bf + size_t(rr) * VB);
               vmac(acc[k], w, xr.v);
             }
           } else {
-            xr.load_s(bf + size_t(q & 0xffff) * VB, sw);
+            ldrow(xr, bf + size_t(q & 0xffff) * VB);
             vmac(acc[k], w, xr.v);
           }
         }
@@ -437,9 +467,9 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
           const uint32_t rn = TR ? uint32_t(rbf[gr[k]]) : uint32_t(r);
           if (rn != 0xffffu) {
             V v = cn;
-            for (uint32_t w = a.cmask[cs + r]; w; w &= w - 1) v = vadd(v, un[__ffs(w) - 1]);
+            for (M w = cmask[cs + r]; w; w &= w - 1) v = vadd(v, un[lowbit(w)]);
             Row<T, VB> xr;
-            xr.load_s(bf + size_t(rn) * VB, sw);
+            ldrow(xr, bf + size_t(rn) * VB);
             vmac(acc[k], v, xr.v);
           }
         }
@@ -471,9 +501,10 @@ __global__ void __launch_bounds__(RPT <= 2 ? 1024 : 512) k_virtual(VArgs a, VTab
 }
 
 // diagonal of every row: En(block) + Ep(proton configuration) + pn part
+template <class M>
 __global__ void k_virtual_diag(uint64_t n, int nblocks, const uint64_t* __restrict__ bstart,
-                               const uint32_t* __restrict__ bclass, const uint32_t* __restrict__ bmask,
-                               const uint32_t* __restrict__ cstart, const uint32_t* __restrict__ cmask,
+                               const uint32_t* __restrict__ bclass, const M* __restrict__ bmask,
+                               const uint32_t* __restrict__ cstart, const M* __restrict__ cmask,
                                const double* __restrict__ En, const double* __restrict__ Ep,
                                const double* __restrict__ Vd, int np, double* __restrict__ diag) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -485,18 +516,18 @@ __global__ void k_virtual_diag(uint64_t n, int nblocks, const uint64_t* __restri
   }
   const uint32_t g = cstart[bclass[lo]] + uint32_t(i - bstart[lo]);
   double d = En[lo] + Ep[g];
-  const uint32_t pm = cmask[g];
-  for (uint32_t w = bmask[lo]; w; w &= w - 1) {
-    const int an = __ffs(w) - 1;
-    for (uint32_t z = pm; z; z &= z - 1) d += Vd[an * np + (__ffs(z) - 1)];
+  const M pm = cmask[g];
+  for (M w = bmask[lo]; w; w &= w - 1) {
+    const int an = lowbit(w);
+    for (M z = pm; z; z &= z - 1) d += Vd[an * np + lowbit(z)];
   }
   diag[i] = d;
 }
 
-template <class T, int VB, int RPT, bool DF, bool TR>
+template <class T, int VB, int RPT, bool DF, bool TR, class M, bool ST>
 void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const VTab<T>& tl, const T* x, void* y,
                 int ldy, int m, int threads, size_t smem, int* err, cudaStream_t s) {
-  auto kern = k_virtual<T, VB, RPT, DF, TR>;
+  auto kern = k_virtual<T, VB, RPT, DF, TR, M, ST>;
   CG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   kern<<<unsigned(a.lmax ? h.virt->nblocks : 0), threads, smem, s>>>(a, tb, tl, x, y, ldy, m, err);
   CG_CUDA(cudaGetLastError());
@@ -506,8 +537,10 @@ void launch_rpt(const Hamiltonian& h, const VArgs& a, const VTab<T>& tb, const V
 VArgs make_args(const VirtualOp& v, const Hamiltonian& h) {
   VArgs a;
   a.nn = v.nn; a.np = v.np; a.ndm = v.ndm; a.dm0 = v.dm0; a.lmax = v.lmax;
-  a.bstart = v.bstart.p; a.blen = v.blen.p; a.bclass = v.bclass.p; a.bmask = v.bmask.p; a.order = v.order.p;
-  a.cstart = v.cstart.p; a.cmask = v.cmask.p;
+  a.bstart = v.bstart.p; a.blen = v.blen.p; a.bclass = v.bclass.p; a.order = v.order.p;
+  a.bmask = v.wide ? static_cast<const void*>(v.bmask64.p) : static_cast<const void*>(v.bmask.p);
+  a.cmask = v.wide ? static_cast<const void*>(v.cmask64.p) : static_cast<const void*>(v.cmask.p);
+  a.cstart = v.cstart.p;
   a.nt_off = v.nt_off.p; a.nt = v.nt.p; a.nn_off = v.nn_off.p; a.nn2 = v.nn2.p;
   a.cslice = v.cslice.p; a.sl_off = v.sl_off.p; a.sl_e = v.sl_e.p; a.pp_off = v.pp_off.p; a.pp_rank = v.pp_rank.p;
   a.diag = h.diag.p;
@@ -532,14 +565,19 @@ void virtual_product(const Hamiltonian& h, const T* x, void* y, int ldy, int m, 
   VArgs a = make_args(v, h);
   const int npp = v.np * v.np;
   const size_t vsz = DF ? 2 * sizeof(float) : sizeof(T);  // bytes of one element value
-  const size_t smem = kVirtualSmemHead + size_t(3) * v.lmax * VB * sizeof(T) + (3 * size_t(npp + 4) + 64) * vsz +
-                      (v.truncated ? 16 + size_t(3) * v.rmax * sizeof(uint16_t) : 0);
-  if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "neutron block too long for the shared-memory staging");
+  // staged: own block, two target blocks (and, with lists, their maps) in
+  // shared memory; blocks too long for that read x and the maps through L2
+  const size_t tabs = (3 * size_t(npp + 4) + 2 * size_t(v.np)) * vsz;
+  const size_t smem_staged = kVirtualSmemHead + size_t(3) * v.lmax * VB * sizeof(T) + tabs +
+                             (v.truncated ? 16 + size_t(3) * v.rmax * sizeof(uint16_t) : 0);
+  const bool staged = smem_staged <= 227 * 1024;
+  const size_t smem = staged ? smem_staged : kVirtualSmemHead + tabs + 16;
+  if (smem > 227 * 1024) throw Error(CG_ERR_UNSUPPORTED, "interaction slices too large for shared memory");
   // rows per thread: threads <= 512, or <= 1024 when the staging buffers
   // leave room for one CTA per SM only (long blocks, e.g. fp 5+5): there two
   // rows per thread and twice the warps hide the shared-memory latency better
   // than four rows per thread
-  const int thread_cap = smem > 113 * 1024 ? 1024 : 512;
+  const int thread_cap = (staged && smem > 113 * 1024) ? 1024 : 512;
   int rpt = 1;
   while ((v.lmax + rpt - 1) / rpt > thread_cap) rpt <<= 1;
   int threads = (v.lmax + rpt - 1) / rpt;
@@ -547,21 +585,28 @@ void virtual_product(const Hamiltonian& h, const T* x, void* y, int ldy, int m, 
   if (rpt > 8) throw Error(CG_ERR_UNSUPPORTED, "neutron block longer than 4096 rows");
   DBuf<int>& err = v.err;
   CG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-  if (v.truncated) {
-    switch (rpt) {
-      case 1: launch_rpt<T, VB, 1, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      case 2: launch_rpt<T, VB, 2, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      case 4: launch_rpt<T, VB, 4, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      default: launch_rpt<T, VB, 8, DF, true>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-    }
-  } else {
-    switch (rpt) {
-      case 1: launch_rpt<T, VB, 1, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      case 2: launch_rpt<T, VB, 2, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      case 4: launch_rpt<T, VB, 4, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-      default: launch_rpt<T, VB, 8, DF, false>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break;
-    }
+#define CG_VIRTUAL_RPT(TRV, MV, STV)                                                                         \
+  switch (rpt) {                                                                                             \
+    case 1: launch_rpt<T, VB, 1, DF, TRV, MV, STV>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break; \
+    case 2: launch_rpt<T, VB, 2, DF, TRV, MV, STV>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break; \
+    case 4: launch_rpt<T, VB, 4, DF, TRV, MV, STV>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break; \
+    default: launch_rpt<T, VB, 8, DF, TRV, MV, STV>(h, a, tb, tl, x, y, ldy, m, threads, smem, err.p, s); break; \
   }
+#define CG_VIRTUAL_ST(TRV, MV)    \
+  if (staged) {                   \
+    CG_VIRTUAL_RPT(TRV, MV, true)  \
+  } else {                        \
+    CG_VIRTUAL_RPT(TRV, MV, false) \
+  }
+  if (v.wide) {
+    CG_VIRTUAL_ST(true, unsigned long long)
+  } else if (v.truncated) {
+    CG_VIRTUAL_ST(true, uint32_t)
+  } else {
+    CG_VIRTUAL_ST(false, uint32_t)
+  }
+#undef CG_VIRTUAL_ST
+#undef CG_VIRTUAL_RPT
   int herr = 0;
   CG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   CG_CUDA(cudaStreamSynchronize(s));
@@ -673,7 +718,6 @@ uint64_t Hamiltonian::device_bytes() const {
 void virtual_build(const System& sys, const Operator& op, const Basis& b, int precision, Hamiltonian& h) {
   if (precision != CG_PREC_FP64 && precision != CG_PREC_FP32)
     throw Error(CG_ERR_ARG, "Hamiltonian precision must be CG_PREC_FP64 or CG_PREC_FP32");
-  refuse_wide(b, "the on-the-fly product");
   auto t_begin = std::chrono::steady_clock::now();
   CG_CUDA(cudaGetDevice(&h.device));
   if (h.device != b.device) throw Error(CG_ERR_ARG, "basis lives on another device");
@@ -684,7 +728,9 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   auto vp = std::make_shared<VirtualOp>();
   VirtualOp& v = *vp;
   const int nn = b.nn, np = b.np, ns = b.ns;
-  if (nn > 32 || np > 32) throw Error(CG_ERR_UNSUPPORTED, "more than 32 m-states per species");
+  const bool wide = b.wide;  // 64-bit species masks (wide.cu); the list machinery below
+  if (nn > 64 || np > 45)
+    throw Error(CG_ERR_UNSUPPORTED, "the on-the-fly product takes at most 64 neutron and 45 proton m-states");
   v.nn = nn;
   v.np = np;
   HostOp H = host_operator(sys, op);
@@ -704,40 +750,72 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   const int nblocks = int(b.h_bstart.size());
   const int nclasses = int(b.h_cstart.size()) - 1;
   v.nblocks = nblocks;
-  v.nconf_p = b.h_cmasks.size();
+  // species masks of block neutrons and list protons
+  auto nmask_of = [&](int beta) -> uint64_t { return wide ? b.h_wbmask[beta] : uint64_t(b.h_bmask[beta]); };
+  auto pmask_of = [&](size_t g) -> uint64_t { return wide ? b.h_wcmask[g] : uint64_t(b.h_cmasks[g]); };
+  const size_t nmembers = wide ? b.h_wcmask.size() : b.h_cmasks.size();
+  v.nconf_p = nmembers;
   std::vector<uint32_t> blen(nblocks), order(nblocks);
   for (int i = 0; i < nblocks; ++i) {
     uint32_t c = b.h_bclass[i];
     blen[i] = b.h_cstart[c + 1] - b.h_cstart[c];
     v.lmax = std::max<int>(v.lmax, int(blen[i]));
   }
-  std::vector<int32_t> block_of(std::max<uint64_t>(b.neut.nconf, 1), -1);
-  for (int i = 0; i < nblocks; ++i) block_of[colex_host(b.h_bmask[i], b.h_binom)] = i;
+  // block of a neutron configuration (-1: not a block of the basis)
+  std::vector<int32_t> block_tab(wide ? 1 : std::max<uint64_t>(b.neut.nconf, 1), -1);
+  std::unordered_map<uint64_t, int32_t> block_map;
+  for (int i = 0; i < nblocks; ++i) {
+    if (wide) block_map[b.h_wbmask[i]] = i;
+    else block_tab[colex_host(b.h_bmask[i], b.h_binom)] = i;
+  }
+  auto block_of = [&](uint64_t nu) -> int32_t {
+    if (!wide) return block_tab[colex_host(nu, b.h_binom)];
+    auto it = block_map.find(nu);
+    return it == block_map.end() ? -1 : it->second;
+  };
+  // rank of a proton configuration in its (2m, parity) class, -1 when the
+  // basis has no such configuration (a wide basis holds only the enumerated ones)
+  std::unordered_map<uint64_t, uint32_t> univ;
+  if (wide)
+    for (size_t i = 0; i < b.h_wpuniv.size(); ++i) univ[b.h_wpuniv[i]] = uint32_t(i);
+  auto class_rank = [&](uint64_t pi) -> int64_t {
+    if (!wide) return b.h_pcrank[colex_host(pi, b.h_binom)];
+    auto it = univ.find(pi);
+    return it == univ.end() ? -1 : int64_t(b.h_wpuniv_rank[it->second]);
+  };
   // truncated basis: the "classes" of the basis are its lists.  Each list
   // member keeps its rank in the untruncated class (b.h_pcrank), and each list
   // a map class rank -> list rank (0xffff: not in the list), padded to 8
   // entries so that every map is a 16-byte bulk copy
-  const bool trunc = b.truncated;
+  const bool trunc = b.truncated || wide;
   std::vector<uint32_t> gcr, lmap_off, lmap_len, g_list;
   std::vector<uint16_t> lmap;
   if (trunc) {
+    // class size of a proton configuration
+    std::function<uint32_t(uint64_t)> class_size;
     std::map<std::pair<int, int>, uint32_t> csize;  // untruncated class sizes by (2m, parity)
-    std::vector<uint32_t> key_of(std::max<uint64_t>(b.prot.nconf, 1), 0);
+    std::vector<uint32_t> key_of;
     std::vector<std::pair<int, int>> keys;
-    for (uint64_t i = 0; i < b.prot.nconf; ++i) {
-      const std::pair<int, int> k{b.prot.lex_m2[i], b.prot.lex_par[i]};
-      if (csize[k]++ == 0) keys.push_back(k);
+    if (wide) {
+      class_size = [&](uint64_t pi) -> uint32_t { return b.h_wpuniv_csize[univ.at(pi)]; };
+    } else {
+      key_of.assign(std::max<uint64_t>(b.prot.nconf, 1), 0);
+      for (uint64_t i = 0; i < b.prot.nconf; ++i) {
+        const std::pair<int, int> k{b.prot.lex_m2[i], b.prot.lex_par[i]};
+        if (csize[k]++ == 0) keys.push_back(k);
+      }
+      std::map<std::pair<int, int>, uint32_t> key_id;
+      for (size_t i = 0; i < keys.size(); ++i) key_id[keys[i]] = uint32_t(i);
+      for (uint64_t i = 0; i < b.prot.nconf; ++i)
+        key_of[colex_host(b.prot.lex_mask[i], b.h_binom)] = key_id[{b.prot.lex_m2[i], b.prot.lex_par[i]}];
+      class_size = [&](uint64_t pi) -> uint32_t { return csize[keys[key_of[colex_host(pi, b.h_binom)]]]; };
     }
-    std::map<std::pair<int, int>, uint32_t> key_id;
-    for (size_t i = 0; i < keys.size(); ++i) key_id[keys[i]] = uint32_t(i);
-    for (uint64_t i = 0; i < b.prot.nconf; ++i)
-      key_of[colex_host(b.prot.lex_mask[i], b.h_binom)] = key_id[{b.prot.lex_m2[i], b.prot.lex_par[i]}];
-    gcr.assign(std::max<size_t>(b.h_cmasks.size(), 1), 0);
-    g_list.assign(std::max<size_t>(b.h_cmasks.size(), 1), 0);
+    gcr.assign(std::max<size_t>(nmembers, 1), 0);
+    g_list.assign(std::max<size_t>(nmembers, 1), 0);
     for (int L = 0; L < nclasses; ++L) {
       const uint32_t g0 = b.h_cstart[L], g1 = b.h_cstart[L + 1];
       uint32_t cs = 0;
-      if (g1 > g0) cs = csize[keys[key_of[colex_host(b.h_cmasks[g0], b.h_binom)]]];
+      if (g1 > g0) cs = class_size(pmask_of(g0));
       if (cs > 0xffff) throw Error(CG_ERR_UNSUPPORTED, "proton class longer than 65535 configurations");
       const uint32_t len = std::max<uint32_t>(8, (cs + 7) / 8 * 8);
       lmap_off.push_back(uint32_t(lmap.size()));
@@ -745,8 +823,9 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
       v.rmax = std::max<int>(v.rmax, int(len));
       lmap.resize(lmap.size() + len, 0xffff);
       for (uint32_t g = g0; g < g1; ++g) {
-        const uint32_t r = b.h_pcrank[colex_host(b.h_cmasks[g], b.h_binom)];
-        if (r >= cs) throw Error(CG_ERR_INTERNAL, "list member outside its class");
+        const int64_t rr = class_rank(pmask_of(g));
+        const uint32_t r = uint32_t(rr);
+        if (rr < 0 || r >= cs) throw Error(CG_ERR_INTERNAL, "list member outside its class");
         gcr[g] = r;
         g_list[g] = uint32_t(L);
         lmap[lmap_off[L] + r] = uint16_t(g - g0);
@@ -755,6 +834,7 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
     if (lmap.size() >= (1ull << 32)) throw Error(CG_ERR_UNSUPPORTED, "class-to-list maps beyond 2^32 entries");
   }
   v.truncated = trunc;
+  v.wide = wide;
   const uint64_t nall = nn == 64 ? ~0ull : ((1ull << nn) - 1);
   const uint64_t pall_local = np == 64 ? ~0ull : ((1ull << np) - 1);
   const auto& m2 = b.sp_m2;
@@ -765,7 +845,7 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   std::vector<VPair> nn2;
   std::vector<double> En(nblocks, 0.0);
   for (int beta = 0; beta < nblocks; ++beta) {
-    const uint64_t nu = b.h_bmask[beta];
+    const uint64_t nu = nmask_of(beta);
     const uint64_t holes = ~nu & nall;
     double e = 0;
     for (uint64_t t = nu; t; t &= t - 1) {
@@ -785,7 +865,7 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
       for (uint64_t w = holes; w; w &= w - 1) {
         const int c = __builtin_ctzll(w);
         const uint64_t nu2 = nu ^ (1ull << a) ^ (1ull << c);
-        const int tb = block_of[colex_host(nu2, b.h_binom)];
+        const int tb = block_of(nu2);
         if (tb < 0) continue;
         NTrans tr{};
         tr.target = uint32_t(tb);
@@ -818,7 +898,7 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
             const int d = __builtin_ctzll(z);
             if (m2[a] + m2[bb] != m2[c] + m2[d] || (par[a] ^ par[bb] ^ par[c] ^ par[d])) continue;
             const uint64_t K = nu ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
-            const int tb = block_of[colex_host(K, b.h_binom)];
+            const int tb = block_of(K);
             if (tb < 0) {
               if (trunc) continue;  // the target block is outside the truncated basis
               throw Error(CG_ERR_INTERNAL, "two-neutron move leaves the basis");
@@ -836,16 +916,16 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   }
 
   // proton transitions (grouped by 2m change) and PP2 per proton configuration
-  const uint64_t npc = b.h_cmasks.size();
+  const uint64_t npc = nmembers;
   std::vector<uint32_t> pt_off(npc * v.ndm + 1, 0), pp_off(npc + 1, 0);
   std::vector<uint2> pt;
   std::vector<double> pt_c, Ep(npc, 0.0);
   std::vector<VPair> pp2;
   std::vector<std::vector<std::pair<uint2, double>>> bydm(v.ndm);
   for (uint64_t g = 0; g < npc; ++g) {
-    const uint64_t pi = b.h_cmasks[g];
+    const uint64_t pi = pmask_of(g);
     const uint64_t holes = ~pi & pall_local;
-    const uint64_t P = pi << nn;  // global bits
+    const G P = G(pi) << nn;  // global bits
     double e = 0;
     for (uint64_t t = pi; t; t &= t - 1) {
       int q = nn + __builtin_ctzll(t);
@@ -865,7 +945,9 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
       for (uint64_t w = holes; w; w &= w - 1) {
         const int dl = __builtin_ctzll(w);
         const uint64_t pi2 = pi ^ (1ull << bl) ^ (1ull << dl);
-        const uint32_t rank = b.h_pcrank[colex_host(pi2, b.h_binom)];
+        const int64_t crank = class_rank(pi2);
+        if (crank < 0) continue;  // a configuration no list of the basis holds
+        const uint32_t rank = uint32_t(crank);
         const int bg = nn + bl, dg = nn + dl;
         const int sign = move_sign(pi, bl, dl);
         uint2 q;
@@ -874,10 +956,10 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
         double cp = 0.0;
         if (dmi_of(bg, dg) == v.dm0) {
           const int x = std::min(bg, dg), yy = std::max(bg, dg);
-          const uint64_t S0 = bl < dl ? P : (pi2 << nn);
+          const G S0 = bl < dl ? P : (G(pi2) << nn);
           cp = H.term1(S0, x, yy);
-          for (uint64_t z = P & ~(1ull << bg); z; z &= z - 1) {
-            const int sc = __builtin_ctzll(z);
+          for (G z = P & ~gbit(bg); z; z &= z - 1) {
+            const int sc = ctzg(z);
             cp += H.term2(S0, std::min(x, sc), std::max(x, sc), std::min(yy, sc), std::max(yy, sc));
           }
         }
@@ -900,11 +982,13 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
           for (uint64_t z = holes & ~below_h(c - nn + 1); z; z &= z - 1) {
             const int d = nn + __builtin_ctzll(z);
             if (m2[a] + m2[bb] != m2[c] + m2[d] || (par[a] ^ par[bb] ^ par[c] ^ par[d])) continue;
-            const uint64_t K = P ^ (1ull << a) ^ (1ull << bb) ^ (1ull << c) ^ (1ull << d);
+            const G K = P ^ gbit(a) ^ gbit(bb) ^ gbit(c) ^ gbit(d);
             const bool fwd = (a < c) || (a == c && bb < d);
             const double val = fwd ? H.term2(P, a, bb, c, d) : H.term2(K, c, d, a, bb);
             // rank in the own block's list (the class; truncated: skip targets outside the list)
-            uint32_t rank = b.h_pcrank[colex_host(K >> nn, b.h_binom)];
+            const int64_t crank = class_rank(uint64_t(K >> nn));
+            if (crank < 0) continue;
+            uint32_t rank = uint32_t(crank);
             if (trunc) {
               rank = lmap[lmap_off[g_list[g]] + rank];
               if (rank == 0xffff) continue;
@@ -1036,10 +1120,20 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
   v.bstart.upload(b.h_bstart, s);
   v.blen.upload(blen, s);
   v.bclass.upload(b.h_bclass, s);
-  v.bmask.upload(b.h_bmask, s);
+  if (wide) {
+    v.bmask64.upload(b.h_wbmask, s);
+    v.bmask.alloc(1);
+  } else {
+    v.bmask.upload(b.h_bmask, s);
+  }
   v.order.upload(order, s);
   v.cstart.upload(b.h_cstart, s);
-  v.cmask.upload(b.h_cmasks, s);
+  if (wide) {
+    v.cmask64.upload(b.h_wcmask, s);
+    v.cmask.alloc(1);
+  } else {
+    v.cmask.upload(b.h_cmasks, s);
+  }
   v.nt_off.upload(nt_off, s);
   v.nt.upload(nt, s);
   v.nn_off.upload(nn_off, s);
@@ -1083,9 +1177,14 @@ void virtual_build(const System& sys, const Operator& op, const Basis& b, int pr
     dEn.upload(En, s);
     dEp.upload(Ep, s);
     dVd.upload(Vd, s);
-    k_virtual_diag<<<unsigned((b.n + 255) / 256), 256, 0, s>>>(b.n, nblocks, v.bstart.p, v.bclass.p, v.bmask.p,
-                                                               v.cstart.p, v.cmask.p, dEn.p, dEp.p, dVd.p, np,
-                                                               h.diag.p);
+    const unsigned gd = unsigned((b.n + 255) / 256);
+    if (wide)
+      k_virtual_diag<unsigned long long><<<gd, 256, 0, s>>>(
+          b.n, nblocks, v.bstart.p, v.bclass.p, reinterpret_cast<const unsigned long long*>(v.bmask64.p), v.cstart.p,
+          reinterpret_cast<const unsigned long long*>(v.cmask64.p), dEn.p, dEp.p, dVd.p, np, h.diag.p);
+    else
+      k_virtual_diag<uint32_t><<<gd, 256, 0, s>>>(b.n, nblocks, v.bstart.p, v.bclass.p, v.bmask.p, v.cstart.p,
+                                                  v.cmask.p, dEn.p, dEp.p, dVd.p, np, h.diag.p);
     CG_CUDA(cudaGetLastError());
     count_launch();
     CG_CUDA(cudaStreamSynchronize(s));

@@ -75,6 +75,8 @@ struct VirtualOp {
   // truncated basis: rows of a block are a list (allowed proton configurations of its class);
   // proton-transition tables hold class ranks, mapped to list ranks by lmap (0xffff: outside)
   bool truncated = false;
+  bool wide = false;                                // 64-bit species masks (bmask64, cmask64)
+  DBuf<uint64_t> bmask64, cmask64;
   int rmax = 0;                                     // longest map (entries, a multiple of 8)
   DBuf<uint32_t> gcr;                               // nconf_p: class rank of each list member
   DBuf<uint16_t> lmap;                              // per list: class rank -> list rank
@@ -86,7 +88,8 @@ struct VirtualOp {
            sl_off.bytes() + sl_e.bytes() + sl_c.bytes() + sl_cf.bytes() + pp_off.bytes() + pp_rank.bytes() +
            pp_h.bytes() + pp_hf.bytes() + W.bytes() + Un.bytes() + Up.bytes() +
            Wf.bytes() + Unf.bytes() + Upf.bytes() + Wl.bytes() + Unl.bytes() + Upl.bytes() + sl_cl.bytes() +
-           pp_hl.bytes() + gcr.bytes() + lmap.bytes() + lmap_off.bytes() + lmap_len.bytes();
+           pp_hl.bytes() + gcr.bytes() + lmap.bytes() + lmap_off.bytes() + lmap_len.bytes() + bmask64.bytes() +
+           cmask64.bytes();
   }
 };
 

@@ -575,6 +575,14 @@ void basis_build_wide(const System& sys, Basis& b) {
   // proton classes by (2m, parity), lexicographic inside
   std::map<std::pair<int, int>, std::vector<uint32_t>> cls;
   for (size_t i = 0; i < ep.mask.size(); ++i) cls[{ep.msum[i], ep.psum[i]}].push_back(uint32_t(i));
+  b.h_wpuniv = ep.mask;
+  b.h_wpuniv_rank.assign(ep.mask.size(), 0);
+  b.h_wpuniv_csize.assign(ep.mask.size(), 0);
+  for (auto& kv : cls)
+    for (size_t r = 0; r < kv.second.size(); ++r) {
+      b.h_wpuniv_rank[kv.second[r]] = uint32_t(r);
+      b.h_wpuniv_csize[kv.second[r]] = uint32_t(kv.second.size());
+    }
   // neutron blocks in lexicographic order, each with its list of allowed
   // proton configurations (the class itself when nothing is truncated)
   std::map<std::vector<int>, uint32_t> list_id;

@@ -180,13 +180,48 @@ def test_wide_jt_of_reference_vectors(gpu_available, tmp_path):
 
 
 @pytest.mark.gpu
-def test_wide_refused_routes(gpu_available, tmp_path):
+@pytest.mark.parametrize("name", CASES)
+def test_wide_on_the_fly_matches_stored(gpu_available, name, tmp_path):
+    """The on-the-fly product of a wide basis (64-bit species masks, the
+    class-to-list maps of the truncated tables) equals the stored matrix's:
+    diagonal within 1e-12, FP64 and double-float within 1e-11 of max |y|,
+    FP32 within 1e-5."""
     import cosmo_gb300 as cg
-    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    p = cg.Problem(W.write_case(str(tmp_path), name))
     b = cg.ManyBodyStates(p)
-    with pytest.raises(cg.CosmoError) as e:
-        cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
-    assert e.value.status == -6  # CG_ERR_UNSUPPORTED
+    hs = cg.Hamiltonian(p, b, cg.CG_PREC_FP64)
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP64, virtual=True)
+    assert hv.virtual
+    np.testing.assert_allclose(hv.diagonal(), hs.diagonal(), rtol=0, atol=1e-12)
+    for m in (1, 5, 8):
+        x = np.random.default_rng(m).standard_normal((b.n, m))
+        ys = hs.times_matrix(x)
+        scale = np.abs(ys).max()
+        np.testing.assert_allclose(hv.times_matrix(x), ys, rtol=0, atol=1e-11 * scale)
+        np.testing.assert_allclose(hv.times_matrix(x, cg.CG_PREC_FP32), ys, rtol=0, atol=1e-5 * scale)
+        np.testing.assert_allclose(hv.times_matrix(x, cg.CG_PREC_REFINE), ys, rtol=0, atol=1e-11 * scale)
+
+
+@pytest.mark.gpu
+def test_wide_on_the_fly_davidson_and_forced(gpu_available, tmp_path):
+    """Mixed Davidson on the wide on-the-fly product reaches the reference's
+    1 hw eigenvalues; forced on bitstring-sized systems the wide on-the-fly
+    product equals the bitstring one's."""
+    import cosmo_gb300 as cg
+    g = golden("spsdpf_1hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_1hw"))
+    b = cg.ManyBodyStates(p)
+    hv = cg.Hamiltonian(p, b, cg.CG_PREC_FP32, virtual=True)
+    r = cg.davidson_diagonalization(hv, 5, precision=cg.CG_PREC_FP32, tol_resid=1e-6, block=5, lim=40)
+    assert r.stats.converged == 5
+    np.testing.assert_allclose(r.eig, g["ref_eig"][:5], rtol=0, atol=1e-6)
+    for name, pp in _narrow_cases(str(tmp_path)):
+        bn, bw = cg.ManyBodyStates(pp), cg.ManyBodyStates(pp, wide=True)
+        hn = cg.Hamiltonian(pp, bn, cg.CG_PREC_FP64, virtual=True)
+        hw = cg.Hamiltonian(pp, bw, cg.CG_PREC_FP64, virtual=True)
+        x = np.random.default_rng(3).standard_normal((bn.n, 8))
+        yn = hn.times_matrix(x)
+        np.testing.assert_allclose(hw.times_matrix(x), yn, rtol=0, atol=1e-11 * np.abs(yn).max(), err_msg=name)
 
 
 def _narrow_cases(tmp):
