@@ -115,9 +115,9 @@ cg_status cg_basis_build(const cg_problem* p, cg_basis** out);
  * 2^26 configurations is refused), determinants as pairs of 64-bit species
  * masks located by binary search (SM::locate, include/sm/ManyBodyStates.cxx:
  * 92-130).  Same order, .mbs bytes, stored Hamiltonian, Davidson, <J-J+> /
- * <T-T+>, occupations, XSHLSF / XSHLEMB amplitudes and batched solves as the
- * bitstring basis; the on-the-fly product refuses it (CG_ERR_UNSUPPORTED).  cg_basis_build_wide builds that representation for
- * any system (the two agree on every system both take). */
+ * <T-T+>, occupations, XSHLSF / XSHLEMB amplitudes, batched solves and the
+ * on-the-fly product as the bitstring basis.  cg_basis_build_wide builds that
+ * representation for any system (the two agree on every system both take). */
 cg_status cg_basis_build_wide(const cg_problem* p, cg_basis** out);
 cg_status cg_basis_is_wide(const cg_basis* b, int32_t* wide);
 void cg_basis_destroy(cg_basis* b);
