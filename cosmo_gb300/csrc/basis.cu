@@ -351,9 +351,4 @@ uint64_t basis_locate_host(const Basis& b, const uint16_t* t) {
   return no + b.h_pcrank[colex_host(pmask, b.h_binom)];
 }
 
-void refuse_wide(const Basis& b, const char* route) {
-  if (b.wide)
-    throw Error(CG_ERR_UNSUPPORTED, std::string(route) + " takes valence spaces of at most 32 m-states per species");
-}
-
 }  // namespace cg

@@ -142,8 +142,6 @@ void wide_onebody_partials(const Basis& parent, const Basis& daughter, const dou
                            unsigned grid, int* err, cudaStream_t s);
 void wide_sf_partials(const Basis& parent, const Basis& daughter, const double* psid, int nq, const double* psip,
                       const int* sidx, int nsidx, double* part, unsigned grid, int* err, cudaStream_t s);
-// refuses a wide basis on a route that only takes bitstring bases
-void refuse_wide(const Basis& b, const char* route);
 uint64_t colex_host(uint64_t mask, const std::vector<uint64_t>& binom);
 
 // <J-J+> = ||J+ psi||^2 and <T-T+> = ||T+ psi||^2 of nst host vectors (state k at vecs + k*n).
