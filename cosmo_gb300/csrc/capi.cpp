@@ -116,8 +116,10 @@ cg_status cg_problem_create(const cg_problem_desc* d, cg_problem** out) {
     CG_NOT_NULL(d);
     CG_NOT_NULL(out);
     *out = nullptr;
-    if (d->n_sps < 1 || d->n_sps > 64 || d->n_neutron_sps < 0 || d->n_neutron_sps > d->n_sps)
+    if (d->n_sps < 1 || d->n_neutron_sps < 0 || d->n_neutron_sps > d->n_sps)
       throw cg::Error(CG_ERR_ARG, "bad s.p. table size");
+    if (d->n_neutron_sps > 64 || d->n_sps - d->n_neutron_sps > 64)
+      throw cg::Error(CG_ERR_UNSUPPORTED, "more than 64 m-scheme s.p. states per species");
     CG_NOT_NULL(d->sps);
     if (d->nv < 0 || d->zv < 0) throw cg::Error(CG_ERR_ARG, "negative particle number");
     auto p = std::make_unique<cg_problem>();

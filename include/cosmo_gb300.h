@@ -74,8 +74,8 @@ cg_status cg_problem_load_xml(const char* xml_path, const char* system_name, cg_
 /* A problem from explicit operator terms, as SM::PPMatrix is assembled from
  * any set of MBOperator components (include/sm/PPMatrix.cxx:42-60, pushed in
  * include/xsm/DEXHVcsb.cxx:47-49).  sps: n_sps rows of 8 int32 in the layout of
- * cg_problem_sps (neutron states first); keys are forward ordered as in
- * cg_problem_one_body / cg_problem_two_body. */
+ * cg_problem_sps (neutron states first, at most 64 per species); keys are
+ * forward ordered as in cg_problem_one_body / cg_problem_two_body. */
 typedef struct {
   int32_t n_sps, n_neutron_sps;
   const int32_t* sps;

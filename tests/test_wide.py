@@ -79,6 +79,26 @@ def test_wide_operator_terms_match_reference(tmp_path):
     np.testing.assert_allclose(v2, g["vspx_vals"], rtol=0, atol=1e-13)
 
 
+def test_wide_problem_from_terms(tmp_path):
+    """A problem built from an explicit 80-state table and operator terms
+    (cg_problem_create) holds them unchanged; more than 64 states in a
+    species is refused."""
+    import cosmo_gb300 as cg
+    g = golden("spsdpf_0hw")
+    p = cg.Problem(W.write_case(str(tmp_path), "spsdpf_0hw"))
+    k1, v1 = p.one_body()
+    k2, v2 = p.two_body()
+    q = cg.Problem.from_terms(p.sps(), 40, 20, 13, 1, 0, k1, v1, k2, v2)
+    assert q.info.n_sps == 80 and np.array_equal(q.sps(), g["sps"])
+    r1, w1 = q.one_body()
+    r2, w2 = q.two_body()
+    assert np.array_equal(r1, k1) and np.array_equal(w1, v1)
+    assert np.array_equal(r2, k2) and np.array_equal(w2, v2)
+    big = np.concatenate([p.sps()[:40]] * 2)  # 80 neutron states
+    with pytest.raises(cg.CosmoError):
+        cg.Problem.from_terms(big, 80, 2, 0, 0, 0, k1[:0], v1[:0], k2[:0], v2[:0])
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", CASES)
 def test_wide_basis_matches_reference(gpu_available, name, tmp_path):
